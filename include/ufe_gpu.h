@@ -1,0 +1,269 @@
+/*
+ * ufe_gpu.h -- C ABI of the GB300 velocity solver for UFEMISM 2.0.
+ *
+ * The library replaces, behind plain C calls, the part of UFEMISM's ice-dynamics step that
+ * computes velocities: the SSA/DIVA Picard loop with its stiffness-matrix assembly and Krylov
+ * solve, the mesh CSR operators that loop applies, and the CSR matrix-equation solve that the
+ * reference hands to PETSc.  A Fortran caller binds these entry points with ISO_C_BINDING.
+ *
+ * Conventions
+ *   - Every array is a host array in the layout UFEMISM's derived types hold it: 2-D arrays are
+ *     column-major (Fortran order), mesh connectivity is 1-based with 0 meaning "none".
+ *   - CSR matrices follow type_sparse_matrix_CSR_dp (src/UPSY/basic/CSR_sparse_matrix_type.f90:15-38):
+ *     ptr(m+1), ind(nnz), val(nnz); `index_base` says whether ptr/ind are 0- or 1-based.
+ *   - Every call returns an int32 status: 0 ok, >0 a warning (the result is usable), <0 an error.
+ *     ufe_ctx_last_error() returns the message of the last failure on a context.
+ *   - One host thread per context.  Calls are synchronous: work runs on the context's own CUDA
+ *     stream and the call returns after the results are in the caller's buffers.
+ *   - No entry point falls back to the CPU.  A context that cannot reach a GB300-class device
+ *     (sm_103) fails at ufe_ctx_create.
+ */
+#ifndef UFE_GPU_H
+#define UFE_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes -------------------------------------------------------------------------- */
+#define UFE_OK                    0
+#define UFE_WARN_PICARD_MAXIT     1   /* viscosity iteration hit visc_it_nit (SSA_main.f90:229-232) */
+#define UFE_WARN_KRYLOV_MAXIT     2   /* a Krylov solve stopped at krylov_max_it before the tolerance */
+#define UFE_ERR_INVALID          -1   /* bad argument or missing setup step */
+#define UFE_ERR_NAN              -2   /* NaN/Inf in a result or an input */
+#define UFE_ERR_DIVERGED         -3   /* Picard divergence limits (SSA_main.f90:207-213) or Krylov breakdown */
+#define UFE_ERR_THERMO_UNSTABLE  -4   /* more than 1% unstable columns (thermodynamics_3D_heat_equation.f90:255-290) */
+#define UFE_ERR_DEVICE           -5   /* CUDA error, or no sm_103 device */
+#define UFE_ERR_CAPACITY         -6   /* an output buffer is too small, or a mesh exceeds a built-in limit */
+
+typedef struct ufe_ctx ufe_ctx;
+
+/* ---- mesh ---------------------------------------------------------------------------------- */
+/* The arrays of type_mesh (src/UPSY/types/mesh_types.f90:57-97) that the velocity solve reads. */
+typedef struct {
+  int32_t nV, nTri, nC_mem, nz;
+  const double  *V;      /* nV x 2                                                  */
+  const int32_t *nC;     /* nV                                                      */
+  const int32_t *C;      /* nV x nC_mem, counter-clockwise, edge to edge on borders */
+  const int32_t *niTri;  /* nV                                                      */
+  const int32_t *iTri;   /* nV x nC_mem, counter-clockwise                          */
+  const int32_t *VBI;    /* nV, 0..8                                                */
+  const int32_t *Tri;    /* nTri x 3, counter-clockwise                             */
+  const int32_t *TriC;   /* nTri x 3, neighbour across from vertex n (0 = none)     */
+  const int32_t *TriBI;  /* nTri, 0..8                                              */
+  const double  *TriGC;  /* nTri x 2, geometric centres                             */
+  const double  *zeta;   /* nz, scaled vertical coordinate (0 = surface, 1 = base)  */
+} ufe_mesh_desc;
+
+/* Matrix operators of type_mesh (mesh_types.f90:212-231). */
+enum ufe_operator {
+  UFE_OP_MAP_A_B = 0,  /* M_map_a_b    nTri x nV   */
+  UFE_OP_DDX_A_B,      /* M_ddx_a_b                */
+  UFE_OP_DDY_A_B,      /* M_ddy_a_b                */
+  UFE_OP_MAP_B_A,      /* M_map_b_a    nV x nTri   */
+  UFE_OP_DDX_B_A,      /* M_ddx_b_a                */
+  UFE_OP_DDY_B_A,      /* M_ddy_b_a                */
+  UFE_OP_DDX_A_A,      /* M_ddx_a_a    nV x nV     */
+  UFE_OP_DDY_A_A,      /* M_ddy_a_a                */
+  UFE_OP_M2_DDX_B_B,   /* M2_ddx_b_b   nTri x nTri */
+  UFE_OP_M2_DDY_B_B,   /* M2_ddy_b_b               */
+  UFE_OP_M2_D2DX2_B_B, /* M2_d2dx2_b_b             */
+  UFE_OP_M2_D2DXDY_B_B,/* M2_d2dxdy_b_b            */
+  UFE_OP_M2_D2DY2_B_B, /* M2_d2dy2_b_b             */
+  UFE_OP_COUNT
+};
+
+/* ---- solver configuration ------------------------------------------------------------------ */
+enum ufe_sliding_law {      /* choice_sliding_law (sliding_laws.f90:25-81) */
+  UFE_SLIDING_NO_SLIDING = 0,
+  UFE_SLIDING_WEERTMAN   = 1,
+  UFE_SLIDING_COULOMB    = 2,
+  UFE_SLIDING_BUDD       = 3,
+  UFE_SLIDING_TSAI2015   = 4,
+  UFE_SLIDING_SCHOOF2005 = 5
+};
+enum ufe_bc {               /* BC_{u,v}_{west,east,south,north} (solve_linearised_SSA_DIVA.f90:481-641) */
+  UFE_BC_INFINITE = 0,
+  UFE_BC_ZERO     = 1
+};
+enum ufe_precision {
+  UFE_PREC_FP64       = 0,  /* FP64 everywhere                                              */
+  UFE_PREC_FP32_REFINE = 1  /* FP32 Krylov (matrix, vectors, preconditioner), FP64 residual
+                               recomputation and iterative refinement to the same tolerance   */
+};
+enum ufe_initial_guess {
+  UFE_X0_ZERO    = 0,       /* every Krylov solve starts from x = 0, as PETSc does by default  */
+  UFE_X0_CURRENT = 1        /* start from the current Picard iterate                          */
+};
+
+/* Scalars of model_configuration.f90 that the velocity solve reads (names without _config). */
+typedef struct {
+  int32_t choice_sliding_law;             /* enum ufe_sliding_law                           */
+  int32_t do_include_SSADIVA_crossterms;  /* :276, default 1                                */
+  int32_t do_GL_subgrid_friction;         /* :340, default 1                                */
+  int32_t BC_u_west, BC_u_east, BC_u_south, BC_u_north;   /* :316-323, default infinite   */
+  int32_t BC_v_west, BC_v_east, BC_v_south, BC_v_north;
+  int32_t visc_it_nit;                    /* :308, default 50                               */
+  double  visc_it_norm_dUV_tol;           /* :307, default 5e-5                             */
+  double  visc_it_relax;                  /* :309, default 0.2                              */
+  double  visc_eff_min;                   /* :310, default 1e4                              */
+  double  vel_max;                        /* :311, default 5000                             */
+  double  stress_balance_PETSc_rtol;      /* :312, default 1e-7                             */
+  double  stress_balance_PETSc_abstol;    /* :313, default 1e-5                             */
+  double  Glens_flow_law_exponent;        /* :591, default 3                                */
+  double  Glens_flow_law_epsilon_sq_0;    /* :592, default 1e-8                             */
+  double  slid_Weertman_m;                /* :333, default 3                                */
+  double  slid_Budd_q_plastic;            /* :334, default 0.3                              */
+  double  slid_Budd_u_threshold;          /* :335, default 100                              */
+  double  subgrid_friction_exponent_on_B_grid; /* :345, default 2                           */
+  double  slid_beta_max;                  /* :348, default 1e20                             */
+  double  slid_delta_v;                   /* :349, default 1e-3                             */
+  /* Krylov controls of this library (PETSc takes them from its runtime options) */
+  int32_t krylov_max_it;                  /* default 10000 (PETSc's default max_it)          */
+  int32_t krylov_initial_guess;           /* enum ufe_initial_guess, default UFE_X0_CURRENT  */
+  int32_t precision;                      /* enum ufe_precision, default UFE_PREC_FP64       */
+  double  krylov_inner_rtol;              /* FP32 inner-solve reduction per refinement step, default 1e-4 */
+  int32_t reserved[8];
+} ufe_solver_params;
+
+/* Fields of type_ice_model / type_bed_roughness_model that the velocity solve reads.
+ * Bed-roughness fields are taken after any A-grid grounded-fraction scaling
+ * (apply_grounded_fractions_to_bed_roughness, sliding_laws.f90:573-641; off by default). */
+typedef struct {
+  const double  *Hi;                  /* nV       ice thickness [m]                          */
+  const double  *Hs;                  /* nV       surface elevation [m]                      */
+  const double  *A_flow;              /* nV x nz  Glen flow factor [Pa^-n yr^-1]             */
+  const double  *fraction_gr_b;       /* nTri     sub-grid grounded fraction on triangles    */
+  const int32_t *mask_grounded_ice;   /* nV       0/1                                        */
+  const double  *beta_sq;             /* nV       Weertman/Tsai/Schoof roughness (or NULL)   */
+  const double  *alpha_sq;            /* nV       Tsai/Schoof Coulomb coefficient (or NULL)  */
+  const double  *effective_pressure;  /* nV       [Pa] (Tsai/Schoof; or NULL)                */
+  const double  *till_yield_stress;   /* nV       [Pa] (Coulomb/Budd, already extended; or NULL) */
+} ufe_ice_state;
+
+/* Prescribed-velocity boundary condition (solve_SSA optional arguments); all NULL = none. */
+typedef struct {
+  const int32_t *mask_b;  /* nTri, 1 = velocity prescribed */
+  const double  *u_b;     /* nTri */
+  const double  *v_b;     /* nTri */
+} ufe_bc_prescribed;
+
+/* State of type_ice_velocity_solver_DIVA (ice_model_types.f90:63-109) carried between solves. */
+typedef struct {
+  double *u_vav_b, *v_vav_b;    /* nTri       in/out: vertically averaged velocity          */
+  double *u_base_b, *v_base_b;  /* nTri       in/out: basal velocity                        */
+  double *tau_bx_b, *tau_by_b;  /* nTri       in/out: basal shear stress                    */
+  double *eta_3D_b;             /* nTri x nz  in/out: effective viscosity on triangles      */
+  double *u_3D_b, *v_3D_b;      /* nTri x nz  out:    3-D velocity (NULL to skip)            */
+} ufe_diva_state;
+
+typedef struct {
+  int32_t n_visc_its;       /* Picard iterations                                          */
+  int32_t n_Axb_its;        /* Krylov iterations summed over the Picard iterations        */
+  int32_t n_refinements;    /* FP64 refinement steps (UFE_PREC_FP32_REFINE)               */
+  int32_t status;           /* same value the call returns                               */
+  double  L2_uv;            /* last Picard change norm (calc_L2_norm_uv)                  */
+  double  visc_it_relax_applied;
+  double  device_ms;        /* device time of the solve                                   */
+  int32_t reserved[6];
+} ufe_solve_stats;
+
+/* ---- context ------------------------------------------------------------------------------- */
+void        ufe_default_params(ufe_solver_params *p);
+int32_t     ufe_ctx_create(int32_t device, ufe_ctx **out);
+void        ufe_ctx_destroy(ufe_ctx *ctx);
+const char *ufe_ctx_last_error(const ufe_ctx *ctx);
+int32_t     ufe_ctx_get_stream(ufe_ctx *ctx, void **cuda_stream);   /* the context's cudaStream_t */
+int32_t     ufe_ctx_synchronize(ufe_ctx *ctx);
+
+/* ---- mesh and operators -------------------------------------------------------------------- */
+/* Copy a mesh to the device.  Replaces calc_all_secondary_mesh_data's role as the source of the
+ * arrays the solver needs; builds the row translation tables tiuv2n/n2tiuv implicitly
+ * (mesh_translation_tables.f90:187-197: row = 2(ti-1)+uv). */
+int32_t ufe_mesh_upload(ufe_ctx *ctx, const ufe_mesh_desc *mesh);
+
+/* Build every operator of enum ufe_operator on the GPU (calc_all_matrix_operators_mesh,
+ * mesh_disc_calc_matrix_operators_2D.f90:26-59, minus the 1st-order b_b pair). */
+int32_t ufe_mesh_build_operators(ufe_ctx *ctx);
+
+/* Install a caller-built operator instead (the Fortran mesh%M_* matrix). */
+int32_t ufe_mesh_set_operator(ufe_ctx *ctx, int32_t op, int32_t m, int32_t n, int64_t nnz,
+                              const int32_t *ptr, const int32_t *ind, const double *val,
+                              int32_t index_base);
+
+int32_t ufe_operator_info(ufe_ctx *ctx, int32_t op, int32_t *m, int32_t *n, int64_t *nnz);
+/* Copy an operator back in CSR form (ptr m+1, ind/val nnz) with the requested index base. */
+int32_t ufe_operator_export(ufe_ctx *ctx, int32_t op, int32_t *ptr, int32_t *ind, double *val,
+                            int32_t index_base);
+
+/* map_a_b_2D/3D, ddx_a_b_2D/3D, ..., ddy_b_a_2D/3D (mesh_disc_apply_operators.f90:18-431):
+ * y(:,k) = M_op x(:,k) for k = 1..ncols, column-major x (n x ncols) and y (m x ncols). */
+int32_t ufe_apply_operator(ufe_ctx *ctx, int32_t op, const double *x, double *y, int32_t ncols);
+
+/* ---- CSR algebra (caller-supplied matrices) ------------------------------------------------ */
+/* multiply_CSR_matrix_with_vector_1D/2D (CSR_matrix_vector_multiplication.f90:198-364). */
+int32_t ufe_csr_spmv(ufe_ctx *ctx, int32_t m, int32_t n, int64_t nnz, const int32_t *ptr,
+                     const int32_t *ind, const double *val, int32_t index_base,
+                     const double *x, double *y, int32_t ncols);
+
+/* solve_matrix_equation_CSR_PETSc (petsc_basic.f90:32-64): Jacobi-preconditioned BiCGStab in the
+ * form of PETSc's KSPBCGS with left preconditioning; converged when the preconditioned residual
+ * norm is <= max(rtol * ||D^-1 b||, abstol).  xx is the initial guess on entry (pass zeros to
+ * reproduce PETSc's default zero guess) and the solution on exit. */
+int32_t ufe_solve_csr(ufe_ctx *ctx, int32_t m, int64_t nnz, const int32_t *ptr, const int32_t *ind,
+                      const double *val, int32_t index_base, const double *bb, double *xx,
+                      double rtol, double abstol, int32_t max_it, int32_t *n_Axb_its);
+
+/* ---- linearised SSA/DIVA ------------------------------------------------------------------- */
+/* The stiffness matrix and load vector of solve_SSA_DIVA_linearised
+ * (solve_linearised_SSA_DIVA.f90:58-153), exported in the reference's own CSR layout: rows
+ * 2(ti-1)+uv, entries in the order add_entry_CSR_dist appends them, 1-based.  `cap` is the
+ * capacity of ind/val; *nnz_out receives the entry count. */
+int32_t ufe_assemble_linearised(ufe_ctx *ctx, const ufe_solver_params *p,
+                                const double *N_b, const double *dN_dx_b, const double *dN_dy_b,
+                                const double *basal_friction_coefficient_b,
+                                const double *tau_dx_b, const double *tau_dy_b,
+                                const double *u_b_prev, const double *v_b_prev,
+                                const ufe_bc_prescribed *bc,
+                                int32_t *ptr, int32_t *ind, double *val, double *bb,
+                                int64_t cap, int64_t *nnz_out);
+
+/* solve_SSA_DIVA_linearised (solve_linearised_SSA_DIVA.f90:23-178): u_b/v_b are the current
+ * solution on entry (initial guess under UFE_X0_CURRENT) and the new solution on exit;
+ * u_b_prev/v_b_prev receive the entry values, as gather_to_all does at :54-55. */
+int32_t ufe_solve_linearised(ufe_ctx *ctx, const ufe_solver_params *p,
+                             double *u_b, double *v_b,
+                             const double *N_b, const double *dN_dx_b, const double *dN_dy_b,
+                             const double *basal_friction_coefficient_b,
+                             const double *tau_dx_b, const double *tau_dy_b,
+                             double *u_b_prev, double *v_b_prev,
+                             const ufe_bc_prescribed *bc, int32_t *n_Axb_its);
+
+/* ---- full velocity solves ------------------------------------------------------------------ */
+/* solve_SSA (SSA_main.f90:87-242): u_b/v_b in/out (warm start in, solution out). */
+int32_t ufe_solve_ssa(ufe_ctx *ctx, const ufe_solver_params *p, const ufe_ice_state *ice,
+                      const ufe_bc_prescribed *bc, double *u_b, double *v_b,
+                      int32_t *n_visc_its, int32_t *n_Axb_its, ufe_solve_stats *stats);
+
+/* solve_DIVA (DIVA_main.f90:88-262). */
+int32_t ufe_solve_diva(ufe_ctx *ctx, const ufe_solver_params *p, const ufe_ice_state *ice,
+                       const ufe_bc_prescribed *bc, ufe_diva_state *st,
+                       int32_t *n_visc_its, int32_t *n_Axb_its, ufe_solve_stats *stats);
+
+/* Device-resident form of the two solves, for callers that keep the ice state on the GPU between
+ * time steps: ufe_ice_upload copies the inputs once; ufe_solve_*_resident runs a solve from the
+ * resident velocity state (reset to zero when `cold_start` is 1); ufe_velocity_download copies
+ * the resident velocity state back (u_b/v_b for SSA, the u_vav/v_vav pair for DIVA). */
+int32_t ufe_ice_upload(ufe_ctx *ctx, const ufe_ice_state *ice, const ufe_bc_prescribed *bc);
+int32_t ufe_solve_ssa_resident(ufe_ctx *ctx, const ufe_solver_params *p, int32_t cold_start,
+                               ufe_solve_stats *stats);
+int32_t ufe_solve_diva_resident(ufe_ctx *ctx, const ufe_solver_params *p, int32_t cold_start,
+                                ufe_solve_stats *stats);
+int32_t ufe_velocity_download(ufe_ctx *ctx, double *u_b, double *v_b);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* UFE_GPU_H */

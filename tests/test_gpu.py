@@ -1,0 +1,270 @@
+"""GPU parity tests: the CUDA path, called through the C ABI, against the oracle and the
+reference's known answers.  Tolerances: integer structure and operator applications bit-exact;
+Krylov-based results within 1e-8 relative L2 (FP64) or 1e-6 (FP32 Krylov + FP64 refinement)."""
+import numpy as np
+import pytest
+
+from helpers import kat_csr, load_kats, load_small_dome, rel_l2, same_structure
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def dome(pkg, gpu_lib):
+    mesh, ice, params, ops, sol = load_small_dome(pkg)
+    return mesh, ice, params, ops, sol
+
+
+@pytest.fixture(scope="module")
+def gpu_golden_ops(pkg, dome):
+    mesh, _, _, ops, _ = dome
+    s = pkg.VelocitySolver(mesh, operators=ops)
+    yield s
+    s.close()
+
+
+@pytest.fixture(scope="module")
+def gpu_built_ops(pkg, dome):
+    mesh = dome[0]
+    s = pkg.VelocitySolver(mesh)
+    yield s
+    s.close()
+
+
+# ---- CSR algebra -------------------------------------------------------------------------------
+@pytest.mark.parametrize("name", ["spmv_6x6", "spmv_7x7_1", "spmv_7x7_2"])
+def test_spmv_kats(pkg, gpu_golden_ops, name):
+    k = load_kats()[name]
+    y = gpu_golden_ops.multiply_CSR_matrix_with_vector_1D(kat_csr(pkg, k), np.array(k["x"], float))
+    assert np.array_equal(y, np.array(k["y"], float))
+
+
+def test_spmv_bitexact_random(pkg, oracle_mod, gpu_golden_ops):
+    import scipy.sparse as sp
+    A = pkg.CSR.from_scipy(sp.random(500, 300, density=0.05, random_state=7, format="csr"))
+    x = np.asfortranarray(np.random.default_rng(1).normal(size=(300, 3)))
+    assert np.array_equal(gpu_golden_ops.multiply_CSR_matrix_with_vector_2D(A, x), oracle_mod.csr_spmv(A, x))
+
+
+def test_spmv_empty_rows(pkg, gpu_golden_ops):
+    A = pkg.CSR(4, 3, [1, 1, 2, 2, 3], [2, 3], [2.0, -1.0], 1)
+    y = gpu_golden_ops.multiply_CSR_matrix_with_vector_1D(A, np.array([1.0, 2.0, 3.0]))
+    assert np.array_equal(y, [0.0, 4.0, 0.0, -3.0])
+
+
+def test_solve_csr_poisson_kat(pkg, gpu_golden_ops):
+    k = load_kats()["poisson_7"]
+    x, its, st = gpu_golden_ops.solve_matrix_equation_CSR_PETSc(kat_csr(pkg, k), k["b"], np.zeros(7), 1e-12, 0.0)
+    assert st == 0 and np.max(np.abs(x - np.array(k["x"]))) < k["tol"]
+
+
+def test_solve_csr_matches_oracle_and_direct(pkg, oracle_mod, gpu_golden_ops):
+    import scipy.sparse as sp
+    import scipy.sparse.linalg as spla
+    rng = np.random.default_rng(3)
+    n = 2000
+    A = sp.random(n, n, density=0.003, random_state=4, format="csr")
+    A = (A + sp.diags(np.abs(A).sum(1).A1 + 1.0 + rng.random(n))).tocsr()
+    b = rng.normal(size=n)
+    C = pkg.CSR.from_scipy(A)
+    xg, itg, stg = gpu_golden_ops.solve_matrix_equation_CSR_PETSc(C, b, np.zeros(n), 1e-12, 0.0)
+    xo, ito, sto = oracle_mod.csr_solve(C, b, np.zeros(n), 1e-12, 0.0)
+    assert stg == 0 and sto == 0 and abs(itg - ito) <= 2
+    assert rel_l2(xg, spla.spsolve(A.tocsc(), b)) < 1e-10
+
+
+def test_solve_csr_maxit_warns(pkg, gpu_golden_ops):
+    k = load_kats()["poisson_7"]
+    x, its, st = gpu_golden_ops.solve_matrix_equation_CSR_PETSc(kat_csr(pkg, k), k["b"], np.zeros(7), 1e-30, 0.0,
+                                                                 max_it=1)
+    assert st == pkg.abi.UFE_WARN_KRYLOV_MAXIT and its == 1
+
+
+# ---- operators -----------------------------------------------------------------------------------
+def test_gpu_operator_construction_matches_oracle(pkg, dome, gpu_built_ops):
+    """Integer structure identical to the reference's flood fill; values to rounding."""
+    ops = dome[3]
+    for name, A in ops.items():
+        B = gpu_built_ops.operator(name)
+        assert same_structure(A, B), name
+        scale = np.maximum(np.abs(A.val), 1e-300)
+        rows = np.repeat(np.arange(A.m), np.diff(A.ptr))
+        rowmax = np.zeros(A.m)
+        np.maximum.at(rowmax, rows, np.abs(A.val))
+        assert np.max(np.abs(A.val - B.val) / rowmax[rows]) < 1e-11, name
+        del scale
+
+
+def test_apply_operator_bitexact(pkg, oracle_mod, dome, gpu_golden_ops):
+    mesh, _, _, ops, _ = dome
+    rng = np.random.default_rng(5)
+    for name, A in ops.items():
+        x = np.asfortranarray(rng.normal(size=(A.n, 3)))
+        assert np.array_equal(gpu_golden_ops.apply(name, x), oracle_mod.csr_spmv(A, x)), name
+        x1 = rng.normal(size=A.n)
+        assert np.array_equal(gpu_golden_ops.apply(name, x1), oracle_mod.csr_spmv(A, x1)), name
+
+
+# ---- linearised SSA/DIVA ------------------------------------------------------------------------
+def _lin_inputs(nT, seed=1):
+    rng = np.random.default_rng(seed)
+    return [rng.uniform(1e10, 1e12, nT), rng.normal(0, 1e7, nT), rng.normal(0, 1e7, nT),
+            rng.uniform(0, 1e4, nT), rng.normal(0, 1e5, nT), rng.normal(0, 1e5, nT)]
+
+
+@pytest.mark.parametrize("cross", [1, 0])
+def test_assembly_bitexact(pkg, oracle_mod, dome, gpu_golden_ops, cross):
+    mesh, _, params, _, _ = dome
+    p = pkg.abi.default_params(do_include_SSADIVA_crossterms=cross)
+    args = _lin_inputs(mesh.nTri)
+    Ag, bg = gpu_golden_ops.assemble_linearised(p, *args)
+    Ao, bo = oracle_mod.Oracle(mesh).assemble_linearised(p, *args)
+    assert np.array_equal(Ag.ptr, Ao.ptr) and np.array_equal(Ag.ind, Ao.ind)
+    assert np.array_equal(Ag.val, Ao.val)
+    assert np.array_equal(bg, bo)
+
+
+def test_assembly_bc_variants_bitexact(pkg, oracle_mod, dome, gpu_golden_ops):
+    mesh = dome[0]
+    p = pkg.abi.default_params(BC_u_west=1, BC_v_north=1, BC_v_south=1)
+    args = _lin_inputs(mesh.nTri, seed=2)
+    mask = np.zeros(mesh.nTri, np.int32)
+    mask[::37] = 1
+    bc = dict(mask_b=mask, u_b=np.linspace(-5, 5, mesh.nTri), v_b=np.linspace(3, -3, mesh.nTri))
+    Ag, bg = gpu_golden_ops.assemble_linearised(p, *args, BC=bc)
+    Ao, bo = oracle_mod.Oracle(mesh).assemble_linearised(p, *args, BC=bc)
+    assert np.array_equal(Ag.ptr, Ao.ptr) and np.array_equal(Ag.ind, Ao.ind)
+    assert np.array_equal(Ag.val, Ao.val) and np.array_equal(bg, bo)
+
+
+@pytest.mark.parametrize("precision,tol", [(0, 1e-9), (1, 1e-6)])
+def test_linearised_solve_matches_direct(pkg, oracle_mod, dome, gpu_golden_ops, precision, tol):
+    import scipy.sparse.linalg as spla
+    mesh = dome[0]
+    p = pkg.abi.default_params(stress_balance_PETSc_rtol=1e-12, precision=precision)
+    args = _lin_inputs(mesh.nTri, seed=4)
+    A, bb = oracle_mod.Oracle(mesh).assemble_linearised(p, *args)
+    x = spla.spsolve(A.to_scipy().tocsc(), bb)
+    u, v = np.zeros(mesh.nTri), np.zeros(mesh.nTri)
+    up, vp, its, st = gpu_golden_ops.solve_SSA_DIVA_linearised(p, u, v, *args)
+    assert st in (0, 2) and its > 0
+    assert rel_l2(np.c_[u, v].ravel(), x) < tol
+
+
+# ---- full solves ---------------------------------------------------------------------------------
+def test_ssa_matches_golden(pkg, dome, gpu_golden_ops):
+    mesh, ice, params, ops, sol = dome
+    ssa = pkg.new_ssa_state(mesh.nTri)
+    nv, na, st = gpu_golden_ops.solve_SSA(ice, ssa, params)
+    assert nv == sol["its"][0] and st["status"] == sol["its"][2]
+    assert abs(na - sol["its"][1]) <= max(3, 0.05 * sol["its"][1])
+    assert rel_l2(np.r_[ssa["u_b"], ssa["v_b"]], np.r_[sol["u_b"], sol["v_b"]]) < 1e-8
+
+
+def test_ssa_gpu_operators_vs_oracle(pkg, oracle_mod, dome, gpu_built_ops):
+    mesh, ice, params, ops, sol = dome
+    ssa = pkg.new_ssa_state(mesh.nTri)
+    nv, na, st = gpu_built_ops.solve_SSA(ice, ssa, params)
+    assert nv == sol["its"][0]
+    assert rel_l2(np.r_[ssa["u_b"], ssa["v_b"]], np.r_[sol["u_b"], sol["v_b"]]) < 1e-8
+
+
+def test_ssa_resident_path_equals_host_api(pkg, dome, gpu_golden_ops):
+    mesh, ice, params, _, sol = dome
+    gpu_golden_ops.ice_upload(ice)
+    st = gpu_golden_ops.solve_resident(params, diva=False, cold_start=True)
+    u, v = gpu_golden_ops.velocity_download()
+    assert st["n_visc_its"] == sol["its"][0]
+    assert rel_l2(np.r_[u, v], np.r_[sol["u_b"], sol["v_b"]]) < 1e-8
+    st2 = gpu_golden_ops.solve_resident(params, diva=False, cold_start=True)   # graph reuse
+    u2, v2 = gpu_golden_ops.velocity_download()
+    assert np.array_equal(u, u2) and np.array_equal(v, v2)                  # deterministic
+
+
+def test_ssa_converged_dome_oracle_parity(pkg, oracle_mod):
+    mesh, ice, params = pkg.geometry.small_dome(seed=1)
+    params.stress_balance_PETSc_rtol = 1e-12
+    orc = oracle_mod.Oracle(mesh)
+    g = pkg.VelocitySolver(mesh, operators=orc.operators())
+    a, b = pkg.new_ssa_state(mesh.nTri), pkg.new_ssa_state(mesh.nTri)
+    nvg, nag, stg = g.solve_SSA(ice, a, params)
+    nvo, nao, sto = orc.solve_SSA(ice, b, params)
+    g.close()
+    assert stg["status"] == sto["status"] == 0 and nvg == nvo
+    assert rel_l2(np.r_[a["u_b"], a["v_b"]], np.r_[b["u_b"], b["v_b"]]) < 1e-8
+
+
+@pytest.mark.parametrize("sliding", ["Schoof2005", "Tsai2015", "Weertman"])
+def test_diva_matches_oracle(pkg, oracle_mod, sliding):
+    mesh, ice, params = pkg.geometry.small_channel(sliding=sliding)
+    params.stress_balance_PETSc_rtol = 1e-12
+    params.visc_it_nit = 12
+    orc = oracle_mod.Oracle(mesh)
+    g = pkg.VelocitySolver(mesh, operators=orc.operators())
+    a, b = pkg.new_diva_state(mesh.nTri, mesh.nz), pkg.new_diva_state(mesh.nTri, mesh.nz)
+    nvg, nag, stg = g.solve_DIVA(ice, a, params)
+    nvo, nao, sto = orc.solve_DIVA(ice, b, params)
+    g.close()
+    assert nvg == nvo and stg["status"] == sto["status"]
+    for k in ("u_vav_b", "v_vav_b", "u_base_b", "tau_bx_b", "eta_3D_b", "u_3D_b", "v_3D_b"):
+        assert rel_l2(a[k], b[k]) < 1e-8, k
+
+
+def test_mixed_precision_matches_fp64(pkg, dome, gpu_golden_ops):
+    mesh, ice, params, _, _ = dome
+    p64 = pkg.abi.default_params(choice_sliding_law="Weertman", visc_it_norm_dUV_tol=1e-4,
+                                 stress_balance_PETSc_rtol=1e-10)
+    p32 = pkg.abi.default_params(choice_sliding_law="Weertman", visc_it_norm_dUV_tol=1e-4,
+                                 stress_balance_PETSc_rtol=1e-10, precision=1)
+    a, b = pkg.new_ssa_state(mesh.nTri), pkg.new_ssa_state(mesh.nTri)
+    n64 = gpu_golden_ops.solve_SSA(ice, a, p64)
+    n32 = gpu_golden_ops.solve_SSA(ice, b, p32)
+    assert n32[2]["status"] == 0 and n32[2]["n_refinements"] >= 1
+    assert rel_l2(np.r_[b["u_b"], b["v_b"]], np.r_[a["u_b"], a["v_b"]]) < 1e-6
+
+
+# ---- failure behaviour ---------------------------------------------------------------------------
+def test_nan_input_reports_nan(pkg, dome, gpu_golden_ops):
+    mesh, ice, params, _, _ = dome
+    bad = dict(ice)
+    bad["Hs"] = ice["Hs"].copy()
+    bad["Hs"][10] = np.nan
+    ssa = pkg.new_ssa_state(mesh.nTri)
+    with pytest.raises(pkg.UfeError) as e:
+        gpu_golden_ops.solve_SSA(bad, ssa, params)
+    assert e.value.code == pkg.abi.UFE_ERR_NAN
+
+
+def test_invalid_params_rejected(pkg, dome, gpu_golden_ops):
+    mesh, ice, params, _, _ = dome
+    p = pkg.abi.default_params(choice_sliding_law=17)
+    with pytest.raises(pkg.UfeError) as e:
+        gpu_golden_ops.solve_SSA(ice, pkg.new_ssa_state(mesh.nTri), p)
+    assert e.value.code == pkg.abi.UFE_ERR_INVALID
+
+
+def test_bad_mesh_rejected(pkg, dome):
+    mesh = dome[0]
+    bad = pkg.mesh.Mesh.from_arrays(mesh.V, mesh.nC, mesh.C, mesh.niTri, mesh.iTri, mesh.VBI,
+                                    mesh.Tri, np.asfortranarray(mesh.TriC + 5 * mesh.nTri), mesh.TriBI, mesh.TriGC,
+                                    mesh.zeta, (mesh.xmin, mesh.xmax, mesh.ymin, mesh.ymax))
+    with pytest.raises(pkg.UfeError) as e:
+        pkg.VelocitySolver(bad)
+    assert e.value.code == pkg.abi.UFE_ERR_INVALID
+
+
+def test_picard_maxit_warning(pkg, dome, gpu_golden_ops):
+    mesh, ice, params, _, _ = dome
+    p = pkg.abi.default_params(choice_sliding_law="Weertman", visc_it_nit=2)
+    ssa = pkg.new_ssa_state(mesh.nTri)
+    nv, na, st = gpu_golden_ops.solve_SSA(ice, ssa, p)
+    assert st["status"] == pkg.abi.UFE_WARN_PICARD_MAXIT and nv == 3
+
+
+def test_no_grounded_ice_zero_velocity(pkg, dome, gpu_golden_ops):
+    mesh, ice, params, _, _ = dome
+    z = dict(ice)
+    z["mask_grounded_ice"] = np.zeros(mesh.nV, np.int32)
+    ssa = {"u_b": np.ones(mesh.nTri), "v_b": np.ones(mesh.nTri)}
+    nv, na, st = gpu_golden_ops.solve_SSA(z, ssa, params)
+    assert nv == 0 and not ssa["u_b"].any()

@@ -1,0 +1,215 @@
+"""ctypes mirror of include/ufe_gpu.h and the loader of the in-tree GB300 library.
+
+The library is loaded from ``_build/libufe_gpu.so`` next to this package.  There is no fallback:
+if the shared object is missing, :func:`load_library` raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libufe_gpu.so")
+
+# status codes
+UFE_OK = 0
+UFE_WARN_PICARD_MAXIT = 1
+UFE_WARN_KRYLOV_MAXIT = 2
+UFE_ERR_INVALID = -1
+UFE_ERR_NAN = -2
+UFE_ERR_DIVERGED = -3
+UFE_ERR_THERMO_UNSTABLE = -4
+UFE_ERR_DEVICE = -5
+UFE_ERR_CAPACITY = -6
+
+# operators (enum ufe_operator)
+OPERATORS = ["MAP_A_B", "DDX_A_B", "DDY_A_B", "MAP_B_A", "DDX_B_A", "DDY_B_A", "DDX_A_A", "DDY_A_A",
+             "M2_DDX_B_B", "M2_DDY_B_B", "M2_D2DX2_B_B", "M2_D2DXDY_B_B", "M2_D2DY2_B_B"]
+OP = {name: i for i, name in enumerate(OPERATORS)}
+
+SLIDING = {"no_sliding": 0, "Weertman": 1, "Coulomb": 2, "Budd": 3, "Tsai2015": 4, "Schoof2005": 5}
+BC = {"infinite": 0, "zero": 1}
+PREC_FP64, PREC_FP32_REFINE = 0, 1
+X0_ZERO, X0_CURRENT = 0, 1
+
+dptr = C.POINTER(C.c_double)
+iptr = C.POINTER(C.c_int32)
+
+
+class MeshDesc(C.Structure):
+    _fields_ = [("nV", C.c_int32), ("nTri", C.c_int32), ("nC_mem", C.c_int32), ("nz", C.c_int32),
+                ("V", dptr), ("nC", iptr), ("C", iptr), ("niTri", iptr), ("iTri", iptr), ("VBI", iptr),
+                ("Tri", iptr), ("TriC", iptr), ("TriBI", iptr), ("TriGC", dptr), ("zeta", dptr)]
+
+
+class SolverParams(C.Structure):
+    _fields_ = [("choice_sliding_law", C.c_int32), ("do_include_SSADIVA_crossterms", C.c_int32),
+                ("do_GL_subgrid_friction", C.c_int32),
+                ("BC_u_west", C.c_int32), ("BC_u_east", C.c_int32), ("BC_u_south", C.c_int32), ("BC_u_north", C.c_int32),
+                ("BC_v_west", C.c_int32), ("BC_v_east", C.c_int32), ("BC_v_south", C.c_int32), ("BC_v_north", C.c_int32),
+                ("visc_it_nit", C.c_int32),
+                ("visc_it_norm_dUV_tol", C.c_double), ("visc_it_relax", C.c_double), ("visc_eff_min", C.c_double),
+                ("vel_max", C.c_double), ("stress_balance_PETSc_rtol", C.c_double),
+                ("stress_balance_PETSc_abstol", C.c_double), ("Glens_flow_law_exponent", C.c_double),
+                ("Glens_flow_law_epsilon_sq_0", C.c_double), ("slid_Weertman_m", C.c_double),
+                ("slid_Budd_q_plastic", C.c_double), ("slid_Budd_u_threshold", C.c_double),
+                ("subgrid_friction_exponent_on_B_grid", C.c_double), ("slid_beta_max", C.c_double),
+                ("slid_delta_v", C.c_double),
+                ("krylov_max_it", C.c_int32), ("krylov_initial_guess", C.c_int32), ("precision", C.c_int32),
+                ("krylov_inner_rtol", C.c_double), ("reserved", C.c_int32 * 8)]
+
+
+class IceState(C.Structure):
+    _fields_ = [("Hi", dptr), ("Hs", dptr), ("A_flow", dptr), ("fraction_gr_b", dptr),
+                ("mask_grounded_ice", iptr), ("beta_sq", dptr), ("alpha_sq", dptr),
+                ("effective_pressure", dptr), ("till_yield_stress", dptr)]
+
+
+class BCPrescribed(C.Structure):
+    _fields_ = [("mask_b", iptr), ("u_b", dptr), ("v_b", dptr)]
+
+
+class DivaState(C.Structure):
+    _fields_ = [("u_vav_b", dptr), ("v_vav_b", dptr), ("u_base_b", dptr), ("v_base_b", dptr),
+                ("tau_bx_b", dptr), ("tau_by_b", dptr), ("eta_3D_b", dptr), ("u_3D_b", dptr), ("v_3D_b", dptr)]
+
+
+class SolveStats(C.Structure):
+    _fields_ = [("n_visc_its", C.c_int32), ("n_Axb_its", C.c_int32), ("n_refinements", C.c_int32),
+                ("status", C.c_int32), ("L2_uv", C.c_double), ("visc_it_relax_applied", C.c_double),
+                ("device_ms", C.c_double), ("reserved", C.c_int32 * 6)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}
+
+
+def default_params(**overrides) -> SolverParams:
+    """The defaults of UFEMISM's model_configuration.f90 (same values as ufe_default_params)."""
+    p = SolverParams()
+    p.choice_sliding_law = SLIDING["Weertman"]
+    p.do_include_SSADIVA_crossterms = 1
+    p.do_GL_subgrid_friction = 1
+    for side in ("west", "east", "south", "north"):
+        setattr(p, f"BC_u_{side}", BC["infinite"])
+        setattr(p, f"BC_v_{side}", BC["infinite"])
+    p.visc_it_nit = 50
+    p.visc_it_norm_dUV_tol = 5e-5
+    p.visc_it_relax = 0.2
+    p.visc_eff_min = 1e4
+    p.vel_max = 5000.0
+    p.stress_balance_PETSc_rtol = 1e-7
+    p.stress_balance_PETSc_abstol = 1e-5
+    p.Glens_flow_law_exponent = 3.0
+    p.Glens_flow_law_epsilon_sq_0 = 1e-8
+    p.slid_Weertman_m = 3.0
+    p.slid_Budd_q_plastic = 0.3
+    p.slid_Budd_u_threshold = 100.0
+    p.subgrid_friction_exponent_on_B_grid = 2.0
+    p.slid_beta_max = 1e20
+    p.slid_delta_v = 1e-3
+    p.krylov_max_it = 10000
+    p.krylov_initial_guess = X0_CURRENT
+    p.precision = PREC_FP64
+    p.krylov_inner_rtol = 1e-4
+    for k, v in overrides.items():
+        if k == "choice_sliding_law" and isinstance(v, str):
+            v = SLIDING[v]
+        setattr(p, k, v)
+    return p
+
+
+# -- numpy <-> ctypes helpers -------------------------------------------------------------------
+def as_d(a):
+    """Pointer to a contiguous float64 buffer (Fortran-ordered arrays are flattened column-major)."""
+    if a is None:
+        return None
+    assert a.dtype == np.float64 and (a.flags.f_contiguous or a.flags.c_contiguous), "float64 contiguous array needed"
+    return a.ctypes.data_as(dptr)
+
+
+def as_i(a):
+    if a is None:
+        return None
+    assert a.dtype == np.int32 and (a.flags.f_contiguous or a.flags.c_contiguous), "int32 contiguous array needed"
+    return a.ctypes.data_as(iptr)
+
+
+def mesh_desc(mesh) -> tuple[MeshDesc, list]:
+    """A MeshDesc over a :class:`mesh.Mesh`; the returned list keeps the arrays alive."""
+    keep = [mesh.V, mesh.nC, mesh.C, mesh.niTri, mesh.iTri, mesh.VBI, mesh.Tri, mesh.TriC, mesh.TriBI,
+            mesh.TriGC, mesh.zeta]
+    d = MeshDesc(mesh.nV, mesh.nTri, mesh.nC_mem, mesh.nz, as_d(mesh.V), as_i(mesh.nC), as_i(mesh.C),
+                 as_i(mesh.niTri), as_i(mesh.iTri), as_i(mesh.VBI), as_i(mesh.Tri), as_i(mesh.TriC),
+                 as_i(mesh.TriBI), as_d(mesh.TriGC), as_d(mesh.zeta))
+    return d, keep
+
+
+def ice_state(ice: dict) -> tuple[IceState, list]:
+    keep = [v for v in ice.values() if isinstance(v, np.ndarray)]
+    s = IceState(as_d(ice["Hi"]), as_d(ice["Hs"]), as_d(ice["A_flow"]), as_d(ice["fraction_gr_b"]),
+                 as_i(ice["mask_grounded_ice"]), as_d(ice.get("beta_sq")), as_d(ice.get("alpha_sq")),
+                 as_d(ice.get("effective_pressure")), as_d(ice.get("till_yield_stress")))
+    return s, keep
+
+
+def bc_prescribed(bc: dict | None):
+    if not bc:
+        return None, []
+    b = BCPrescribed(as_i(bc["mask_b"]), as_d(bc["u_b"]), as_d(bc["v_b"]))
+    return b, [bc["mask_b"], bc["u_b"], bc["v_b"]]
+
+
+# -- the library ---------------------------------------------------------------------------------
+EXPORTS = {
+    "ufe_default_params": (None, [C.POINTER(SolverParams)]),
+    "ufe_ctx_create": (C.c_int32, [C.c_int32, C.POINTER(C.c_void_p)]),
+    "ufe_ctx_destroy": (None, [C.c_void_p]),
+    "ufe_ctx_last_error": (C.c_char_p, [C.c_void_p]),
+    "ufe_ctx_get_stream": (C.c_int32, [C.c_void_p, C.POINTER(C.c_void_p)]),
+    "ufe_ctx_synchronize": (C.c_int32, [C.c_void_p]),
+    "ufe_mesh_upload": (C.c_int32, [C.c_void_p, C.POINTER(MeshDesc)]),
+    "ufe_mesh_build_operators": (C.c_int32, [C.c_void_p]),
+    "ufe_mesh_set_operator": (C.c_int32, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_int64, iptr, iptr, dptr,
+                                          C.c_int32]),
+    "ufe_operator_info": (C.c_int32, [C.c_void_p, C.c_int32, iptr, iptr, C.POINTER(C.c_int64)]),
+    "ufe_operator_export": (C.c_int32, [C.c_void_p, C.c_int32, iptr, iptr, dptr, C.c_int32]),
+    "ufe_apply_operator": (C.c_int32, [C.c_void_p, C.c_int32, dptr, dptr, C.c_int32]),
+    "ufe_csr_spmv": (C.c_int32, [C.c_void_p, C.c_int32, C.c_int32, C.c_int64, iptr, iptr, dptr, C.c_int32, dptr,
+                                 dptr, C.c_int32]),
+    "ufe_solve_csr": (C.c_int32, [C.c_void_p, C.c_int32, C.c_int64, iptr, iptr, dptr, C.c_int32, dptr, dptr,
+                                  C.c_double, C.c_double, C.c_int32, iptr]),
+    "ufe_assemble_linearised": (C.c_int32, [C.c_void_p, C.POINTER(SolverParams), dptr, dptr, dptr, dptr, dptr, dptr,
+                                            dptr, dptr, C.POINTER(BCPrescribed), iptr, iptr, dptr, dptr, C.c_int64,
+                                            C.POINTER(C.c_int64)]),
+    "ufe_solve_linearised": (C.c_int32, [C.c_void_p, C.POINTER(SolverParams), dptr, dptr, dptr, dptr, dptr, dptr,
+                                         dptr, dptr, dptr, dptr, C.POINTER(BCPrescribed), iptr]),
+    "ufe_solve_ssa": (C.c_int32, [C.c_void_p, C.POINTER(SolverParams), C.POINTER(IceState), C.POINTER(BCPrescribed),
+                                  dptr, dptr, iptr, iptr, C.POINTER(SolveStats)]),
+    "ufe_solve_diva": (C.c_int32, [C.c_void_p, C.POINTER(SolverParams), C.POINTER(IceState), C.POINTER(BCPrescribed),
+                                   C.POINTER(DivaState), iptr, iptr, C.POINTER(SolveStats)]),
+    "ufe_ice_upload": (C.c_int32, [C.c_void_p, C.POINTER(IceState), C.POINTER(BCPrescribed)]),
+    "ufe_solve_ssa_resident": (C.c_int32, [C.c_void_p, C.POINTER(SolverParams), C.c_int32, C.POINTER(SolveStats)]),
+    "ufe_solve_diva_resident": (C.c_int32, [C.c_void_p, C.POINTER(SolverParams), C.c_int32, C.POINTER(SolveStats)]),
+    "ufe_velocity_download": (C.c_int32, [C.c_void_p, dptr, dptr]),
+}
+
+_LIB = None
+
+
+def load_library(path: str = LIB_PATH):
+    """Load libufe_gpu.so and declare every entry point of include/ufe_gpu.h."""
+    global _LIB
+    if _LIB is not None and path == LIB_PATH:
+        return _LIB
+    if not os.path.exists(path):
+        raise RuntimeError(f"GB300 library not built: {path} is missing (run build())")
+    lib = C.CDLL(path)
+    for name, (res, args) in EXPORTS.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    if path == LIB_PATH:
+        _LIB = lib
+    return lib

@@ -1,0 +1,134 @@
+// Internal declarations of the GB300 velocity-solve library (not part of the C ABI).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string>
+#include <vector>
+#include <exception>
+
+#include "../../include/ufe_gpu.h"
+
+// ------------------------------------------------------------------------------------------
+// error handling: every CUDA call is checked; a failure records a message on the context and
+// turns into UFE_ERR_DEVICE at the ABI.
+struct ufe_error {
+  int32_t code;
+  std::string msg;
+};
+
+#define UFE_CUDA(call)                                                                        \
+  do {                                                                                        \
+    cudaError_t e_ = (call);                                                                  \
+    if (e_ != cudaSuccess)                                                                    \
+      throw ufe_error{UFE_ERR_DEVICE, std::string(#call) + ": " + cudaGetErrorString(e_)};    \
+  } while (0)
+
+#define UFE_REQUIRE(cond, code, text)                                                         \
+  do {                                                                                        \
+    if (!(cond)) throw ufe_error{(code), (text)};                                             \
+  } while (0)
+
+// ------------------------------------------------------------------------------------------
+// device CSR matrix, 0-based.  Families of operators that share one sparsity pattern share the
+// ptr/ind arrays (a_b: map/ddx/ddy; b_a: map/ddx/ddy; a_a: ddx/ddy; b_b 2nd order: 5 operators).
+struct DevCSR {
+  int32_t m = 0, n = 0;
+  int64_t nnz = 0;
+  int32_t *ptr = nullptr;
+  int32_t *ind = nullptr;
+  double *val = nullptr;
+};
+
+// Krylov / Picard scalars that live on the device for a whole solve.
+struct KrylovScalars {
+  double rho, rhoold, alpha, omega, omegaold, beta;
+  double dp, ttol, rnorm0;
+  int32_t it;          // iterations of the current solve
+  int32_t active;      // 1 while iterating
+  int32_t status;      // UFE_* of the current solve
+  int32_t total_its;   // summed over the Picard iterations
+  int32_t max_it;
+  int32_t refinements; // FP64 refinement steps of the current Picard iteration
+  int32_t tbreak;      // t = 0 in the last iteration: x + alpha p is the final update
+  int32_t pad;
+};
+
+struct PicardScalars {
+  double L2, L2_prev, relax, eps0, eta_max;
+  int32_t it, nit_diverg, active, status;
+  int32_t n_refine;
+  int32_t pad[3];
+};
+
+// Partial sums of one reduction stage: each block writes `nparts` values at
+// partials[slot * max_blocks + blockIdx.x]; the last block to arrive sums them in block order.
+constexpr int kMaxReduceBlocks = 4096;
+constexpr int kReduceSlots = 8;
+
+struct ReduceArea {
+  double *partials = nullptr;     // kReduceSlots * kMaxReduceBlocks
+  unsigned int *tickets = nullptr; // one counter per reduction site
+};
+
+// ------------------------------------------------------------------------------------------
+struct ufe_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::string last_error;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+
+  // mesh (device, as uploaded: 1-based, column-major)
+  bool has_mesh = false;
+  int32_t nV = 0, nTri = 0, nC_mem = 0, nz = 0;
+  double *V = nullptr, *TriGC = nullptr, *zeta = nullptr;
+  int32_t *nC = nullptr, *C = nullptr, *niTri = nullptr, *iTri = nullptr, *VBI = nullptr;
+  int32_t *Tri = nullptr, *TriC = nullptr, *TriBI = nullptr;
+  std::vector<double> zeta_host;
+
+  DevCSR ops[UFE_OP_COUNT];
+  bool op_set[UFE_OP_COUNT] = {};
+  std::vector<void *> op_allocs;   // device allocations owned by the operators
+
+  // solver workspace (allocated lazily for the mesh size)
+  struct Work *work = nullptr;
+
+  ReduceArea red;
+};
+
+// Run an ABI body, turning exceptions into status codes and messages.
+template <class F>
+inline int32_t guarded(ufe_ctx *ctx, F &&body) {
+  if (!ctx) return UFE_ERR_INVALID;
+  try {
+    int32_t rc = body();
+    if (rc >= 0) ctx->last_error.clear();
+    return rc;
+  } catch (const ufe_error &e) {
+    ctx->last_error = e.msg;
+    return e.code;
+  } catch (const std::exception &e) {
+    ctx->last_error = e.what();
+    return UFE_ERR_DEVICE;
+  }
+}
+
+
+// helpers implemented in ufe_ctx.cu
+void *dev_alloc(size_t bytes);
+void dev_free(void *p);
+void free_operators(ufe_ctx *ctx);
+void ensure_reduce_area(ufe_ctx *ctx);
+int32_t pick_blocks(int64_t items, int threads, int max_blocks);
+
+// ufe_operators.cu
+void build_operators_gpu(ufe_ctx *ctx);
+
+// ufe_spmv.cu
+void launch_csr_spmv(cudaStream_t s, const DevCSR &A, const double *x, double *y, int32_t ncols);
+
+// ufe_velocity.cu
+void free_work(ufe_ctx *ctx);
+int32_t solve_csr_device(ufe_ctx *ctx, const DevCSR &A, const double *b, double *x, double rtol,
+                         double abstol, int32_t max_it, int32_t *its);
+

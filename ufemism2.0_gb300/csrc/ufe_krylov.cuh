@@ -1,0 +1,343 @@
+// Krylov kernels: Jacobi-preconditioned BiCGStab in the form of PETSc's KSPBCGS with left
+// preconditioning (the solver UFEMISM's solve_matrix_equation_CSR_PETSc hands its systems to,
+// src/UPSY/basic/petsc_basic.f90:32-141, run with -ksp_type bcgs -pc_type jacobi).
+//
+// One iteration is three kernels:
+//   k_p_spmv : p <- r - beta*omega*v + beta*p (also evaluated on the fly for gathered columns),
+//              v <- D^-1 A p, partial (v, r^)                       -> alpha
+//   k_s_spmv : s <- r - alpha*v (on the fly for gathered columns),
+//              t <- D^-1 A s, partials (s,t), (t,t), (s,s)           -> omega
+//   k_xr     : x <- x + alpha*p + omega*s,  r <- s - omega*t,
+//              partials (r, r^), (r, r)                             -> convergence test, beta
+// p and v are double-buffered by iteration parity, so the on-the-fly updates read old values.
+// Every reduction is the deterministic last-block sum of ufe_work.cuh; kernels loop over their
+// rows with a grid stride so the grid never exceeds the partial-sum capacity.
+#pragma once
+
+#include <type_traits>
+
+#include "ufe_work.cuh"
+
+template <class V> struct ScalarOf { using T = double; };
+template <> struct ScalarOf<float2> { using T = float; };
+template <> struct ScalarOf<double2> { using T = double; };
+
+// ---- vector element helpers ---------------------------------------------------------------
+__device__ __forceinline__ double v_dot(double2 a, double2 b) { return a.x * b.x + a.y * b.y; }
+__device__ __forceinline__ double v_dot(float2 a, float2 b) {
+  return (double)a.x * (double)b.x + (double)a.y * (double)b.y;
+}
+__device__ __forceinline__ double v_dot(double a, double b) { return a * b; }
+__device__ __forceinline__ double2 v_mul(double2 d, double2 y) { return make_double2(d.x * y.x, d.y * y.y); }
+__device__ __forceinline__ float2 v_mul(float2 d, float2 y) { return make_float2(d.x * y.x, d.y * y.y); }
+__device__ __forceinline__ double v_mul(double d, double y) { return d * y; }
+template <class V> __device__ __forceinline__ V v_zero();
+template <> __device__ __forceinline__ double2 v_zero<double2>() { return make_double2(0.0, 0.0); }
+template <> __device__ __forceinline__ float2 v_zero<float2>() { return make_float2(0.f, 0.f); }
+template <> __device__ __forceinline__ double v_zero<double>() { return 0.0; }
+// p_new = r - (beta*omega)*v + beta*p   (PETSc VecAXPBYPCZ(P, 1, -beta*omega, beta, R, V))
+__device__ __forceinline__ double2 v_pupd(double2 r, double bw, double2 v, double beta, double2 p) {
+  return make_double2(r.x - bw * v.x + beta * p.x, r.y - bw * v.y + beta * p.y);
+}
+__device__ __forceinline__ float2 v_pupd(float2 r, float bw, float2 v, float beta, float2 p) {
+  return make_float2(r.x - bw * v.x + beta * p.x, r.y - bw * v.y + beta * p.y);
+}
+__device__ __forceinline__ double v_pupd(double r, double bw, double v, double beta, double p) {
+  return r - bw * v + beta * p;
+}
+// r - a*v
+__device__ __forceinline__ double2 v_sub_scaled(double2 r, double a, double2 v) {
+  return make_double2(r.x - a * v.x, r.y - a * v.y);
+}
+__device__ __forceinline__ float2 v_sub_scaled(float2 r, float a, float2 v) {
+  return make_float2(r.x - a * v.x, r.y - a * v.y);
+}
+__device__ __forceinline__ double v_sub_scaled(double r, double a, double v) { return r - a * v; }
+// x + a*p + w*s
+__device__ __forceinline__ double2 v_xupd(double2 x, double a, double2 p, double w, double2 s) {
+  return make_double2(x.x + a * p.x + w * s.x, x.y + a * p.y + w * s.y);
+}
+__device__ __forceinline__ float2 v_xupd(float2 x, float a, float2 p, float w, float2 s) {
+  return make_float2(x.x + a * p.x + w * s.x, x.y + a * p.y + w * s.y);
+}
+__device__ __forceinline__ double v_xupd(double x, double a, double p, double w, double s) {
+  return x + a * p + w * s;
+}
+__device__ __forceinline__ double2 v_shfl_xor(double2 a, int o) {
+  return make_double2(__shfl_xor_sync(0xffffffffu, a.x, o), __shfl_xor_sync(0xffffffffu, a.y, o));
+}
+__device__ __forceinline__ float2 v_shfl_xor(float2 a, int o) {
+  return make_float2(__shfl_xor_sync(0xffffffffu, a.x, o), __shfl_xor_sync(0xffffffffu, a.y, o));
+}
+__device__ __forceinline__ double v_shfl_xor(double a, int o) { return __shfl_xor_sync(0xffffffffu, a, o); }
+__device__ __forceinline__ double2 v_add(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ float2 v_add(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ double v_add(double a, double b) { return a + b; }
+
+// ---- matrix access policies ---------------------------------------------------------------
+// 2x2-block rows (one triangle = its u and v rows), FP64 or FP32 blocks; L lanes per block row.
+template <typename Real, int L>
+struct BsrMat {
+  using Vec = typename std::conditional<sizeof(Real) == 8, double2, float2>::type;
+  using Blk = typename std::conditional<sizeof(Real) == 8, double4, float4>::type;
+  static constexpr int kLanes = L;
+  int32_t items;
+  const int32_t *__restrict__ ptr;
+  const int32_t *__restrict__ col;
+  const Blk *__restrict__ blk;
+  template <class G>
+  __device__ __forceinline__ Vec row_partial(int i, int lane, G get) const {
+    Vec y = v_zero<Vec>();
+    int k2 = __ldg(ptr + i + 1);
+    for (int k = __ldg(ptr + i) + lane; k < k2; k += L) {
+      Blk a = blk[k];
+      Vec x = get(__ldg(col + k));
+      y.x += a.x * x.x + a.y * x.y;
+      y.y += a.z * x.x + a.w * x.y;
+    }
+    return y;
+  }
+};
+
+// scalar CSR rows (the general matrix-equation solve), one lane per row
+struct CsrMat {
+  using Vec = double;
+  static constexpr int kLanes = 1;
+  int32_t items;
+  const int32_t *__restrict__ ptr;
+  const int32_t *__restrict__ col;
+  const double *__restrict__ val;
+  template <class G>
+  __device__ __forceinline__ double row_partial(int i, int lane, G get) const {
+    double y = 0.0;
+    int k2 = __ldg(ptr + i + 1);
+    for (int k = __ldg(ptr + i); k < k2; ++k) y += __ldg(val + k) * get(__ldg(col + k));
+    return y;
+  }
+};
+
+template <class Vec>
+struct KV {
+  Vec *X, *R, *RP, *S, *T, *B;
+  const Vec *dinv;
+  Vec *P[2], *V[2];
+};
+
+// reduction sites (one ticket each)
+enum : int {
+  kSiteInit = 0, kSiteP, kSiteS, kSiteXR, kSiteResid, kSitePicard, kSiteAux, kSiteInner, kSiteCount
+};
+
+struct CondArg {
+  cudaGraphConditionalHandle handle;
+  int use;
+};
+
+__device__ __forceinline__ void set_cond(CondArg c, int value) {
+  if (c.use) cudaGraphSetConditional(c.handle, value ? 1u : 0u);
+}
+
+template <int L, class Vec>
+__device__ __forceinline__ Vec lane_reduce(Vec y) {
+#pragma unroll
+  for (int o = L / 2; o > 0; o >>= 1) y = v_add(y, v_shfl_xor(y, o));
+  return y;
+}
+
+// Lanes of one group must be in one warp: blockDim.x is a multiple of 32 and L divides 32.
+#define KRYLOV_ROWS(M, i, lane)                                                                \
+  const int lane = threadIdx.x % M::kLanes;                                                    \
+  const int64_t gstride_ = ((int64_t)gridDim.x * blockDim.x) / M::kLanes;                      \
+  const int64_t nrows_pad_ = ((mat.items + gstride_ - 1) / gstride_) * gstride_;               \
+  for (int64_t i##_64 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / M::kLanes;          \
+       i##_64 < nrows_pad_; i##_64 += gstride_)
+
+// r = D^-1 (b - A x), r^ = r, p = v = 0; tests the initial residual (KSPConvergedDefault at
+// iteration 0) and primes rho = (r, r^).
+template <class M>
+__global__ void k_krylov_init(M mat, KV<typename M::Vec> v, KrylovScalars *ks, double rtol,
+                              double abstol, int max_it, int x_is_zero, double *partials,
+                              unsigned int *tickets, CondArg cond) {
+  using Vec = typename M::Vec;
+  double acc[2] = {0.0, 0.0};
+  KRYLOV_ROWS(M, i, lane) {
+    const int i = (int)i_64;
+    const bool live = i < mat.items;
+    Vec ax = v_zero<Vec>();
+    if (!x_is_zero) {
+      Vec part = live ? mat.row_partial(i, lane, [&](int j) { return v.X[j]; }) : v_zero<Vec>();
+      ax = lane_reduce<M::kLanes>(part);
+    }
+    if (live && lane == 0) {
+      Vec b = v.B[i], d = v.dinv[i];
+      Vec r = v_mul(d, v_sub_scaled(b, 1.0, ax));
+      Vec db = v_mul(d, b);
+      v.R[i] = r;
+      v.RP[i] = r;
+      v.P[0][i] = v_zero<Vec>();
+      v.V[0][i] = v_zero<Vec>();
+      if (x_is_zero) v.X[i] = v_zero<Vec>();
+      acc[0] += v_dot(r, r);
+      acc[1] += v_dot(db, db);
+    }
+  }
+  double tot[2];
+  if (grid_sum<2>(acc, partials, tickets + kSiteInit, tot)) {
+    double dp = sqrt(tot[0]);
+    double bnorm = sqrt(tot[1]);
+    double rnorm0 = bnorm != 0.0 ? bnorm : dp;
+    KrylovScalars s = *ks;
+    s.dp = dp;
+    s.rnorm0 = rnorm0;
+    s.ttol = fmax(rtol * rnorm0, abstol);
+    s.it = 0;
+    s.max_it = max_it;
+    s.rho = tot[0];
+    s.rhoold = 1.0;
+    s.alpha = 1.0;
+    s.omegaold = 1.0;
+    s.omega = 1.0;
+    s.beta = s.rho;  // (rho/rhoold)*(alpha/omegaold) with rhoold = alpha = omegaold = 1
+    s.status = UFE_OK;
+    s.tbreak = 0;
+    s.active = 1;
+    if (isnan(dp)) { s.status = UFE_ERR_NAN; s.active = 0; }
+    else if (dp <= s.ttol) s.active = 0;
+    else if (s.rho == 0.0) { s.status = UFE_ERR_DIVERGED; s.active = 0; }
+    *ks = s;
+    set_cond(cond, s.active);
+  }
+}
+
+template <class M>
+__global__ void k_p_spmv(M mat, KV<typename M::Vec> v, KrylovScalars *ks, double *partials,
+                         unsigned int *tickets) {
+  using Vec = typename M::Vec;
+  using R = typename ScalarOf<Vec>::T;
+  const KrylovScalars s = *ks;
+  if (!s.active) return;
+  const int cur = s.it & 1, nxt = cur ^ 1;
+  const R beta = (R)s.beta, bw = (R)(s.beta * s.omegaold);
+  const Vec *__restrict__ Po = v.P[cur];
+  const Vec *__restrict__ Vo = v.V[cur];
+  const Vec *__restrict__ Rr = v.R;
+  double acc[1] = {0.0};
+  KRYLOV_ROWS(M, i, lane) {
+    const int i = (int)i_64;
+    const bool live = i < mat.items;
+    Vec part = live ? mat.row_partial(i, lane, [&](int j) { return v_pupd(Rr[j], bw, Vo[j], beta, Po[j]); })
+                    : v_zero<Vec>();
+    Vec y = lane_reduce<M::kLanes>(part);
+    if (live && lane == 0) {
+      v.P[nxt][i] = v_pupd(Rr[i], bw, Vo[i], beta, Po[i]);
+      Vec vn = v_mul(v.dinv[i], y);
+      v.V[nxt][i] = vn;
+      acc[0] += v_dot(vn, v.RP[i]);
+    }
+  }
+  double tot[1];
+  if (grid_sum<1>(acc, partials, tickets + kSiteP, tot)) {
+    KrylovScalars t = *ks;
+    double d1 = tot[0];
+    if (d1 == 0.0 || isnan(d1)) { t.status = isnan(d1) ? UFE_ERR_NAN : UFE_ERR_DIVERGED; t.active = 0; }
+    else t.alpha = t.rho / d1;
+    *ks = t;
+  }
+}
+
+template <class M>
+__global__ void k_s_spmv(M mat, KV<typename M::Vec> v, KrylovScalars *ks, double *partials,
+                         unsigned int *tickets) {
+  using Vec = typename M::Vec;
+  using R = typename ScalarOf<Vec>::T;
+  const KrylovScalars s = *ks;
+  if (!s.active) return;
+  const int nxt = (s.it & 1) ^ 1;
+  const R alpha = (R)s.alpha;
+  const Vec *__restrict__ Vn = v.V[nxt];
+  const Vec *__restrict__ Rr = v.R;
+  double acc[3] = {0.0, 0.0, 0.0};
+  KRYLOV_ROWS(M, i, lane) {
+    const int i = (int)i_64;
+    const bool live = i < mat.items;
+    Vec part = live ? mat.row_partial(i, lane, [&](int j) { return v_sub_scaled(Rr[j], alpha, Vn[j]); })
+                    : v_zero<Vec>();
+    Vec y = lane_reduce<M::kLanes>(part);
+    if (live && lane == 0) {
+      Vec si = v_sub_scaled(Rr[i], alpha, Vn[i]);
+      Vec ti = v_mul(v.dinv[i], y);
+      v.S[i] = si;
+      v.T[i] = ti;
+      acc[0] += v_dot(si, ti);
+      acc[1] += v_dot(ti, ti);
+      acc[2] += v_dot(si, si);
+    }
+  }
+  double tot[3];
+  if (grid_sum<3>(acc, partials, tickets + kSiteS, tot)) {
+    KrylovScalars t = *ks;
+    if (tot[1] == 0.0) {
+      // t = 0: if s = 0 too, x + alpha p solves the system (bcgs.c's breakdown branch)
+      if (tot[2] != 0.0) { t.status = UFE_ERR_DIVERGED; t.active = 0; }
+      else { t.omega = 0.0; t.tbreak = 1; }
+    } else if (isnan(tot[1])) {
+      t.status = UFE_ERR_NAN; t.active = 0;
+    } else {
+      t.omega = tot[0] / tot[1];
+    }
+    *ks = t;
+  }
+}
+
+template <class M>
+__global__ void k_xr(M mat, KV<typename M::Vec> v, KrylovScalars *ks, double *partials,
+                     unsigned int *tickets, CondArg cond) {
+  using Vec = typename M::Vec;
+  using R = typename ScalarOf<Vec>::T;
+  const KrylovScalars s = *ks;
+  if (!s.active) return;
+  const int nxt = (s.it & 1) ^ 1;
+  const R alpha = (R)s.alpha, omega = (R)s.omega;
+  double acc[2] = {0.0, 0.0};
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < mat.items; i += stride) {
+    Vec pi = v.P[nxt][i], si = v.S[i], ti = v.T[i];
+    v.X[i] = v_xupd(v.X[i], alpha, pi, omega, si);
+    Vec ri = v_sub_scaled(si, omega, ti);
+    v.R[i] = ri;
+    acc[0] += v_dot(ri, v.RP[i]);
+    acc[1] += v_dot(ri, ri);
+  }
+  double tot[2];
+  if (grid_sum<2>(acc, partials, tickets + kSiteXR, tot)) {
+    KrylovScalars t = *ks;
+    t.it += 1;
+    t.total_its += 1;
+    double dp = sqrt(tot[1]);
+    t.dp = dp;
+    double rho_new = tot[0];
+    t.rhoold = t.rho;
+    t.omegaold = t.omega;
+    t.rho = rho_new;
+    if (t.tbreak) { t.active = 0; t.status = UFE_OK; t.dp = 0.0; }
+    else if (isnan(dp)) { t.status = UFE_ERR_NAN; t.active = 0; }
+    else if (dp <= t.ttol) { t.active = 0; }
+    else if (dp >= 1e4 * t.rnorm0) { t.status = UFE_ERR_DIVERGED; t.active = 0; }
+    else if (t.it >= t.max_it) { t.status = UFE_WARN_KRYLOV_MAXIT; t.active = 0; }
+    else if (rho_new == 0.0) { t.status = UFE_ERR_DIVERGED; t.active = 0; }
+    else t.beta = (t.rho / t.rhoold) * (t.alpha / t.omegaold);
+    *ks = t;
+    set_cond(cond, t.active);
+  }
+}
+
+// Grid for the Krylov kernels: enough blocks to cover the rows once, capped so that the
+// per-block partial sums fit the reduction area.
+template <class M>
+inline unsigned krylov_grid(const M &mat, int threads, int max_blocks) {
+  int64_t lanes = (int64_t)mat.items * M::kLanes;
+  int64_t b = (lanes + threads - 1) / threads;
+  if (b > max_blocks) b = max_blocks;
+  if (b < 1) b = 1;
+  return (unsigned)b;
+}

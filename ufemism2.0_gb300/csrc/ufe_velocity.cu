@@ -1,0 +1,1651 @@
+// The SSA/DIVA velocity solve on the GPU.
+//
+// One Picard (viscosity) iteration of solve_SSA / solve_DIVA
+// (src/UFEMISM/ice_dynamics/conservation_of_momentum/SSA_DIVA/SSA_main.f90:165-234,
+//  DIVA_main.f90:170-251) is a handful of fused kernels:
+//
+//   k_vertex_{ssa,diva}  one thread per vertex: the b->a operator row (strain rates, velocities
+//                        on vertices, DIVA vertical shear), Glen viscosity, N = eta H, the
+//                        sliding law (and DIVA's F-integral and beta_eff)
+//   k_assemble<MODE>     one thread per triangle: the a->b operator row (N_b, dN/dx, dN/dy,
+//                        beta_b), the 2x2-block stiffness row on the 2nd-order b_b pattern
+//                        (solve_linearised_SSA_DIVA.f90:180-641), the Jacobi diagonal, the FP32
+//                        copy, and the Krylov initial residual
+//   Krylov               ufe_krylov.cuh, three kernels per BiCGStab iteration
+//   k_finalize_{ssa,diva} velocity limits, relaxation, (DIVA basal velocity and stress), the
+//                        Picard L2 norm and divergence control (SSA_DIVA_utilities.f90:84-184)
+//
+// The whole solve is one CUDA graph: a conditional while-node for the Picard loop holds a
+// nested while-node for the Krylov loop; the last block of the relevant reduction sets each
+// loop condition on the device, so no host round trip happens inside a solve.
+#include <cmath>
+#include <cstring>
+#include <cstdlib>
+#include <algorithm>
+
+#include "ufe_krylov.cuh"
+
+namespace {
+
+constexpr double kIceDensity = 910.0;  // src/UPSY/basic/parameters.f90:23
+constexpr double kGrav = 9.81;         // parameters.f90:20
+constexpr int kMaxNz = 64;
+constexpr int kThreads = 256;
+constexpr int kMaxRefine = 60;
+
+enum ErrFlags : int { kErrNoDiag = 1, kErrBcNeighbour = 2, kErrNoNeighbour = 4 };
+
+int sm_count(ufe_ctx *ctx) {
+  static int cached = -1;
+  if (cached < 0) {
+    int v = 0;
+    cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, ctx->device);
+    cached = v > 0 ? v : 148;
+  }
+  return cached;
+}
+
+int max_grid(ufe_ctx *ctx) {
+  int g = sm_count(ctx) * 8;
+  return g < kMaxReduceBlocks ? g : kMaxReduceBlocks;
+}
+
+// ---- physics (device) ---------------------------------------------------------------------
+struct PhysParams {
+  int sliding_law, crossterms, gl_subgrid, has_bc;
+  int bc_u[4], bc_v[4];   // N, E, S, W
+  double n_glen, visc_eff_min, vel_max, m_weertman, delta_v, beta_max, fgr_exp;
+  double budd_q, budd_u0;
+  double picard_tol;
+  int visc_it_nit;
+};
+
+PhysParams make_phys(const ufe_solver_params &p, int has_bc) {
+  PhysParams q;
+  q.sliding_law = p.choice_sliding_law;
+  q.crossterms = p.do_include_SSADIVA_crossterms;
+  q.gl_subgrid = p.do_GL_subgrid_friction;
+  q.has_bc = has_bc;
+  q.bc_u[0] = p.BC_u_north; q.bc_u[1] = p.BC_u_east; q.bc_u[2] = p.BC_u_south; q.bc_u[3] = p.BC_u_west;
+  q.bc_v[0] = p.BC_v_north; q.bc_v[1] = p.BC_v_east; q.bc_v[2] = p.BC_v_south; q.bc_v[3] = p.BC_v_west;
+  q.n_glen = p.Glens_flow_law_exponent;
+  q.visc_eff_min = p.visc_eff_min;
+  q.vel_max = p.vel_max;
+  q.m_weertman = p.slid_Weertman_m;
+  q.delta_v = p.slid_delta_v;
+  q.beta_max = p.slid_beta_max;
+  q.fgr_exp = p.subgrid_friction_exponent_on_B_grid;
+  q.budd_q = p.slid_Budd_q_plastic;
+  q.budd_u0 = p.slid_Budd_u_threshold;
+  q.picard_tol = p.visc_it_norm_dUV_tol;
+  q.visc_it_nit = p.visc_it_nit;
+  return q;
+}
+
+// calc_effective_viscosity_Glen_2D / _3D_uv_only (constitutive_equation.f90:25-80)
+__device__ __forceinline__ double glen(double eps0, double ux, double uy, double vx, double vy,
+                                       double uz, double vz, double A, double n) {
+  double e = ux * ux + vy * vy + ux * vy + 0.25 * ((uy + vx) * (uy + vx)) + 0.25 * (uz * uz + vz * vz) + eps0;
+  return 0.5 * pow(A, -1.0 / n) * pow(e, (1.0 - n) / (2.0 * n));
+}
+__device__ __forceinline__ double glen2d(double eps0, double ux, double uy, double vx, double vy,
+                                         double A, double n) {
+  double e = ux * ux + vy * vy + ux * vy + 0.25 * ((uy + vx) * (uy + vx)) + eps0;
+  return 0.5 * pow(A, -1.0 / n) * pow(e, (1.0 - n) / (2.0 * n));
+}
+
+struct SlidingIn {
+  const double *beta_sq, *alpha_sq, *effp, *tys;
+};
+
+// velocity-dependent part of the sliding laws (sliding_laws.f90:25-351) and the beta_max cap (:76)
+__device__ double sliding_beta(const PhysParams &q, const SlidingIn &s, int vi, double u, double v) {
+  double uabs = sqrt(q.delta_v * q.delta_v + u * u + v * v);
+  double m = q.m_weertman, beta = 0.0;
+  switch (q.sliding_law) {
+    case UFE_SLIDING_NO_SLIDING: beta = 0.0; break;
+    case UFE_SLIDING_WEERTMAN: beta = s.beta_sq[vi] * pow(uabs, 1.0 / m - 1.0); break;
+    case UFE_SLIDING_COULOMB: beta = s.tys[vi] / uabs; break;
+    case UFE_SLIDING_BUDD:
+      beta = s.tys[vi] * pow(uabs, q.budd_q - 1.0) / pow(q.budd_u0, q.budd_q);
+      break;
+    case UFE_SLIDING_TSAI2015:
+      beta = fmin(s.alpha_sq[vi] * s.effp[vi], s.beta_sq[vi] * pow(uabs, 1.0 / m)) * pow(uabs, -1.0);
+      break;
+    case UFE_SLIDING_SCHOOF2005: {
+      double b = s.beta_sq[vi], aN = s.alpha_sq[vi] * s.effp[vi];
+      beta = ((b * pow(uabs, 1.0 / m) * s.alpha_sq[vi] * s.effp[vi]) / pow(pow(b, m) * uabs + pow(aN, m), 1.0 / m)) *
+             pow(uabs, -1.0);
+      break;
+    }
+    default: beta = 0.0;
+  }
+  return fmin(q.beta_max, beta);
+}
+
+struct OpRow {  // a CSR family with shared pattern
+  const int32_t *ptr, *ind;
+  const double *v0, *v1, *v2;
+};
+
+// ---- prologue: driving stress (calc_driving_stress, SSA_DIVA_utilities.f90:21-57) and the
+// vertically averaged flow factor (calc_vertically_averaged_flow_parameter, SSA_main.f90:312-337)
+__global__ void k_prologue(int nV, int nTri, int nz, OpRow ab, const double *Hi, const double *Hs,
+                           const double *A_flow, const double *zeta, double2 *tau_d, double *Avav,
+                           PicardScalars *ps, KrylovScalars *ks, double relax0, double eps0, double n_glen) {
+  int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < nTri; t += stride) {
+    double Hib = 0.0, dx = 0.0, dy = 0.0;
+    for (int k = ab.ptr[t]; k < ab.ptr[t + 1]; ++k) {
+      int v = ab.ind[k];
+      Hib = Hib + ab.v0[k] * Hi[v];
+      dx = dx + ab.v1[k] * Hs[v];
+      dy = dy + ab.v2[k] * Hs[v];
+    }
+    tau_d[t] = make_double2(-kIceDensity * kGrav * Hib * dx, -kIceDensity * kGrav * Hib * dy);
+  }
+  if (Avav)
+    for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < nV; v += stride) {
+      double a = 0.0;
+      for (int k = 1; k < nz; ++k)
+        a = a + 0.5 * (A_flow[(int64_t)k * nV + v] + A_flow[(int64_t)(k - 1) * nV + v]) * (zeta[k] - zeta[k - 1]);
+      Avav[v] = a;
+    }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    PicardScalars p;
+    memset(&p, 0, sizeof(p));
+    p.L2 = 1e9;
+    p.L2_prev = 1e9;
+    p.relax = relax0;
+    p.eps0 = eps0;
+    p.eta_max = 0.5 * pow(1e-18, -1.0 / n_glen) * pow(eps0, (1.0 - n_glen) / (2.0 * n_glen));
+    p.active = 1;
+    *ps = p;
+    KrylovScalars k;
+    memset(&k, 0, sizeof(k));
+    *ks = k;
+  }
+}
+
+// ---- SSA vertex kernel ----------------------------------------------------------------------
+// calc_horizontal_strain_rates (SSA_DIVA_utilities.f90:59-82), calc_effective_viscosity
+// (SSA_main.f90:339-392) up to N_a, and the vertex part of calc_basal_friction_coefficient
+// (sliding_laws.f90:25-81): all from one pass over the b->a operator row.
+__global__ void k_vertex_ssa(int nV, OpRow ba, const double2 *uv, const double *Avav, const double *Hi,
+                             SlidingIn sl, PhysParams q, const PicardScalars *ps, double *N_a, double *beta_a) {
+  const double eps0 = ps->eps0, eta_max = ps->eta_max;
+  int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t vi = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; vi < nV; vi += stride) {
+    double ux = 0, uy = 0, vx = 0, vy = 0, ua = 0, va = 0;
+    for (int k = ba.ptr[vi]; k < ba.ptr[vi + 1]; ++k) {
+      double2 w = uv[ba.ind[k]];
+      double m = ba.v0[k], dx = ba.v1[k], dy = ba.v2[k];
+      ux = ux + dx * w.x;
+      uy = uy + dy * w.x;
+      vx = vx + dx * w.y;
+      vy = vy + dy * w.y;
+      ua = ua + m * w.x;
+      va = va + m * w.y;
+    }
+    double eta = glen2d(eps0, ux, uy, vx, vy, Avav[vi], q.n_glen);
+    eta = fmin(fmax(eta, q.visc_eff_min), eta_max);
+    N_a[vi] = eta * fmax(0.1, Hi[vi]);
+    beta_a[vi] = sliding_beta(q, sl, (int)vi, ua, va);
+  }
+}
+
+// ---- DIVA vertex kernel ---------------------------------------------------------------------
+// calc_horizontal_strain_rates, calc_vertical_shear_strain_rates (DIVA_main.f90:375-410),
+// calc_effective_viscosity (:412-479), the surface value of calc_F_integrals' F2 (:481-520) and
+// the vertex part of calc_effective_basal_friction_coefficient (:522-574).
+__global__ void k_vertex_diva(int nV, int nTri, int nz, OpRow ba, const double2 *uv, const double2 *uv_base,
+                              const double2 *tau_b, const double *eta_3D_b, const double *A_flow,
+                              const double *Hi, const double *zeta_g, SlidingIn sl, PhysParams q,
+                              const PicardScalars *ps, double *eta_3D_a, double *N_a, double *F2a1,
+                              double *beta_a, double *beta_eff_a) {
+  __shared__ double zeta[kMaxNz];
+  for (int k = threadIdx.x; k < nz; k += blockDim.x) zeta[k] = zeta_g[k];
+  __syncthreads();
+  const double eps0 = ps->eps0, eta_max = ps->eta_max;
+  const float h_floor_sp = 0.1f;  // max(0.1, Hi) with a default-real literal (DIVA_main.f90:468)
+  int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t vi = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; vi < nV; vi += stride) {
+    const int k1 = ba.ptr[vi], k2 = ba.ptr[vi + 1];
+    double ux = 0, uy = 0, vx = 0, vy = 0, ua = 0, va = 0;
+    for (int k = k1; k < k2; ++k) {
+      int tj = ba.ind[k];
+      double2 w = uv[tj], wb = uv_base[tj];
+      double m = ba.v0[k], dx = ba.v1[k], dy = ba.v2[k];
+      ux = ux + dx * w.x;
+      uy = uy + dy * w.x;
+      vx = vx + dx * w.y;
+      vy = vy + dy * w.y;
+      ua = ua + m * wb.x;
+      va = va + m * wb.y;
+    }
+    double eta_k[kMaxNz];
+    for (int l = 0; l < nz; ++l) {
+      double duz = 0.0, dvz = 0.0;
+      for (int k = k1; k < k2; ++k) {
+        int tj = ba.ind[k];
+        double e = fmax(q.visc_eff_min, eta_3D_b[(int64_t)l * nTri + tj]);
+        double2 tb = tau_b[tj];
+        double m = ba.v0[k];
+        duz = duz + m * (tb.x * zeta[l] / e);
+        dvz = dvz + m * (tb.y * zeta[l] / e);
+      }
+      int64_t ix = (int64_t)l * nV + vi;
+      double e = glen(eps0, ux, uy, vx, vy, duz, dvz, A_flow[ix], q.n_glen);
+      e = fmin(fmax(e, q.visc_eff_min), eta_max);
+      eta_k[l] = e;
+      eta_3D_a[ix] = e;
+    }
+    double vav = 0.0;
+    for (int l = 1; l < nz; ++l) vav = vav + 0.5 * (eta_k[l] + eta_k[l - 1]) * (zeta[l] - zeta[l - 1]);
+    N_a[vi] = vav * fmax((double)h_floor_sp, Hi[vi]);
+    // F2 at the surface: integrate zeta^2/eta from the base (zeta = 1) up to zeta(1) = 0
+    double intg = 0.0;
+    for (int l = nz - 1; l >= 1; --l) {
+      double f1 = zeta[l] * zeta[l] / eta_k[l], f0 = zeta[l - 1] * zeta[l - 1] / eta_k[l - 1];
+      intg = intg - 0.5 * (f1 + f0) * (zeta[l] - zeta[l - 1]);
+    }
+    double F2 = -fmax(0.1, Hi[vi]) * intg;
+    F2a1[vi] = F2;
+    double b = sliding_beta(q, sl, (int)vi, ua, va);
+    beta_a[vi] = b;
+    beta_eff_a[vi] = (q.sliding_law == UFE_SLIDING_NO_SLIDING) ? 1.0 / F2 : b / (1.0 + b * F2);
+  }
+}
+
+// ---- assembly -----------------------------------------------------------------------------
+enum AssembleMode : int { kFromTriangles = 0, kFromSSA = 1, kFromDIVA = 2 };
+
+struct AssembleArgs {
+  int nV, nTri, nz;
+  OpRow ab;
+  const int32_t *m2_ptr, *m2_ind;
+  const double *m2_x, *m2_y, *m2_xx, *m2_xy, *m2_yy;
+  const int32_t *TriBI, *TriC;
+  // inputs (by mode)
+  const double *N_b, *dNx_b, *dNy_b, *beta_b_in;          // kFromTriangles
+  const double *N_a, *beta_a, *beta_eff_a, *F2a1, *eta_3D_a; // kFromSSA / kFromDIVA
+  const double *fgr_b;
+  const double2 *tau_d;
+  const int32_t *bc_mask;
+  const double2 *bc_uv;
+  const double2 *x0;        // Krylov initial guess (or null = zero)
+  // outputs
+  double4 *blk;
+  float4 *blk32;
+  double2 *rhs, *dinv, *X, *R, *RP, *P0, *V0;
+  float2 *dinv32;
+  double *beta_b_out, *bfc_b, *F2b1, *eta_3D_b;
+  int *err;
+  // Krylov
+  KrylovScalars *ks;
+  double rtol, abstol;
+  int max_it;
+  double *partials;
+  unsigned int *tickets;
+};
+
+__device__ __forceinline__ int find_col(const int32_t *ind, int k1, int k2, int col) {
+  for (int k = k1; k < k2; ++k)
+    if (ind[k] == col) return k;
+  return -1;
+}
+
+template <int MODE>
+__global__ void k_assemble(AssembleArgs a, PhysParams q, CondArg cond) {
+  double acc[2] = {0.0, 0.0};
+  const int nTri = a.nTri;
+  int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t t64 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t64 < nTri; t64 += stride) {
+    const int t = (int)t64;
+    // -- coefficients of this triangle
+    double N, dNx, dNy, beta;
+    if (MODE == kFromTriangles) {
+      N = a.N_b[t]; dNx = a.dNx_b[t]; dNy = a.dNy_b[t]; beta = a.beta_b_in[t];
+    } else {
+      N = 0.0; dNx = 0.0; dNy = 0.0; beta = 0.0;
+      double bfc = 0.0, f2 = 0.0;
+      const double *bsrc = (MODE == kFromSSA) ? a.beta_a : a.beta_eff_a;
+      for (int k = a.ab.ptr[t]; k < a.ab.ptr[t + 1]; ++k) {
+        int v = a.ab.ind[k];
+        double m = a.ab.v0[k], na = a.N_a[v];
+        N = N + m * na;
+        dNx = dNx + a.ab.v1[k] * na;
+        dNy = dNy + a.ab.v2[k] * na;
+        beta = beta + m * bsrc[v];
+        if (MODE == kFromDIVA) {
+          bfc = bfc + m * a.beta_a[v];
+          f2 = f2 + m * a.F2a1[v];
+        }
+      }
+      if (q.gl_subgrid) beta = beta * pow(a.fgr_b[t], q.fgr_exp);
+      if (MODE == kFromDIVA) {
+        a.bfc_b[t] = bfc;
+        a.F2b1[t] = f2;
+        for (int l = 0; l < a.nz; ++l) {
+          double e = 0.0;
+          for (int k = a.ab.ptr[t]; k < a.ab.ptr[t + 1]; ++k)
+            e = e + a.ab.v0[k] * a.eta_3D_a[(int64_t)l * a.nV + a.ab.ind[k]];
+          a.eta_3D_b[(int64_t)l * nTri + t] = e;
+        }
+      }
+      a.beta_b_out[t] = beta;
+    }
+    // -- block row on the 2nd-order b_b pattern
+    const int k1 = a.m2_ptr[t], k2 = a.m2_ptr[t + 1];
+    const int kd = find_col(a.m2_ind, k1, k2, t);
+    if (kd < 0) { atomicOr(a.err, kErrNoDiag); continue; }
+    double2 rhs;
+    const int bcm = q.has_bc ? a.bc_mask[t] : 0;
+    const int tbi = a.TriBI[t];
+    if (bcm == 1 || tbi > 0) {
+      for (int k = k1; k < k2; ++k) a.blk[k] = make_double4(0.0, 0.0, 0.0, 0.0);
+      double *bd = reinterpret_cast<double *>(a.blk);
+      if (bcm == 1) {
+        // prescribed velocity (solve_linearised_SSA_DIVA.f90:94-109)
+        bd[4 * (int64_t)kd + 0] = 1.0;
+        bd[4 * (int64_t)kd + 3] = 1.0;
+        rhs = a.bc_uv[t];
+      } else {
+        // domain border (:111-143, row routine :481-641)
+        const int side = (tbi - 1) / 2;  // 0 N (1,2), 1 E (3,4), 2 S (5,6), 3 W (7,8)
+        rhs = make_double2(0.0, 0.0);
+        for (int uvc = 0; uvc < 2; ++uvc) {
+          const int choice = uvc == 0 ? q.bc_u[side] : q.bc_v[side];
+          const int comp = uvc == 0 ? 0 : 3;  // uu or vv entry of the block
+          if (choice == UFE_BC_INFINITE) {
+            int nnb = 0;
+            for (int n = 0; n < 3; ++n) {
+              int tj = a.TriC[(int64_t)n * nTri + t];
+              if (tj == 0) continue;
+              nnb++;
+              int kk = find_col(a.m2_ind, k1, k2, tj - 1);
+              if (kk < 0) { atomicOr(a.err, kErrBcNeighbour); continue; }
+              bd[4 * (int64_t)kk + comp] = 1.0;
+            }
+            if (nnb == 0) atomicOr(a.err, kErrNoNeighbour);
+            bd[4 * (int64_t)kd + comp] = -1.0 * (double)nnb;
+          } else {  // UFE_BC_ZERO
+            bd[4 * (int64_t)kd + comp] = 1.0;
+          }
+        }
+      }
+    } else {
+      // free rows (calc_SSA_DIVA_stiffness_matrix_row_free :180-329, sans variant :331-479)
+      for (int k = k1; k < k2; ++k) {
+        const int tj = a.m2_ind[k];
+        const double x_ = a.m2_x[k], y_ = a.m2_y[k], xx = a.m2_xx[k], xy = a.m2_xy[k], yy = a.m2_yy[k];
+        double uAu, uAv, vAu, vAv;
+        if (q.crossterms) {
+          uAu = 4.0 * N * xx + 4.0 * dNx * x_ + N * yy + dNy * y_;
+          uAv = 3.0 * N * xy + 2.0 * dNx * y_ + dNy * x_;
+          vAv = 4.0 * N * yy + 4.0 * dNy * y_ + N * xx + dNx * x_;
+          vAu = 3.0 * N * xy + 2.0 * dNy * x_ + dNx * y_;
+          if (tj == t) { uAu = uAu - beta; vAv = vAv - beta; }
+        } else {
+          uAu = 4.0 * xx + yy;
+          uAv = 3.0 * xy;
+          vAv = 4.0 * yy + xx;
+          vAu = 3.0 * xy;
+          if (tj == t) { uAu = uAu - beta / N; vAv = vAv - beta / N; }
+        }
+        a.blk[k] = make_double4(uAu, uAv, vAu, vAv);
+      }
+      double2 td = a.tau_d[t];
+      rhs = q.crossterms ? make_double2(-td.x, -td.y) : make_double2(-td.x / N, -td.y / N);
+    }
+    // -- Jacobi diagonal (PCJACOBI; a zero diagonal entry is replaced by one)
+    const double4 dg = a.blk[kd];
+    const double2 di = make_double2(dg.x != 0.0 ? 1.0 / dg.x : 1.0, dg.w != 0.0 ? 1.0 / dg.w : 1.0);
+    a.dinv[t] = di;
+    a.rhs[t] = rhs;
+    if (a.blk32) {
+      for (int k = k1; k < k2; ++k) {
+        double4 b = a.blk[k];
+        a.blk32[k] = make_float4((float)b.x, (float)b.y, (float)b.z, (float)b.w);
+      }
+      a.dinv32[t] = make_float2((float)di.x, (float)di.y);
+    }
+    // -- Krylov initial residual r = D^-1 (b - A x0)
+    double2 ax = make_double2(0.0, 0.0);
+    double2 x0t = make_double2(0.0, 0.0);
+    if (a.x0) {
+      x0t = a.x0[t];
+      for (int k = k1; k < k2; ++k) {
+        double4 b = a.blk[k];
+        double2 xj = a.x0[a.m2_ind[k]];
+        ax.x += b.x * xj.x + b.y * xj.y;
+        ax.y += b.z * xj.x + b.w * xj.y;
+      }
+    }
+    a.X[t] = x0t;
+    double2 r = make_double2(di.x * (rhs.x - ax.x), di.y * (rhs.y - ax.y));
+    double2 db = make_double2(di.x * rhs.x, di.y * rhs.y);
+    a.R[t] = r;
+    a.RP[t] = r;
+    a.P0[t] = make_double2(0.0, 0.0);
+    a.V0[t] = make_double2(0.0, 0.0);
+    acc[0] += r.x * r.x + r.y * r.y;
+    acc[1] += db.x * db.x + db.y * db.y;
+  }
+  double tot[2];
+  if (grid_sum<2>(acc, a.partials, a.tickets + kSiteInit, tot)) {
+    double dp = sqrt(tot[0]);
+    double bnorm = sqrt(tot[1]);
+    double rnorm0 = bnorm != 0.0 ? bnorm : dp;
+    KrylovScalars s = *a.ks;
+    s.dp = dp;
+    s.rnorm0 = rnorm0;
+    s.ttol = fmax(a.rtol * rnorm0, a.abstol);
+    s.it = 0;
+    s.max_it = a.max_it;
+    s.rho = tot[0];
+    s.rhoold = 1.0;
+    s.alpha = 1.0;
+    s.omegaold = 1.0;
+    s.omega = 1.0;
+    s.beta = s.rho;
+    s.status = UFE_OK;
+    s.tbreak = 0;
+    s.refinements = 0;
+    s.active = 1;
+    if (isnan(dp)) { s.status = UFE_ERR_NAN; s.active = 0; }
+    else if (dp <= s.ttol) s.active = 0;
+    else if (s.rho == 0.0) { s.status = UFE_ERR_DIVERGED; s.active = 0; }
+    *a.ks = s;
+    set_cond(cond, s.active);
+  }
+}
+
+// ---- FP32 inner solve with FP64 refinement --------------------------------------------------
+// inner system: (D^-1 A) d = r with r the FP64 residual, solved from d = 0 in FP32
+__global__ void k_inner_init(int nTri, const double2 *R, float2 *R32, float2 *RP32, float2 *x32,
+                             float2 *P32, float2 *V32, const KrylovScalars *outer, KrylovScalars *ks32,
+                             double inner_rtol, int max_it, double *partials, unsigned int *tickets,
+                             CondArg cond) {
+  double acc[1] = {0.0};
+  int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < nTri; t += stride) {
+    double2 r = R[t];
+    float2 r32 = make_float2((float)r.x, (float)r.y);
+    R32[t] = r32;
+    RP32[t] = r32;
+    x32[t] = make_float2(0.f, 0.f);
+    P32[t] = make_float2(0.f, 0.f);
+    V32[t] = make_float2(0.f, 0.f);
+    acc[0] += (double)r32.x * r32.x + (double)r32.y * r32.y;
+  }
+  double tot[1];
+  if (grid_sum<1>(acc, partials, tickets + kSiteInner, tot)) {
+    KrylovScalars s;
+    memset(&s, 0, sizeof(s));
+    const KrylovScalars o = *outer;
+    s.total_its = ks32->total_its;
+    double dp = sqrt(tot[0]);
+    s.dp = dp;
+    s.rnorm0 = dp;
+    // reduce the residual by inner_rtol, but never below what the outer test needs
+    s.ttol = fmax(inner_rtol * dp, 0.5 * o.ttol);
+    s.max_it = max_it;
+    s.rho = tot[0];
+    s.rhoold = s.alpha = s.omegaold = s.omega = 1.0;
+    s.beta = s.rho;
+    s.active = (dp > s.ttol && s.rho != 0.0) ? 1 : 0;
+    *ks32 = s;
+    set_cond(cond, s.active);
+  }
+}
+
+__global__ void k_xadd(int nTri, double2 *X, const float2 *x32) {
+  int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < nTri; t += stride) {
+    double2 x = X[t];
+    float2 d = x32[t];
+    X[t] = make_double2(x.x + (double)d.x, x.y + (double)d.y);
+  }
+}
+
+// FP64 residual r = D^-1 (b - A x) and the outer (refinement) convergence test
+template <int L>
+__global__ void k_residual64(BsrMat<double, L> mat, const double2 *X, const double2 *B, const double2 *dinv,
+                             double2 *R, KrylovScalars *ks, const KrylovScalars *ks32, double *partials,
+                             unsigned int *tickets, CondArg cond) {
+  using MT = BsrMat<double, L>;
+  double acc[1] = {0.0};
+  KRYLOV_ROWS(MT, i, lane) {
+    const int i = (int)i_64;
+    const bool live = i < mat.items;
+    double2 part = live ? mat.row_partial(i, lane, [&](int j) { return X[j]; }) : make_double2(0.0, 0.0);
+    double2 ax = lane_reduce<L>(part);
+    if (live && lane == 0) {
+      double2 b = B[i], d = dinv[i];
+      double2 r = make_double2(d.x * (b.x - ax.x), d.y * (b.y - ax.y));
+      R[i] = r;
+      acc[0] += r.x * r.x + r.y * r.y;
+    }
+  }
+  double tot[1];
+  if (grid_sum<1>(acc, partials, tickets + kSiteResid, tot)) {
+    KrylovScalars s = *ks;
+    const KrylovScalars in = *ks32;
+    double dp = sqrt(tot[0]);
+    s.dp = dp;
+    s.refinements += 1;
+    s.it += in.it;
+    if (in.status < 0 && in.status != UFE_ERR_DIVERGED) { s.status = in.status; s.active = 0; }
+    else if (isnan(dp)) { s.status = UFE_ERR_NAN; s.active = 0; }
+    else if (dp <= s.ttol) s.active = 0;
+    else if (s.refinements >= kMaxRefine || s.it >= s.max_it) { s.status = UFE_WARN_KRYLOV_MAXIT; s.active = 0; }
+    *ks = s;
+    set_cond(cond, s.active);
+  }
+}
+
+// ---- Picard bookkeeping ---------------------------------------------------------------------
+// Divergence control of SSA_main.f90:196-213 / DIVA_main.f90:211-228, convergence (:222-225),
+// iteration limit (:228-232).  Runs in the last block of the finalize reduction.
+__device__ void picard_step(PicardScalars *psp, KrylovScalars *ks, double r1, double r2, const PhysParams &q,
+                            double n_glen, CondArg cond) {
+  PicardScalars p = *psp;
+  KrylovScalars k = *ks;
+  p.it += 1;
+  p.n_refine += k.refinements;
+  if (k.status < 0) {
+    p.status = k.status;
+    p.active = 0;
+    *psp = p;
+    set_cond(cond, 0);
+    return;
+  }
+  if (k.status == UFE_WARN_KRYLOV_MAXIT) p.status = UFE_WARN_KRYLOV_MAXIT;
+  p.L2_prev = p.L2;
+  p.L2 = 2.0 * r1 / fmax(r2, 1e-8);
+  if (p.L2 > p.L2_prev) p.nit_diverg += 1; else p.nit_diverg = 0;
+  if (p.nit_diverg > 2) {
+    p.nit_diverg = 0;
+    p.relax = p.relax * 0.9;
+    p.eps0 = p.eps0 * 1.2;
+    p.eta_max = 0.5 * pow(1e-18, -1.0 / n_glen) * pow(p.eps0, (1.0 - n_glen) / (2.0 * n_glen));
+  }
+  int stop = 0;
+  if (p.relax <= 0.05 || p.eps0 >= 1e-5) {
+    if (p.relax < 0.05 || p.eps0 > 1e-5) { p.status = UFE_ERR_DIVERGED; stop = 1; }
+  }
+  if (isnan(p.L2)) { p.status = UFE_ERR_NAN; stop = 1; }
+  int converged = p.L2 < q.picard_tol;
+  if (!stop && !converged && p.it > q.visc_it_nit) {
+    if (p.status == UFE_OK) p.status = UFE_WARN_PICARD_MAXIT;
+    stop = 1;
+  }
+  if (!stop && converged && p.it > q.visc_it_nit && p.status == UFE_OK) {
+    // converged on the last allowed iteration: the reference still warns (SSA_main.f90:229)
+    p.status = UFE_WARN_PICARD_MAXIT;
+  }
+  p.active = (!stop && !converged) ? 1 : 0;
+  *psp = p;
+  set_cond(cond, p.active);
+}
+
+// apply_velocity_limits + relax_viscosity_iterations + calc_L2_norm_uv (SSA_DIVA_utilities.f90:84-184)
+template <bool DIVA>
+__global__ void k_finalize(int nTri, const double2 *X, double2 *uv, PhysParams q, PicardScalars *ps,
+                           KrylovScalars *ks, const double *beta_eff_b, const double *bfc_b, const double *F2b1,
+                           double2 *uv_base, double2 *tau_b, double *partials, unsigned int *tickets,
+                           CondArg cond) {
+  const double r = ps->relax;
+  double acc[2] = {0.0, 0.0};
+  int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < nTri; t += stride) {
+    double2 x = X[t], o = uv[t];
+    double u = x.x, v = x.y;
+    double uabs = sqrt(u * u + v * v);
+    if (uabs > q.vel_max) { u = u * q.vel_max / uabs; v = v * q.vel_max / uabs; }
+    u = (r * u) + ((1.0 - r) * o.x);
+    v = (r * v) + ((1.0 - r) * o.y);
+    uv[t] = make_double2(u, v);
+    if (DIVA) {
+      if (q.sliding_law == UFE_SLIDING_NO_SLIDING) uv_base[t] = make_double2(0.0, 0.0);
+      else {
+        double den = 1.0 + bfc_b[t] * F2b1[t];
+        uv_base[t] = make_double2(u / den, v / den);
+      }
+      double be = beta_eff_b[t];
+      tau_b[t] = make_double2(u * be, v * be);
+    }
+    acc[0] += (u - o.x) * (u - o.x) + (v - o.y) * (v - o.y);
+    acc[1] += (u + o.x) * (u + o.x) + (v + o.y) * (v + o.y);
+  }
+  double tot[2];
+  if (grid_sum<2>(acc, partials, tickets + kSitePicard, tot)) picard_step(ps, ks, tot[0], tot[1], q, q.n_glen, cond);
+}
+
+// ---- DIVA 3-D velocities (calc_3D_velocities, DIVA_main.f90:629-676) -------------------------
+__global__ void k_diva_F1(int nV, int nz, const double *eta_3D_a, const double *Hi, const double *zeta_g,
+                          double *F1_3D_a) {
+  __shared__ double zeta[kMaxNz];
+  for (int k = threadIdx.x; k < nz; k += blockDim.x) zeta[k] = zeta_g[k];
+  __syncthreads();
+  int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t vi = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; vi < nV; vi += stride) {
+    double h = fmax(0.1, Hi[vi]);
+    double intg = 0.0;
+    F1_3D_a[(int64_t)(nz - 1) * nV + vi] = -h * intg;
+    for (int l = nz - 1; l >= 1; --l) {
+      double f1 = zeta[l] / eta_3D_a[(int64_t)l * nV + vi];
+      double f0 = zeta[l - 1] / eta_3D_a[(int64_t)(l - 1) * nV + vi];
+      intg = intg - 0.5 * (f1 + f0) * (zeta[l] - zeta[l - 1]);
+      F1_3D_a[(int64_t)(l - 1) * nV + vi] = -h * intg;
+    }
+  }
+}
+
+__global__ void k_diva_u3d(int nV, int nTri, int nz, OpRow ab, const double *F1_3D_a, const double2 *uv_base,
+                           const double2 *tau_b, const double *bfc_b, int no_sliding, double *u3, double *v3) {
+  int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  int64_t total = (int64_t)nTri * nz;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += stride) {
+    int l = (int)(e / nTri), t = (int)(e - (int64_t)l * nTri);
+    double f = 0.0;
+    for (int k = ab.ptr[t]; k < ab.ptr[t + 1]; ++k) f = f + ab.v0[k] * F1_3D_a[(int64_t)l * nV + ab.ind[k]];
+    if (no_sliding) {
+      double2 tb = tau_b[t];
+      u3[e] = tb.x * f;
+      v3[e] = tb.y * f;
+    } else {
+      double2 ub = uv_base[t];
+      double c = 1.0 + bfc_b[t] * f;
+      u3[e] = ub.x * c;
+      v3[e] = ub.y * c;
+    }
+  }
+}
+
+// ---- small helpers ---------------------------------------------------------------------------
+__global__ void k_interleave(int n, const double *a, const double *b, double2 *out) {
+  int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
+    out[i] = make_double2(a ? a[i] : 0.0, b ? b[i] : 0.0);
+}
+
+__global__ void k_deinterleave(int n, const double2 *in, double *a, double *b) {
+  int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    double2 w = in[i];
+    a[i] = w.x;
+    b[i] = w.y;
+  }
+}
+
+// Export of the stiffness matrix in the reference's CSR layout (rows 2(ti-1)+uv, entries in the
+// order add_entry_CSR_dist appends them): first the row lengths, then the entries.
+__device__ int bc_choice_dev(const PhysParams &q, int tbi, int uvc) {
+  int side = (tbi - 1) / 2;
+  return uvc == 0 ? q.bc_u[side] : q.bc_v[side];
+}
+
+__global__ void k_export_len(int nTri, const int32_t *m2_ptr, const int32_t *TriBI, const int32_t *TriC,
+                             const int32_t *bc_mask, PhysParams q, int32_t *rowlen) {
+  int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < nTri; t += stride) {
+    int len_free = 2 * (m2_ptr[t + 1] - m2_ptr[t]);
+    int bcm = q.has_bc ? bc_mask[t] : 0;
+    for (int uvc = 0; uvc < 2; ++uvc) {
+      int len;
+      if (bcm == 1) len = 1;
+      else if (TriBI[t] > 0) {
+        if (bc_choice_dev(q, TriBI[t], uvc) == UFE_BC_INFINITE) {
+          int nnb = 0;
+          for (int n = 0; n < 3; ++n) nnb += TriC[(int64_t)n * nTri + t] != 0;
+          len = nnb + 1;
+        } else len = 1;
+      } else len = len_free;
+      rowlen[2 * t + uvc] = len;
+    }
+  }
+}
+
+__global__ void k_export_fill(int nTri, const int32_t *m2_ptr, const int32_t *m2_ind, const int32_t *TriBI,
+                              const int32_t *TriC, const int32_t *bc_mask, PhysParams q, const double4 *blk,
+                              const int32_t *ptr, int32_t *ind, double *val) {
+  int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t t64 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t64 < nTri; t64 += stride) {
+    const int t = (int)t64;
+    const int k1 = m2_ptr[t], k2 = m2_ptr[t + 1];
+    const int kd = find_col(m2_ind, k1, k2, t);
+    const int bcm = q.has_bc ? bc_mask[t] : 0;
+    const double *bd = reinterpret_cast<const double *>(blk);
+    for (int uvc = 0; uvc < 2; ++uvc) {
+      const int row = 2 * t + uvc;   // 0-based row of the reference's 2(ti-1)+uv
+      int p = ptr[row];
+      const int comp = uvc == 0 ? 0 : 3;
+      if (bcm == 1) {
+        ind[p] = row; val[p] = 1.0;
+      } else if (TriBI[t] > 0) {
+        if (bc_choice_dev(q, TriBI[t], uvc) == UFE_BC_INFINITE) {
+          int nnb = 0;
+          for (int n = 0; n < 3; ++n) {
+            int tj = TriC[(int64_t)n * nTri + t];
+            if (tj == 0) continue;
+            nnb++;
+            ind[p] = 2 * (tj - 1) + uvc; val[p] = 1.0; ++p;
+          }
+          ind[p] = row; val[p] = -1.0 * (double)nnb;
+        } else {
+          ind[p] = row; val[p] = 1.0;
+        }
+      } else {
+        for (int k = k1; k < k2; ++k) {
+          int tj = m2_ind[k];
+          ind[p] = 2 * tj;     val[p] = bd[4 * (int64_t)k + (uvc == 0 ? 0 : 2)]; ++p;
+          ind[p] = 2 * tj + 1; val[p] = bd[4 * (int64_t)k + (uvc == 0 ? 1 : 3)]; ++p;
+        }
+      }
+    }
+    (void)kd;
+  }
+}
+
+}  // namespace
+
+// ============================================================================================
+// workspace
+
+template <class T>
+static T *alloc_n(size_t n) { return (T *)dev_alloc(sizeof(T) * (n ? n : 1)); }
+
+static void check_operators(ufe_ctx *ctx) {
+  UFE_REQUIRE(ctx->has_mesh, UFE_ERR_INVALID, "no mesh uploaded");
+  for (int op = UFE_OP_MAP_A_B; op <= UFE_OP_DDY_B_A; ++op)
+    UFE_REQUIRE(ctx->op_set[op], UFE_ERR_INVALID, "a->b and b->a operators missing");
+  for (int op = UFE_OP_M2_DDX_B_B; op <= UFE_OP_M2_D2DY2_B_B; ++op)
+    UFE_REQUIRE(ctx->op_set[op], UFE_ERR_INVALID, "2nd-order b_b operators missing");
+  auto same = [&](int a, int b) { return ctx->ops[a].ptr == ctx->ops[b].ptr && ctx->ops[a].ind == ctx->ops[b].ind; };
+  UFE_REQUIRE(same(UFE_OP_MAP_A_B, UFE_OP_DDX_A_B) && same(UFE_OP_MAP_A_B, UFE_OP_DDY_A_B), UFE_ERR_INVALID,
+              "a->b operators must share one sparsity pattern");
+  UFE_REQUIRE(same(UFE_OP_MAP_B_A, UFE_OP_DDX_B_A) && same(UFE_OP_MAP_B_A, UFE_OP_DDY_B_A), UFE_ERR_INVALID,
+              "b->a operators must share one sparsity pattern");
+  for (int op = UFE_OP_M2_DDY_B_B; op <= UFE_OP_M2_D2DY2_B_B; ++op)
+    UFE_REQUIRE(same(UFE_OP_M2_DDX_B_B, op), UFE_ERR_INVALID, "2nd-order b_b operators must share one pattern");
+}
+
+Work *ensure_work(ufe_ctx *ctx) {
+  check_operators(ctx);
+  if (ctx->work) return ctx->work;
+  Work *w = new Work();
+  ctx->work = w;
+  const int nV = ctx->nV, nTri = ctx->nTri, nz = ctx->nz;
+  w->nV = nV; w->nTri = nTri; w->nz = nz;
+  w->nnzb = ctx->ops[UFE_OP_M2_DDX_B_B].nnz;
+  w->blk = alloc_n<double4>(w->nnzb);
+  w->blk32 = alloc_n<float4>(w->nnzb);
+  KrylovVecs &k = w->kv;
+  double2 **d2[] = {&k.X, &k.R, &k.RP, &k.S, &k.T, &k.dinv, &k.B, &k.P[0], &k.P[1], &k.V[0], &k.V[1]};
+  for (auto p : d2) *p = alloc_n<double2>(nTri);
+  float2 **f2[] = {&k.x32, &k.R32, &k.RP32, &k.S32, &k.T32, &k.dinv32, &k.P32[0], &k.P32[1], &k.V32[0], &k.V32[1]};
+  for (auto p : f2) *p = alloc_n<float2>(nTri);
+  w->uv = alloc_n<double2>(nTri);
+  w->tau_d = alloc_n<double2>(nTri);
+  w->fgr_b = alloc_n<double>(nTri);
+  w->bc_mask = alloc_n<int32_t>(nTri);
+  w->bc_uv = alloc_n<double2>(nTri);
+  w->uv_base = alloc_n<double2>(nTri);
+  w->tau_b = alloc_n<double2>(nTri);
+  w->eta_3D_b = alloc_n<double>((size_t)nTri * nz);
+  w->bfc_b = alloc_n<double>(nTri);
+  w->F2b1 = alloc_n<double>(nTri);
+  w->beta_b = alloc_n<double>(nTri);
+  w->Hi = alloc_n<double>(nV);
+  w->Hs = alloc_n<double>(nV);
+  w->Avav = alloc_n<double>(nV);
+  w->A_flow = alloc_n<double>((size_t)nV * nz);
+  w->beta_sq = alloc_n<double>(nV);
+  w->alpha_sq = alloc_n<double>(nV);
+  w->effp = alloc_n<double>(nV);
+  w->tys = alloc_n<double>(nV);
+  w->mask_gr = alloc_n<int32_t>(nV);
+  w->N_a = alloc_n<double>(nV);
+  w->beta_a = alloc_n<double>(nV);
+  w->beta_eff_a = alloc_n<double>(nV);
+  w->F2a1 = alloc_n<double>(nV);
+  w->eta_3D_a = alloc_n<double>((size_t)nV * nz);
+  w->F1_3D_a = alloc_n<double>((size_t)nV * nz);
+  w->N_b_in = alloc_n<double>(nTri);
+  w->dNx_b_in = alloc_n<double>(nTri);
+  w->dNy_b_in = alloc_n<double>(nTri);
+  w->beta_b_in = alloc_n<double>(nTri);
+  w->ks = alloc_n<KrylovScalars>(2);   // [0] outer/FP64, [1] FP32 inner
+  w->ps = alloc_n<PicardScalars>(1);
+  w->err = alloc_n<int>(1);
+  UFE_CUDA(cudaMallocHost(&w->ks_host, sizeof(KrylovScalars) * 2));
+  UFE_CUDA(cudaMallocHost(&w->ps_host, sizeof(PicardScalars)));
+  cudaStream_t s = ctx->stream;
+  UFE_CUDA(cudaMemsetAsync(w->uv, 0, sizeof(double2) * nTri, s));
+  UFE_CUDA(cudaMemsetAsync(w->uv_base, 0, sizeof(double2) * nTri, s));
+  UFE_CUDA(cudaMemsetAsync(w->tau_b, 0, sizeof(double2) * nTri, s));
+  UFE_CUDA(cudaMemsetAsync(w->eta_3D_b, 0, sizeof(double) * (size_t)nTri * nz, s));
+  UFE_CUDA(cudaMemsetAsync(w->ks, 0, sizeof(KrylovScalars) * 2, s));
+  UFE_CUDA(cudaMemsetAsync(w->err, 0, sizeof(int), s));
+  UFE_CUDA(cudaStreamSynchronize(s));
+  return w;
+}
+
+void free_work(ufe_ctx *ctx) {
+  Work *w = ctx->work;
+  if (!w) return;
+  if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  if (w->graph_ssa) cudaGraphExecDestroy(w->graph_ssa);
+  if (w->graph_diva) cudaGraphExecDestroy(w->graph_diva);
+  void *ptrs[] = {w->blk, w->blk32, w->kv.X, w->kv.R, w->kv.RP, w->kv.S, w->kv.T, w->kv.dinv, w->kv.B,
+                  w->kv.P[0], w->kv.P[1], w->kv.V[0], w->kv.V[1], w->kv.x32, w->kv.R32, w->kv.RP32,
+                  w->kv.S32, w->kv.T32, w->kv.dinv32, w->kv.P32[0], w->kv.P32[1], w->kv.V32[0],
+                  w->kv.V32[1], w->uv, w->tau_d, w->fgr_b, w->bc_mask, w->bc_uv, w->uv_base, w->tau_b,
+                  w->eta_3D_b, w->bfc_b, w->F2b1, w->beta_b, w->Hi, w->Hs, w->Avav, w->A_flow, w->beta_sq,
+                  w->alpha_sq, w->effp, w->tys, w->mask_gr, w->N_a, w->beta_a, w->beta_eff_a, w->F2a1,
+                  w->eta_3D_a, w->F1_3D_a, w->N_b_in, w->dNx_b_in, w->dNy_b_in, w->beta_b_in, w->ks,
+                  w->ps, w->err};
+  for (void *p : ptrs) dev_free(p);
+  if (w->ks_host) cudaFreeHost(w->ks_host);
+  if (w->ps_host) cudaFreeHost(w->ps_host);
+  delete w;
+  ctx->work = nullptr;
+}
+
+int32_t bsr_lanes(ufe_ctx *ctx) {
+  static int lanes = -1;
+  if (lanes < 0) {
+    const char *e = getenv("UFE_BSR_LANES");
+    int v = e ? atoi(e) : 4;
+    lanes = (v == 1 || v == 2 || v == 4 || v == 8) ? v : 4;
+  }
+  (void)ctx;
+  return lanes;
+}
+
+// ============================================================================================
+// enqueue helpers
+
+namespace {
+
+struct Solver {
+  ufe_ctx *ctx;
+  Work *w;
+  ufe_solver_params p;
+  PhysParams q;
+  int grid, lanes;
+  OpRow ab, ba;
+  cudaStream_t s;
+
+  Solver(ufe_ctx *c, const ufe_solver_params &pp) : ctx(c), p(pp) {
+    w = ensure_work(ctx);
+    q = make_phys(p, w->has_bc);
+    grid = max_grid(ctx);
+    lanes = bsr_lanes(ctx);
+    s = ctx->stream;
+    const DevCSR &mab = ctx->ops[UFE_OP_MAP_A_B];
+    ab = OpRow{mab.ptr, mab.ind, mab.val, ctx->ops[UFE_OP_DDX_A_B].val, ctx->ops[UFE_OP_DDY_A_B].val};
+    const DevCSR &mba = ctx->ops[UFE_OP_MAP_B_A];
+    ba = OpRow{mba.ptr, mba.ind, mba.val, ctx->ops[UFE_OP_DDX_B_A].val, ctx->ops[UFE_OP_DDY_B_A].val};
+  }
+
+  int eblocks(int64_t n) const { return pick_blocks(n, kThreads, grid); }
+
+  SlidingIn sliding() const { return SlidingIn{w->beta_sq, w->alpha_sq, w->effp, w->tys}; }
+
+  AssembleArgs assemble_args(const double2 *x0) const {
+    AssembleArgs a;
+    memset(&a, 0, sizeof(a));
+    a.nV = w->nV; a.nTri = w->nTri; a.nz = w->nz;
+    a.ab = ab;
+    const DevCSR &m2 = ctx->ops[UFE_OP_M2_DDX_B_B];
+    a.m2_ptr = m2.ptr; a.m2_ind = m2.ind;
+    a.m2_x = m2.val; a.m2_y = ctx->ops[UFE_OP_M2_DDY_B_B].val;
+    a.m2_xx = ctx->ops[UFE_OP_M2_D2DX2_B_B].val; a.m2_xy = ctx->ops[UFE_OP_M2_D2DXDY_B_B].val;
+    a.m2_yy = ctx->ops[UFE_OP_M2_D2DY2_B_B].val;
+    a.TriBI = ctx->TriBI; a.TriC = ctx->TriC;
+    a.N_b = w->N_b_in; a.dNx_b = w->dNx_b_in; a.dNy_b = w->dNy_b_in; a.beta_b_in = w->beta_b_in;
+    a.N_a = w->N_a; a.beta_a = w->beta_a; a.beta_eff_a = w->beta_eff_a; a.F2a1 = w->F2a1; a.eta_3D_a = w->eta_3D_a;
+    a.fgr_b = w->fgr_b; a.tau_d = w->tau_d; a.bc_mask = w->bc_mask; a.bc_uv = w->bc_uv;
+    a.x0 = x0;
+    a.blk = w->blk;
+    a.blk32 = (p.precision == UFE_PREC_FP32_REFINE) ? w->blk32 : nullptr;
+    a.rhs = w->kv.B; a.dinv = w->kv.dinv; a.X = w->kv.X; a.R = w->kv.R; a.RP = w->kv.RP;
+    a.P0 = w->kv.P[0]; a.V0 = w->kv.V[0]; a.dinv32 = w->kv.dinv32;
+    a.beta_b_out = w->beta_b; a.bfc_b = w->bfc_b; a.F2b1 = w->F2b1; a.eta_3D_b = w->eta_3D_b;
+    a.err = w->err;
+    a.ks = w->ks;
+    a.rtol = p.stress_balance_PETSc_rtol;
+    a.abstol = p.stress_balance_PETSc_abstol;
+    a.max_it = p.krylov_max_it;
+    a.partials = ctx->red.partials;
+    a.tickets = ctx->red.tickets;
+    return a;
+  }
+
+  void enqueue_assemble(int mode, bool x0_current, CondArg c) {
+    AssembleArgs a = assemble_args(x0_current ? w->uv : nullptr);
+    int g = eblocks(w->nTri);
+    if (mode == kFromTriangles) k_assemble<kFromTriangles><<<g, kThreads, 0, s>>>(a, q, c);
+    else if (mode == kFromSSA) k_assemble<kFromSSA><<<g, kThreads, 0, s>>>(a, q, c);
+    else k_assemble<kFromDIVA><<<g, kThreads, 0, s>>>(a, q, c);
+    UFE_CUDA(cudaGetLastError());
+  }
+
+  template <class M>
+  void enqueue_krylov_iter(const M &mat, KV<typename M::Vec> v, KrylovScalars *ks, CondArg c) {
+    unsigned g = krylov_grid(mat, kThreads, grid);
+    k_p_spmv<M><<<g, kThreads, 0, s>>>(mat, v, ks, ctx->red.partials, ctx->red.tickets);
+    k_s_spmv<M><<<g, kThreads, 0, s>>>(mat, v, ks, ctx->red.partials, ctx->red.tickets);
+    unsigned g2 = pick_blocks(mat.items, kThreads, grid);
+    k_xr<M><<<g2, kThreads, 0, s>>>(mat, v, ks, ctx->red.partials, ctx->red.tickets, c);
+    UFE_CUDA(cudaGetLastError());
+  }
+
+  template <int L>
+  BsrMat<double, L> mat64() const {
+    const DevCSR &m2 = ctx->ops[UFE_OP_M2_DDX_B_B];
+    return BsrMat<double, L>{w->nTri, m2.ptr, m2.ind, w->blk};
+  }
+  template <int L>
+  BsrMat<float, L> mat32() const {
+    const DevCSR &m2 = ctx->ops[UFE_OP_M2_DDX_B_B];
+    return BsrMat<float, L>{w->nTri, m2.ptr, m2.ind, w->blk32};
+  }
+  KV<double2> kv64() const {
+    KV<double2> v;
+    v.X = w->kv.X; v.R = w->kv.R; v.RP = w->kv.RP; v.S = w->kv.S; v.T = w->kv.T; v.B = w->kv.B;
+    v.dinv = w->kv.dinv;
+    v.P[0] = w->kv.P[0]; v.P[1] = w->kv.P[1]; v.V[0] = w->kv.V[0]; v.V[1] = w->kv.V[1];
+    return v;
+  }
+  KV<float2> kv32() const {
+    KV<float2> v;
+    v.X = w->kv.x32; v.R = w->kv.R32; v.RP = w->kv.RP32; v.S = w->kv.S32; v.T = w->kv.T32; v.B = nullptr;
+    v.dinv = w->kv.dinv32;
+    v.P[0] = w->kv.P32[0]; v.P[1] = w->kv.P32[1]; v.V[0] = w->kv.V32[0]; v.V[1] = w->kv.V32[1];
+    return v;
+  }
+
+  void krylov_iter64(CondArg c) {
+    switch (lanes) {
+      case 1: enqueue_krylov_iter(mat64<1>(), kv64(), w->ks, c); break;
+      case 2: enqueue_krylov_iter(mat64<2>(), kv64(), w->ks, c); break;
+      case 8: enqueue_krylov_iter(mat64<8>(), kv64(), w->ks, c); break;
+      default: enqueue_krylov_iter(mat64<4>(), kv64(), w->ks, c); break;
+    }
+  }
+  void krylov_iter32(CondArg c) {
+    switch (lanes) {
+      case 1: enqueue_krylov_iter(mat32<1>(), kv32(), w->ks + 1, c); break;
+      case 2: enqueue_krylov_iter(mat32<2>(), kv32(), w->ks + 1, c); break;
+      case 8: enqueue_krylov_iter(mat32<8>(), kv32(), w->ks + 1, c); break;
+      default: enqueue_krylov_iter(mat32<4>(), kv32(), w->ks + 1, c); break;
+    }
+  }
+  void enqueue_inner_init(CondArg c) {
+    k_inner_init<<<eblocks(w->nTri), kThreads, 0, s>>>(
+        w->nTri, w->kv.R, w->kv.R32, w->kv.RP32, w->kv.x32, w->kv.P32[0], w->kv.V32[0], w->ks, w->ks + 1,
+        p.krylov_inner_rtol, p.krylov_max_it, ctx->red.partials, ctx->red.tickets, c);
+    UFE_CUDA(cudaGetLastError());
+  }
+  template <int L>
+  void residual64_l(CondArg c) {
+    BsrMat<double, L> m = mat64<L>();
+    k_residual64<L><<<krylov_grid(m, kThreads, grid), kThreads, 0, s>>>(
+        m, w->kv.X, w->kv.B, w->kv.dinv, w->kv.R, w->ks, w->ks + 1, ctx->red.partials, ctx->red.tickets, c);
+  }
+  void enqueue_refine_update(CondArg c) {
+    k_xadd<<<eblocks(w->nTri), kThreads, 0, s>>>(w->nTri, w->kv.X, w->kv.x32);
+    switch (lanes) {
+      case 1: residual64_l<1>(c); break;
+      case 2: residual64_l<2>(c); break;
+      case 8: residual64_l<8>(c); break;
+      default: residual64_l<4>(c); break;
+    }
+    UFE_CUDA(cudaGetLastError());
+  }
+
+  void enqueue_prologue(bool diva) {
+    k_prologue<<<eblocks(std::max(w->nV, w->nTri)), kThreads, 0, s>>>(
+        w->nV, w->nTri, w->nz, ab, w->Hi, w->Hs, w->A_flow, ctx->zeta, w->tau_d, diva ? nullptr : w->Avav,
+        w->ps, w->ks, p.visc_it_relax, p.Glens_flow_law_epsilon_sq_0, p.Glens_flow_law_exponent);
+    UFE_CUDA(cudaMemsetAsync(w->ks + 1, 0, sizeof(KrylovScalars), s));
+    UFE_CUDA(cudaGetLastError());
+  }
+
+  void enqueue_picard_pre(bool diva, CondArg inner) {
+    if (diva) {
+      k_vertex_diva<<<eblocks(w->nV), kThreads, 0, s>>>(
+          w->nV, w->nTri, w->nz, ba, w->uv, w->uv_base, w->tau_b, w->eta_3D_b, w->A_flow, w->Hi, ctx->zeta,
+          sliding(), q, w->ps, w->eta_3D_a, w->N_a, w->F2a1, w->beta_a, w->beta_eff_a);
+    } else {
+      k_vertex_ssa<<<eblocks(w->nV), kThreads, 0, s>>>(w->nV, ba, w->uv, w->Avav, w->Hi, sliding(), q, w->ps,
+                                                       w->N_a, w->beta_a);
+    }
+    UFE_CUDA(cudaGetLastError());
+    enqueue_assemble(diva ? kFromDIVA : kFromSSA, p.krylov_initial_guess == UFE_X0_CURRENT, inner);
+  }
+
+  void enqueue_picard_post(bool diva, CondArg outer) {
+    if (diva)
+      k_finalize<true><<<eblocks(w->nTri), kThreads, 0, s>>>(w->nTri, w->kv.X, w->uv, q, w->ps, w->ks, w->beta_b,
+                                                             w->bfc_b, w->F2b1, w->uv_base, w->tau_b,
+                                                             ctx->red.partials, ctx->red.tickets, outer);
+    else
+      k_finalize<false><<<eblocks(w->nTri), kThreads, 0, s>>>(w->nTri, w->kv.X, w->uv, q, w->ps, w->ks, nullptr,
+                                                              nullptr, nullptr, nullptr, nullptr,
+                                                              ctx->red.partials, ctx->red.tickets, outer);
+    UFE_CUDA(cudaGetLastError());
+  }
+};
+
+// ---- graph construction ----------------------------------------------------------------------
+// Capture `fn` into `g` after `deps`; returns the capture's sink nodes.
+template <class F>
+std::vector<cudaGraphNode_t> capture_into(cudaStream_t s, cudaGraph_t g, const std::vector<cudaGraphNode_t> &deps,
+                                          F &&fn) {
+  UFE_CUDA(cudaStreamBeginCaptureToGraph(s, g, deps.empty() ? nullptr : deps.data(), nullptr, deps.size(),
+                                         cudaStreamCaptureModeThreadLocal));
+  try {
+    fn();
+  } catch (...) {
+    cudaGraph_t dummy;
+    cudaStreamEndCapture(s, &dummy);
+    throw;
+  }
+  cudaStreamCaptureStatus st;
+  const cudaGraphNode_t *sinks = nullptr;
+  size_t nsinks = 0;
+  UFE_CUDA(cudaStreamGetCaptureInfo(s, &st, nullptr, nullptr, &sinks, nullptr, &nsinks));
+  std::vector<cudaGraphNode_t> out(sinks, sinks + nsinks);
+  cudaGraph_t g2;
+  UFE_CUDA(cudaStreamEndCapture(s, &g2));
+  return out;
+}
+
+// Add a while-node after `deps`; returns (node, body graph).
+cudaGraphNode_t add_while(cudaGraph_t g, const std::vector<cudaGraphNode_t> &deps, cudaGraphConditionalHandle h,
+                          cudaGraph_t *body) {
+  cudaGraphNodeParams np = {cudaGraphNodeTypeConditional};
+  np.conditional.handle = h;
+  np.conditional.type = cudaGraphCondTypeWhile;
+  np.conditional.size = 1;
+  cudaGraphNode_t node;
+  UFE_CUDA(cudaGraphAddNode(&node, g, deps.empty() ? nullptr : deps.data(), nullptr, deps.size(), &np));
+  *body = np.conditional.phGraph_out[0];
+  return node;
+}
+
+uint64_t params_key(const ufe_solver_params &p, int lanes, int has_bc) {
+  const unsigned char *b = reinterpret_cast<const unsigned char *>(&p);
+  uint64_t h = 1469598103934665603ull;
+  for (size_t i = 0; i < sizeof(p); ++i) { h ^= b[i]; h *= 1099511628211ull; }
+  h ^= (uint64_t)lanes * 0x9E3779B97F4A7C15ull;
+  h ^= (uint64_t)(has_bc + 7) * 0xC2B2AE3D27D4EB4Full;
+  return h;
+}
+
+// The whole Picard solve as one graph: prologue -> while(picard){ pre -> while(krylov){...} -> post }
+cudaGraphExec_t build_picard_graph(Solver &S, bool diva) {
+  cudaGraph_t g;
+  UFE_CUDA(cudaGraphCreate(&g, 0));
+  try {
+    cudaGraphConditionalHandle h_outer;
+    UFE_CUDA(cudaGraphConditionalHandleCreate(&h_outer, g, 1, cudaGraphCondAssignDefault));
+    auto sinks = capture_into(S.s, g, {}, [&] { S.enqueue_prologue(diva); });
+    cudaGraph_t body;
+    add_while(g, sinks, h_outer, &body);
+    CondArg outer{h_outer, 1};
+    cudaGraphConditionalHandle h_inner;
+    UFE_CUDA(cudaGraphConditionalHandleCreate(&h_inner, body, 0, 0));
+    CondArg inner{h_inner, 1};
+    auto pre = capture_into(S.s, body, {}, [&] { S.enqueue_picard_pre(diva, inner); });
+    cudaGraph_t kbody;
+    cudaGraphNode_t wk = add_while(body, pre, h_inner, &kbody);
+    if (S.p.precision == UFE_PREC_FP32_REFINE) {
+      // refinement loop: inner FP32 BiCGStab, then x += d and the FP64 residual test
+      cudaGraphConditionalHandle h_in32;
+      UFE_CUDA(cudaGraphConditionalHandleCreate(&h_in32, kbody, 0, 0));
+      CondArg in32{h_in32, 1};
+      auto ii = capture_into(S.s, kbody, {}, [&] { S.enqueue_inner_init(in32); });
+      cudaGraph_t ibody;
+      cudaGraphNode_t wi = add_while(kbody, ii, h_in32, &ibody);
+      capture_into(S.s, ibody, {}, [&] { S.krylov_iter32(in32); });
+      capture_into(S.s, kbody, {wi}, [&] { S.enqueue_refine_update(inner); });
+    } else {
+      capture_into(S.s, kbody, {}, [&] { S.krylov_iter64(inner); });
+    }
+    capture_into(S.s, body, {wk}, [&] { S.enqueue_picard_post(diva, outer); });
+    cudaGraphExec_t exec;
+    UFE_CUDA(cudaGraphInstantiate(&exec, g, 0));
+    cudaGraphDestroy(g);
+    return exec;
+  } catch (...) {
+    cudaGraphDestroy(g);
+    throw;
+  }
+}
+
+// Host-driven loop over the same kernels (UFE_NO_GRAPH=1): for debugging and comparison.
+void run_picard_host(Solver &S, bool diva) {
+  CondArg none{0, 0};
+  Work *w = S.w;
+  S.enqueue_prologue(diva);
+  for (int it = 0; it < S.p.visc_it_nit + 2; ++it) {
+    S.enqueue_picard_pre(diva, none);
+    for (;;) {
+      if (S.p.precision == UFE_PREC_FP32_REFINE) {
+        UFE_CUDA(cudaMemcpyAsync(w->ks_host, w->ks, sizeof(KrylovScalars), cudaMemcpyDeviceToHost, S.s));
+        UFE_CUDA(cudaStreamSynchronize(S.s));
+        if (!w->ks_host[0].active) break;
+        S.enqueue_inner_init(none);
+        for (;;) {
+          for (int c = 0; c < 8; ++c) S.krylov_iter32(none);
+          UFE_CUDA(cudaMemcpyAsync(w->ks_host + 1, w->ks + 1, sizeof(KrylovScalars), cudaMemcpyDeviceToHost, S.s));
+          UFE_CUDA(cudaStreamSynchronize(S.s));
+          if (!w->ks_host[1].active) break;
+        }
+        S.enqueue_refine_update(none);
+      } else {
+        for (int c = 0; c < 8; ++c) S.krylov_iter64(none);
+        UFE_CUDA(cudaMemcpyAsync(w->ks_host, w->ks, sizeof(KrylovScalars), cudaMemcpyDeviceToHost, S.s));
+        UFE_CUDA(cudaStreamSynchronize(S.s));
+        if (!w->ks_host[0].active) break;
+      }
+    }
+    S.enqueue_picard_post(diva, none);
+    UFE_CUDA(cudaMemcpyAsync(w->ps_host, w->ps, sizeof(PicardScalars), cudaMemcpyDeviceToHost, S.s));
+    UFE_CUDA(cudaStreamSynchronize(S.s));
+    if (!w->ps_host->active) break;
+  }
+}
+
+bool use_graphs() {
+  static int v = -1;
+  if (v < 0) {
+    const char *e = getenv("UFE_NO_GRAPH");
+    v = (e && *e && *e != '0') ? 0 : 1;
+  }
+  return v == 1;
+}
+
+void validate_params(const ufe_solver_params *p) {
+  UFE_REQUIRE(p, UFE_ERR_INVALID, "null params");
+  UFE_REQUIRE(p->choice_sliding_law >= 0 && p->choice_sliding_law <= UFE_SLIDING_SCHOOF2005, UFE_ERR_INVALID,
+              "unknown sliding law");
+  UFE_REQUIRE(p->visc_it_nit >= 0 && p->krylov_max_it >= 1, UFE_ERR_INVALID, "iteration limits out of range");
+  UFE_REQUIRE(p->precision == UFE_PREC_FP64 || p->precision == UFE_PREC_FP32_REFINE, UFE_ERR_INVALID,
+              "unknown precision mode");
+  UFE_REQUIRE(p->krylov_initial_guess == UFE_X0_ZERO || p->krylov_initial_guess == UFE_X0_CURRENT, UFE_ERR_INVALID,
+              "unknown initial guess mode");
+  const int32_t bcs[8] = {p->BC_u_west, p->BC_u_east, p->BC_u_south, p->BC_u_north,
+                          p->BC_v_west, p->BC_v_east, p->BC_v_south, p->BC_v_north};
+  for (int i = 0; i < 8; ++i)
+    UFE_REQUIRE(bcs[i] == UFE_BC_INFINITE || bcs[i] == UFE_BC_ZERO, UFE_ERR_INVALID, "unsupported boundary condition");
+  UFE_REQUIRE(p->Glens_flow_law_exponent > 0 && p->visc_it_relax > 0 && p->visc_it_relax <= 1, UFE_ERR_INVALID,
+              "flow law exponent or relaxation out of range");
+  UFE_REQUIRE(p->krylov_inner_rtol > 0 && p->krylov_inner_rtol < 1, UFE_ERR_INVALID, "krylov_inner_rtol out of range");
+}
+
+int32_t check_err_flag(Solver &S) {
+  int err = 0;
+  UFE_CUDA(cudaMemcpyAsync(&err, S.w->err, sizeof(int), cudaMemcpyDeviceToHost, S.s));
+  UFE_CUDA(cudaStreamSynchronize(S.s));
+  if (err) {
+    UFE_CUDA(cudaMemsetAsync(S.w->err, 0, sizeof(int), S.s));
+    UFE_REQUIRE(!(err & kErrNoDiag), UFE_ERR_INVALID, "a 2nd-order b_b operator row has no diagonal entry");
+    UFE_REQUIRE(!(err & kErrBcNeighbour), UFE_ERR_INVALID,
+                "a border triangle's neighbour is missing from its b_b operator row");
+    UFE_REQUIRE(false, UFE_ERR_INVALID, "a border triangle has no neighbours");
+  }
+  return UFE_OK;
+}
+
+// Run a resident Picard solve; fills stats; returns the status.
+int32_t run_picard(ufe_ctx *ctx, const ufe_solver_params &p, bool diva, ufe_solve_stats *stats) {
+  Solver S(ctx, p);
+  Work *w = S.w;
+  UFE_REQUIRE(ctx->nz <= kMaxNz, UFE_ERR_CAPACITY, "nz exceeds 64 layers");
+  const int law = p.choice_sliding_law;
+  cudaEventRecord(ctx->ev0, S.s);
+  if (use_graphs()) {
+    cudaGraphExec_t *gx = diva ? &w->graph_diva : &w->graph_ssa;
+    uint64_t *key = diva ? &w->graph_diva_key : &w->graph_ssa_key;
+    uint64_t k = params_key(p, S.lanes, w->has_bc);
+    if (!*gx || *key != k) {
+      if (*gx) cudaGraphExecDestroy(*gx);
+      *gx = nullptr;
+      *gx = build_picard_graph(S, diva);
+      *key = k;
+    }
+    UFE_CUDA(cudaGraphLaunch(*gx, S.s));
+  } else {
+    run_picard_host(S, diva);
+  }
+  cudaEventRecord(ctx->ev1, S.s);
+  UFE_CUDA(cudaMemcpyAsync(w->ps_host, w->ps, sizeof(PicardScalars), cudaMemcpyDeviceToHost, S.s));
+  UFE_CUDA(cudaMemcpyAsync(w->ks_host, w->ks, sizeof(KrylovScalars) * 2, cudaMemcpyDeviceToHost, S.s));
+  UFE_CUDA(cudaStreamSynchronize(S.s));
+  check_err_flag(S);
+  const PicardScalars ps = *w->ps_host;
+  const KrylovScalars ks = w->ks_host[0];
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+  (void)law;
+  int32_t total_its = (p.precision == UFE_PREC_FP32_REFINE) ? w->ks_host[1].total_its : ks.total_its;
+  if (stats) {
+    memset(stats, 0, sizeof(*stats));
+    stats->n_visc_its = ps.it;
+    stats->n_Axb_its = total_its;
+    stats->n_refinements = ps.n_refine;
+    stats->status = ps.status;
+    stats->L2_uv = ps.L2;
+    stats->visc_it_relax_applied = ps.relax;
+    stats->device_ms = ms;
+  }
+  return ps.status;
+}
+
+}  // namespace
+
+// ============================================================================================
+// entry points
+
+static void upload_opt(double *dst, const double *src, size_t n, cudaStream_t s) {
+  if (src) UFE_CUDA(cudaMemcpyAsync(dst, src, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+  else UFE_CUDA(cudaMemsetAsync(dst, 0, sizeof(double) * n, s));
+}
+
+static void upload_bc(ufe_ctx *ctx, Work *w, const ufe_bc_prescribed *bc) {
+  cudaStream_t s = ctx->stream;
+  const int nTri = ctx->nTri;
+  w->has_bc = 0;
+  if (bc && (bc->mask_b || bc->u_b || bc->v_b)) {
+    UFE_REQUIRE(bc->mask_b && bc->u_b && bc->v_b, UFE_ERR_INVALID,
+                "need to provide prescribed u,v fields and mask");  // SSA_main.f90:147-150
+    UFE_CUDA(cudaMemcpyAsync(w->bc_mask, bc->mask_b, sizeof(int32_t) * nTri, cudaMemcpyHostToDevice, s));
+    double *tmp_u = (double *)dev_alloc(sizeof(double) * nTri), *tmp_v = (double *)dev_alloc(sizeof(double) * nTri);
+    UFE_CUDA(cudaMemcpyAsync(tmp_u, bc->u_b, sizeof(double) * nTri, cudaMemcpyHostToDevice, s));
+    UFE_CUDA(cudaMemcpyAsync(tmp_v, bc->v_b, sizeof(double) * nTri, cudaMemcpyHostToDevice, s));
+    k_interleave<<<pick_blocks(nTri, kThreads, 1024), kThreads, 0, s>>>(nTri, tmp_u, tmp_v, w->bc_uv);
+    UFE_CUDA(cudaGetLastError());
+    UFE_CUDA(cudaStreamSynchronize(s));
+    dev_free(tmp_u);
+    dev_free(tmp_v);
+    w->has_bc = 1;
+  }
+}
+
+extern "C" int32_t ufe_ice_upload(ufe_ctx *ctx, const ufe_ice_state *ice, const ufe_bc_prescribed *bc) {
+  return guarded(ctx, [&]() -> int32_t {
+    UFE_REQUIRE(ice && ice->Hi && ice->Hs && ice->A_flow && ice->fraction_gr_b && ice->mask_grounded_ice,
+                UFE_ERR_INVALID, "ice state arrays missing");
+    UFE_CUDA(cudaSetDevice(ctx->device));
+    Work *w = ensure_work(ctx);
+    cudaStream_t s = ctx->stream;
+    const size_t nV = ctx->nV, nTri = ctx->nTri, nz = ctx->nz;
+    UFE_CUDA(cudaMemcpyAsync(w->Hi, ice->Hi, sizeof(double) * nV, cudaMemcpyHostToDevice, s));
+    UFE_CUDA(cudaMemcpyAsync(w->Hs, ice->Hs, sizeof(double) * nV, cudaMemcpyHostToDevice, s));
+    UFE_CUDA(cudaMemcpyAsync(w->A_flow, ice->A_flow, sizeof(double) * nV * nz, cudaMemcpyHostToDevice, s));
+    UFE_CUDA(cudaMemcpyAsync(w->fgr_b, ice->fraction_gr_b, sizeof(double) * nTri, cudaMemcpyHostToDevice, s));
+    UFE_CUDA(cudaMemcpyAsync(w->mask_gr, ice->mask_grounded_ice, sizeof(int32_t) * nV, cudaMemcpyHostToDevice, s));
+    upload_opt(w->beta_sq, ice->beta_sq, nV, s);
+    upload_opt(w->alpha_sq, ice->alpha_sq, nV, s);
+    upload_opt(w->effp, ice->effective_pressure, nV, s);
+    upload_opt(w->tys, ice->till_yield_stress, nV, s);
+    int any = 0;
+    for (size_t v = 0; v < nV && !any; ++v) any = ice->mask_grounded_ice[v] != 0;
+    w->any_grounded = any;
+    upload_bc(ctx, w, bc);
+    UFE_CUDA(cudaStreamSynchronize(s));
+    return UFE_OK;
+  });
+}
+
+static void check_sliding_inputs(const ufe_solver_params *p, const ufe_ice_state *ice) {
+  if (!ice) return;
+  switch (p->choice_sliding_law) {
+    case UFE_SLIDING_WEERTMAN:
+      UFE_REQUIRE(ice->beta_sq, UFE_ERR_INVALID, "Weertman sliding needs beta_sq"); break;
+    case UFE_SLIDING_COULOMB: case UFE_SLIDING_BUDD:
+      UFE_REQUIRE(ice->till_yield_stress, UFE_ERR_INVALID, "Coulomb/Budd sliding needs till_yield_stress"); break;
+    case UFE_SLIDING_TSAI2015: case UFE_SLIDING_SCHOOF2005:
+      UFE_REQUIRE(ice->beta_sq && ice->alpha_sq && ice->effective_pressure, UFE_ERR_INVALID,
+                  "Tsai2015/Schoof2005 sliding needs beta_sq, alpha_sq and effective_pressure");
+      break;
+    default: break;
+  }
+}
+
+static int32_t resident_solve(ufe_ctx *ctx, const ufe_solver_params *p, int32_t cold_start, bool diva,
+                              ufe_solve_stats *stats) {
+  validate_params(p);
+  UFE_CUDA(cudaSetDevice(ctx->device));
+  Work *w = ensure_work(ctx);
+  cudaStream_t s = ctx->stream;
+  const int nTri = ctx->nTri;
+  if (cold_start) {
+    UFE_CUDA(cudaMemsetAsync(w->uv, 0, sizeof(double2) * nTri, s));
+    if (diva) {
+      UFE_CUDA(cudaMemsetAsync(w->uv_base, 0, sizeof(double2) * nTri, s));
+      UFE_CUDA(cudaMemsetAsync(w->tau_b, 0, sizeof(double2) * nTri, s));
+      UFE_CUDA(cudaMemsetAsync(w->eta_3D_b, 0, sizeof(double) * (size_t)nTri * ctx->nz, s));
+    }
+  }
+  bool skip = !w->any_grounded || (!diva && p->choice_sliding_law == UFE_SLIDING_NO_SLIDING);
+  if (skip) {
+    // solve_SSA/solve_DIVA return zero velocities without grounded ice (SSA_main.f90:121-129)
+    UFE_CUDA(cudaMemsetAsync(w->uv, 0, sizeof(double2) * nTri, s));
+    if (diva) UFE_CUDA(cudaMemsetAsync(w->uv_base, 0, sizeof(double2) * nTri, s));
+    UFE_CUDA(cudaStreamSynchronize(s));
+    if (stats) memset(stats, 0, sizeof(*stats));
+    return UFE_OK;
+  }
+  return run_picard(ctx, *p, diva, stats);
+}
+
+extern "C" int32_t ufe_solve_ssa_resident(ufe_ctx *ctx, const ufe_solver_params *p, int32_t cold_start,
+                                          ufe_solve_stats *stats) {
+  return guarded(ctx, [&]() -> int32_t { return resident_solve(ctx, p, cold_start, false, stats); });
+}
+
+extern "C" int32_t ufe_solve_diva_resident(ufe_ctx *ctx, const ufe_solver_params *p, int32_t cold_start,
+                                           ufe_solve_stats *stats) {
+  return guarded(ctx, [&]() -> int32_t { return resident_solve(ctx, p, cold_start, true, stats); });
+}
+
+static void download_pair(ufe_ctx *ctx, const double2 *src, double *a, double *b) {
+  cudaStream_t s = ctx->stream;
+  const int n = ctx->nTri;
+  double *ta = (double *)dev_alloc(sizeof(double) * n), *tb = (double *)dev_alloc(sizeof(double) * n);
+  k_deinterleave<<<pick_blocks(n, kThreads, 1024), kThreads, 0, s>>>(n, src, ta, tb);
+  UFE_CUDA(cudaGetLastError());
+  if (a) UFE_CUDA(cudaMemcpyAsync(a, ta, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+  if (b) UFE_CUDA(cudaMemcpyAsync(b, tb, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+  UFE_CUDA(cudaStreamSynchronize(s));
+  dev_free(ta);
+  dev_free(tb);
+}
+
+static void upload_pair(ufe_ctx *ctx, double2 *dst, const double *a, const double *b) {
+  cudaStream_t s = ctx->stream;
+  const int n = ctx->nTri;
+  double *ta = (double *)dev_alloc(sizeof(double) * n), *tb = (double *)dev_alloc(sizeof(double) * n);
+  upload_opt(ta, a, n, s);
+  upload_opt(tb, b, n, s);
+  k_interleave<<<pick_blocks(n, kThreads, 1024), kThreads, 0, s>>>(n, ta, tb, dst);
+  UFE_CUDA(cudaGetLastError());
+  UFE_CUDA(cudaStreamSynchronize(s));
+  dev_free(ta);
+  dev_free(tb);
+}
+
+extern "C" int32_t ufe_velocity_download(ufe_ctx *ctx, double *u_b, double *v_b) {
+  return guarded(ctx, [&]() -> int32_t {
+    UFE_CUDA(cudaSetDevice(ctx->device));
+    Work *w = ensure_work(ctx);
+    download_pair(ctx, w->uv, u_b, v_b);
+    return UFE_OK;
+  });
+}
+
+extern "C" int32_t ufe_solve_ssa(ufe_ctx *ctx, const ufe_solver_params *p, const ufe_ice_state *ice,
+                                 const ufe_bc_prescribed *bc, double *u_b, double *v_b, int32_t *n_visc_its,
+                                 int32_t *n_Axb_its, ufe_solve_stats *stats) {
+  int32_t rc = ufe_ice_upload(ctx, ice, bc);
+  if (rc != UFE_OK) return rc;
+  return guarded(ctx, [&]() -> int32_t {
+    UFE_REQUIRE(u_b && v_b, UFE_ERR_INVALID, "null velocity arrays");
+    validate_params(p);
+    check_sliding_inputs(p, ice);
+    Work *w = ensure_work(ctx);
+    upload_pair(ctx, w->uv, u_b, v_b);
+    ufe_solve_stats st;
+    int32_t r = resident_solve(ctx, p, 0, false, &st);
+    download_pair(ctx, w->uv, u_b, v_b);
+    if (n_visc_its) *n_visc_its = st.n_visc_its;
+    if (n_Axb_its) *n_Axb_its = st.n_Axb_its;
+    if (stats) *stats = st;
+    return r;
+  });
+}
+
+extern "C" int32_t ufe_solve_diva(ufe_ctx *ctx, const ufe_solver_params *p, const ufe_ice_state *ice,
+                                  const ufe_bc_prescribed *bc, ufe_diva_state *ds, int32_t *n_visc_its,
+                                  int32_t *n_Axb_its, ufe_solve_stats *stats) {
+  int32_t rc = ufe_ice_upload(ctx, ice, bc);
+  if (rc != UFE_OK) return rc;
+  return guarded(ctx, [&]() -> int32_t {
+    UFE_REQUIRE(ds && ds->u_vav_b && ds->v_vav_b && ds->u_base_b && ds->v_base_b && ds->tau_bx_b && ds->tau_by_b &&
+                    ds->eta_3D_b,
+                UFE_ERR_INVALID, "DIVA state arrays missing");
+    validate_params(p);
+    check_sliding_inputs(p, ice);
+    UFE_REQUIRE(ctx->nz <= kMaxNz, UFE_ERR_CAPACITY, "nz exceeds 64 layers");
+    Work *w = ensure_work(ctx);
+    cudaStream_t s = ctx->stream;
+    const size_t nTri = ctx->nTri, nz = ctx->nz;
+    upload_pair(ctx, w->uv, ds->u_vav_b, ds->v_vav_b);
+    upload_pair(ctx, w->uv_base, ds->u_base_b, ds->v_base_b);
+    upload_pair(ctx, w->tau_b, ds->tau_bx_b, ds->tau_by_b);
+    UFE_CUDA(cudaMemcpyAsync(w->eta_3D_b, ds->eta_3D_b, sizeof(double) * nTri * nz, cudaMemcpyHostToDevice, s));
+    ufe_solve_stats st;
+    int32_t r = resident_solve(ctx, p, 0, true, &st);
+    download_pair(ctx, w->uv, ds->u_vav_b, ds->v_vav_b);
+    download_pair(ctx, w->uv_base, ds->u_base_b, ds->v_base_b);
+    download_pair(ctx, w->tau_b, ds->tau_bx_b, ds->tau_by_b);
+    UFE_CUDA(cudaMemcpyAsync(ds->eta_3D_b, w->eta_3D_b, sizeof(double) * nTri * nz, cudaMemcpyDeviceToHost, s));
+    if (r >= 0 && ds->u_3D_b && ds->v_3D_b) {
+      if (!w->any_grounded) {
+        memset(ds->u_3D_b, 0, sizeof(double) * nTri * nz);
+        memset(ds->v_3D_b, 0, sizeof(double) * nTri * nz);
+      } else {
+        double *u3 = (double *)dev_alloc(sizeof(double) * nTri * nz), *v3 = (double *)dev_alloc(sizeof(double) * nTri * nz);
+        Solver S(ctx, *p);
+        k_diva_F1<<<S.eblocks(ctx->nV), kThreads, 0, s>>>(ctx->nV, ctx->nz, w->eta_3D_a, w->Hi, ctx->zeta, w->F1_3D_a);
+        k_diva_u3d<<<S.eblocks((int64_t)nTri * nz), kThreads, 0, s>>>(
+            ctx->nV, ctx->nTri, ctx->nz, S.ab, w->F1_3D_a, w->uv_base, w->tau_b, w->bfc_b,
+            p->choice_sliding_law == UFE_SLIDING_NO_SLIDING, u3, v3);
+        UFE_CUDA(cudaGetLastError());
+        UFE_CUDA(cudaMemcpyAsync(ds->u_3D_b, u3, sizeof(double) * nTri * nz, cudaMemcpyDeviceToHost, s));
+        UFE_CUDA(cudaMemcpyAsync(ds->v_3D_b, v3, sizeof(double) * nTri * nz, cudaMemcpyDeviceToHost, s));
+        UFE_CUDA(cudaStreamSynchronize(s));
+        dev_free(u3);
+        dev_free(v3);
+      }
+    }
+    UFE_CUDA(cudaStreamSynchronize(s));
+    if (n_visc_its) *n_visc_its = st.n_visc_its;
+    if (n_Axb_its) *n_Axb_its = st.n_Axb_its;
+    if (stats) *stats = st;
+    return r;
+  });
+}
+
+// Upload the per-triangle inputs of solve_SSA_DIVA_linearised.
+static void upload_linearised_inputs(ufe_ctx *ctx, Work *w, const double *N_b, const double *dN_dx_b,
+                                     const double *dN_dy_b, const double *beta_b, const double *tau_dx_b,
+                                     const double *tau_dy_b, const ufe_bc_prescribed *bc) {
+  UFE_REQUIRE(N_b && dN_dx_b && dN_dy_b && beta_b && tau_dx_b && tau_dy_b, UFE_ERR_INVALID,
+              "linearised-solve input missing");
+  cudaStream_t s = ctx->stream;
+  const size_t n = ctx->nTri;
+  UFE_CUDA(cudaMemcpyAsync(w->N_b_in, N_b, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+  UFE_CUDA(cudaMemcpyAsync(w->dNx_b_in, dN_dx_b, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+  UFE_CUDA(cudaMemcpyAsync(w->dNy_b_in, dN_dy_b, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+  UFE_CUDA(cudaMemcpyAsync(w->beta_b_in, beta_b, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+  upload_pair(ctx, w->tau_d, tau_dx_b, tau_dy_b);
+  upload_bc(ctx, w, bc);
+}
+
+extern "C" int32_t ufe_assemble_linearised(ufe_ctx *ctx, const ufe_solver_params *p, const double *N_b,
+                                           const double *dN_dx_b, const double *dN_dy_b,
+                                           const double *basal_friction_coefficient_b, const double *tau_dx_b,
+                                           const double *tau_dy_b, const double *u_b_prev, const double *v_b_prev,
+                                           const ufe_bc_prescribed *bc, int32_t *ptr, int32_t *ind, double *val,
+                                           double *bb, int64_t cap, int64_t *nnz_out) {
+  return guarded(ctx, [&]() -> int32_t {
+    (void)u_b_prev; (void)v_b_prev;
+    validate_params(p);
+    UFE_CUDA(cudaSetDevice(ctx->device));
+    Work *w = ensure_work(ctx);
+    upload_linearised_inputs(ctx, w, N_b, dN_dx_b, dN_dy_b, basal_friction_coefficient_b, tau_dx_b, tau_dy_b, bc);
+    Solver S(ctx, *p);
+    CondArg none{0, 0};
+    S.enqueue_assemble(kFromTriangles, false, none);
+    check_err_flag(S);
+    const int nTri = ctx->nTri, nrow = 2 * nTri;
+    cudaStream_t s = ctx->stream;
+    int32_t *rowlen = (int32_t *)dev_alloc(sizeof(int32_t) * (nrow + 1));
+    int32_t *dptr = (int32_t *)dev_alloc(sizeof(int32_t) * (nrow + 1));
+    UFE_CUDA(cudaMemsetAsync(rowlen, 0, sizeof(int32_t) * (nrow + 1), s));
+    const DevCSR &m2 = ctx->ops[UFE_OP_M2_DDX_B_B];
+    k_export_len<<<S.eblocks(nTri), kThreads, 0, s>>>(nTri, m2.ptr, ctx->TriBI, ctx->TriC, w->bc_mask, S.q, rowlen);
+    UFE_CUDA(cudaGetLastError());
+    std::vector<int32_t> hl(nrow + 1);
+    UFE_CUDA(cudaMemcpyAsync(hl.data(), rowlen, sizeof(int32_t) * (nrow + 1), cudaMemcpyDeviceToHost, s));
+    UFE_CUDA(cudaStreamSynchronize(s));
+    std::vector<int32_t> hp(nrow + 1, 0);
+    for (int i = 0; i < nrow; ++i) hp[i + 1] = hp[i] + hl[i];
+    const int64_t nnz = hp[nrow];
+    if (nnz_out) *nnz_out = nnz;
+    int32_t rc = UFE_OK;
+    if (nnz > cap || !ptr || !ind || !val || !bb) {
+      rc = UFE_ERR_CAPACITY;
+    } else {
+      UFE_CUDA(cudaMemcpyAsync(dptr, hp.data(), sizeof(int32_t) * (nrow + 1), cudaMemcpyHostToDevice, s));
+      int32_t *dind = (int32_t *)dev_alloc(sizeof(int32_t) * (nnz ? nnz : 1));
+      double *dval = (double *)dev_alloc(sizeof(double) * (nnz ? nnz : 1));
+      k_export_fill<<<S.eblocks(nTri), kThreads, 0, s>>>(nTri, m2.ptr, m2.ind, ctx->TriBI, ctx->TriC, w->bc_mask,
+                                                         S.q, w->blk, dptr, dind, dval);
+      UFE_CUDA(cudaGetLastError());
+      UFE_CUDA(cudaMemcpyAsync(ind, dind, sizeof(int32_t) * nnz, cudaMemcpyDeviceToHost, s));
+      UFE_CUDA(cudaMemcpyAsync(val, dval, sizeof(double) * nnz, cudaMemcpyDeviceToHost, s));
+      UFE_CUDA(cudaMemcpyAsync(bb, w->kv.B, sizeof(double) * nrow, cudaMemcpyDeviceToHost, s));
+      UFE_CUDA(cudaStreamSynchronize(s));
+      dev_free(dind);
+      dev_free(dval);
+      for (int i = 0; i <= nrow; ++i) ptr[i] = hp[i] + 1;
+      for (int64_t k = 0; k < nnz; ++k) ind[k] += 1;
+    }
+    dev_free(rowlen);
+    dev_free(dptr);
+    return rc;
+  });
+}
+
+extern "C" int32_t ufe_solve_linearised(ufe_ctx *ctx, const ufe_solver_params *p, double *u_b, double *v_b,
+                                        const double *N_b, const double *dN_dx_b, const double *dN_dy_b,
+                                        const double *basal_friction_coefficient_b, const double *tau_dx_b,
+                                        const double *tau_dy_b, double *u_b_prev, double *v_b_prev,
+                                        const ufe_bc_prescribed *bc, int32_t *n_Axb_its) {
+  return guarded(ctx, [&]() -> int32_t {
+    UFE_REQUIRE(u_b && v_b, UFE_ERR_INVALID, "null velocity arrays");
+    validate_params(p);
+    UFE_CUDA(cudaSetDevice(ctx->device));
+    Work *w = ensure_work(ctx);
+    const int nTri = ctx->nTri;
+    if (u_b_prev) memcpy(u_b_prev, u_b, sizeof(double) * nTri);
+    if (v_b_prev) memcpy(v_b_prev, v_b, sizeof(double) * nTri);
+    upload_linearised_inputs(ctx, w, N_b, dN_dx_b, dN_dy_b, basal_friction_coefficient_b, tau_dx_b, tau_dy_b, bc);
+    upload_pair(ctx, w->uv, u_b, v_b);
+    Solver S(ctx, *p);
+    CondArg none{0, 0};
+    UFE_CUDA(cudaMemsetAsync(w->ks, 0, sizeof(KrylovScalars) * 2, S.s));
+    S.enqueue_assemble(kFromTriangles, p->krylov_initial_guess == UFE_X0_CURRENT, none);
+    for (;;) {
+      if (p->precision == UFE_PREC_FP32_REFINE) {
+        UFE_CUDA(cudaMemcpyAsync(w->ks_host, w->ks, sizeof(KrylovScalars), cudaMemcpyDeviceToHost, S.s));
+        UFE_CUDA(cudaStreamSynchronize(S.s));
+        if (!w->ks_host[0].active) break;
+        S.enqueue_inner_init(none);
+        for (;;) {
+          for (int c = 0; c < 8; ++c) S.krylov_iter32(none);
+          UFE_CUDA(cudaMemcpyAsync(w->ks_host + 1, w->ks + 1, sizeof(KrylovScalars), cudaMemcpyDeviceToHost, S.s));
+          UFE_CUDA(cudaStreamSynchronize(S.s));
+          if (!w->ks_host[1].active) break;
+        }
+        S.enqueue_refine_update(none);
+      } else {
+        for (int c = 0; c < 8; ++c) S.krylov_iter64(none);
+        UFE_CUDA(cudaMemcpyAsync(w->ks_host, w->ks, sizeof(KrylovScalars), cudaMemcpyDeviceToHost, S.s));
+        UFE_CUDA(cudaStreamSynchronize(S.s));
+        if (!w->ks_host[0].active) break;
+      }
+    }
+    check_err_flag(S);
+    UFE_CUDA(cudaMemcpyAsync(w->ks_host, w->ks, sizeof(KrylovScalars) * 2, cudaMemcpyDeviceToHost, S.s));
+    UFE_CUDA(cudaStreamSynchronize(S.s));
+    download_pair(ctx, w->kv.X, u_b, v_b);
+    if (n_Axb_its)
+      *n_Axb_its = (p->precision == UFE_PREC_FP32_REFINE) ? w->ks_host[1].total_its : w->ks_host[0].it;
+    return w->ks_host[0].status;
+  });
+}
+
+// General CSR matrix-equation solve (solve_matrix_equation_CSR_PETSc): same BiCGStab kernels on
+// scalar rows, host-checked every few iterations.
+int32_t solve_csr_device(ufe_ctx *ctx, const DevCSR &A, const double *b, double *x, double rtol, double abstol,
+                         int32_t max_it, int32_t *its) {
+  cudaStream_t s = ctx->stream;
+  const int m = A.m;
+  double *vec = (double *)dev_alloc(sizeof(double) * (size_t)m * 10);
+  KrylovScalars *ks = (KrylovScalars *)dev_alloc(sizeof(KrylovScalars));
+  KrylovScalars *hks = nullptr;
+  UFE_CUDA(cudaMallocHost(&hks, sizeof(KrylovScalars)));
+  int32_t status = UFE_OK;
+  try {
+    double *dinv = vec, *R = vec + m, *RP = R + m, *S = RP + m, *T = S + m, *P0 = T + m, *P1 = P0 + m,
+           *V0 = P1 + m, *V1 = V0 + m;
+    // Jacobi diagonal
+    std::vector<int32_t> hp(m + 1), hi(A.nnz);
+    std::vector<double> hv(A.nnz), hd(m);
+    UFE_CUDA(cudaMemcpy(hp.data(), A.ptr, sizeof(int32_t) * (m + 1), cudaMemcpyDeviceToHost));
+    UFE_CUDA(cudaMemcpy(hi.data(), A.ind, sizeof(int32_t) * A.nnz, cudaMemcpyDeviceToHost));
+    UFE_CUDA(cudaMemcpy(hv.data(), A.val, sizeof(double) * A.nnz, cudaMemcpyDeviceToHost));
+    for (int i = 0; i < m; ++i) {
+      double d = 0.0;
+      for (int k = hp[i]; k < hp[i + 1]; ++k)
+        if (hi[k] == i) d += hv[k];
+      hd[i] = d != 0.0 ? 1.0 / d : 1.0;
+    }
+    UFE_CUDA(cudaMemcpyAsync(dinv, hd.data(), sizeof(double) * m, cudaMemcpyHostToDevice, s));
+    UFE_CUDA(cudaMemsetAsync(ks, 0, sizeof(KrylovScalars), s));
+    CsrMat mat{m, A.ptr, A.ind, A.val};
+    KV<double> v;
+    v.X = x; v.R = R; v.RP = RP; v.S = S; v.T = T; v.B = const_cast<double *>(b); v.dinv = dinv;
+    v.P[0] = P0; v.P[1] = P1; v.V[0] = V0; v.V[1] = V1;
+    const int grid = max_grid(ctx);
+    CondArg none{0, 0};
+    k_krylov_init<CsrMat><<<krylov_grid(mat, kThreads, grid), kThreads, 0, s>>>(
+        mat, v, ks, rtol, abstol, max_it, 0, ctx->red.partials, ctx->red.tickets, none);
+    UFE_CUDA(cudaGetLastError());
+    for (;;) {
+      for (int c = 0; c < 8; ++c) {
+        unsigned g = krylov_grid(mat, kThreads, grid);
+        k_p_spmv<CsrMat><<<g, kThreads, 0, s>>>(mat, v, ks, ctx->red.partials, ctx->red.tickets);
+        k_s_spmv<CsrMat><<<g, kThreads, 0, s>>>(mat, v, ks, ctx->red.partials, ctx->red.tickets);
+        k_xr<CsrMat><<<g, kThreads, 0, s>>>(mat, v, ks, ctx->red.partials, ctx->red.tickets, none);
+      }
+      UFE_CUDA(cudaGetLastError());
+      UFE_CUDA(cudaMemcpyAsync(hks, ks, sizeof(KrylovScalars), cudaMemcpyDeviceToHost, s));
+      UFE_CUDA(cudaStreamSynchronize(s));
+      if (!hks->active) break;
+    }
+    *its = hks->it;
+    status = hks->status;
+  } catch (...) {
+    cudaStreamSynchronize(s);
+    dev_free(vec);
+    dev_free(ks);
+    cudaFreeHost(hks);
+    throw;
+  }
+  dev_free(vec);
+  dev_free(ks);
+  cudaFreeHost(hks);
+  return status;
+}

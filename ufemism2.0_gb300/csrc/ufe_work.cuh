@@ -1,0 +1,133 @@
+// Solver workspace and device-side building blocks shared by the Krylov and Picard code.
+#pragma once
+
+#include "ufe_internal.cuh"
+
+// ------------------------------------------------------------------------------------------
+// Deterministic grid reductions without waiting: each block writes its partial sums, and the
+// last block to take a ticket adds all partials in block order (threadFenceReduction pattern).
+// Nothing spins, so no kernel can hang on a reduction.
+
+template <int NV>
+__device__ __forceinline__ void block_sum(double (&v)[NV], double *smem /* NV * 32 */) {
+#pragma unroll
+  for (int j = 0; j < NV; ++j)
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v[j] += __shfl_xor_sync(0xffffffffu, v[j], o);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+  __syncthreads();
+  if (lane == 0)
+#pragma unroll
+    for (int j = 0; j < NV; ++j) smem[j * 32 + warp] = v[j];
+  __syncthreads();
+  if (warp == 0) {
+#pragma unroll
+    for (int j = 0; j < NV; ++j) {
+      double t = (lane < nw) ? smem[j * 32 + lane] : 0.0;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+      v[j] = t;
+    }
+  }
+}
+
+// Reduce NV values over the grid.  Returns true in thread 0 of the last block, with `tot`
+// holding the grid totals; false everywhere else.
+template <int NV>
+__device__ bool grid_sum(double (&v)[NV], double *partials, unsigned int *ticket, double (&tot)[NV]) {
+  __shared__ double smem[NV * 32];
+  __shared__ bool am_last;
+  block_sum<NV>(v, smem);
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int j = 0; j < NV; ++j) partials[j * kMaxReduceBlocks + blockIdx.x] = v[j];
+    __threadfence();
+    unsigned int t = atomicAdd(ticket, 1u);
+    am_last = (t == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (!am_last) return false;
+  __threadfence();
+  double acc[NV];
+#pragma unroll
+  for (int j = 0; j < NV; ++j) {
+    acc[j] = 0.0;
+    for (unsigned int b = threadIdx.x; b < gridDim.x; b += blockDim.x)
+      acc[j] += __ldcg(partials + j * kMaxReduceBlocks + b);
+  }
+  block_sum<NV>(acc, smem);
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int j = 0; j < NV; ++j) tot[j] = acc[j];
+    *ticket = 0u;   // ready for the next launch (stream order separates launches)
+    return true;
+  }
+  return false;
+}
+
+// ------------------------------------------------------------------------------------------
+// Block-sparse stiffness matrix: the 2x2 blocks (u,v) x (u,v) of every triangle pair in the
+// pattern of the 2nd-order b_b operators.  blk[k] = (uu, uv, vu, vv).
+struct BsrView {
+  int32_t nb;               // block rows = nTri
+  const int32_t *ptr;       // nb+1, 0-based
+  const int32_t *col;       // nnzb
+  const double4 *blk;       // nnzb (FP64)
+  const float4 *blk32;      // nnzb (FP32 copy, or null)
+};
+
+// Krylov vectors: interleaved (u,v) per triangle, i.e. row 2(ti-1)+uv of the reference.
+struct KrylovVecs {
+  double2 *X, *R, *RP, *S, *T, *dinv, *B;
+  double2 *P[2], *V[2];
+  // FP32 inner solve
+  float2 *x32, *R32, *RP32, *S32, *T32, *dinv32;
+  float2 *P32[2], *V32[2];
+};
+
+struct Work {
+  int32_t nV = 0, nTri = 0, nz = 0;
+  int64_t nnzb = 0;
+  // stiffness matrix
+  double4 *blk = nullptr;
+  float4 *blk32 = nullptr;
+  int32_t *diag = nullptr;      // index of the diagonal block per block row
+  KrylovVecs kv{};
+  // velocity state and per-solve inputs on triangles
+  double2 *uv = nullptr;        // SSA u_b,v_b  /  DIVA u_vav,v_vav
+  double2 *tau_d = nullptr;     // driving stress
+  double *fgr_b = nullptr;
+  int32_t *bc_mask = nullptr;
+  double2 *bc_uv = nullptr;
+  int32_t has_bc = 0;
+  // DIVA state on triangles
+  double2 *uv_base = nullptr, *tau_b = nullptr;
+  double *eta_3D_b = nullptr;   // nz x nTri
+  double *bfc_b = nullptr, *F2b1 = nullptr;
+  double *beta_b = nullptr;     // applied friction on triangles (SSA) / beta_eff_b (DIVA)
+  // vertex inputs
+  double *Hi = nullptr, *Hs = nullptr, *Avav = nullptr, *A_flow = nullptr;
+  double *beta_sq = nullptr, *alpha_sq = nullptr, *effp = nullptr, *tys = nullptr;
+  int32_t *mask_gr = nullptr;
+  int32_t any_grounded = 0;
+  // vertex work
+  double *N_a = nullptr, *beta_a = nullptr, *beta_eff_a = nullptr, *F2a1 = nullptr;
+  double *eta_3D_a = nullptr;   // nz x nV
+  double *F1_3D_a = nullptr;    // nz x nV (end of solve)
+  // linearised-solve inputs given on triangles (ufe_solve_linearised / ufe_assemble_linearised)
+  double *N_b_in = nullptr, *dNx_b_in = nullptr, *dNy_b_in = nullptr, *beta_b_in = nullptr;
+  // scalars
+  KrylovScalars *ks = nullptr;
+  PicardScalars *ps = nullptr;
+  KrylovScalars *ks_host = nullptr;   // pinned mirrors
+  PicardScalars *ps_host = nullptr;
+  int *err = nullptr;             // assembly error flags
+  // graphs
+  cudaGraphExec_t graph_ssa = nullptr, graph_diva = nullptr;
+  uint64_t graph_ssa_key = 0, graph_diva_key = 0;
+};
+
+Work *ensure_work(ufe_ctx *ctx);
+
+// Lanes per block row in the BSR kernels (1, 2 or 4), chosen by the tuner.
+int32_t bsr_lanes(ufe_ctx *ctx);
