@@ -295,7 +295,12 @@ __global__ void k_xr(M mat, KV<typename M::Vec> v, KrylovScalars *ks, double *pa
   using Vec = typename M::Vec;
   using R = typename ScalarOf<Vec>::T;
   const KrylovScalars s = *ks;
-  if (!s.active) return;
+  if (!s.active) {
+    // an earlier kernel of this iteration stopped the solve: end the loop here as well, so the
+    // while-node never repeats an inactive body
+    if (blockIdx.x == 0 && threadIdx.x == 0) set_cond(cond, 0);
+    return;
+  }
   const int nxt = (s.it & 1) ^ 1;
   const R alpha = (R)s.alpha, omega = (R)s.omega;
   double acc[2] = {0.0, 0.0};
