@@ -1,0 +1,345 @@
+"""Benchmark: converged DIVA velocity solves per second on the MISMIP+-shaped channel.
+
+Workload (one step): a DIVA velocity solve from a cold start (u = 0) on the channel of
+geometry.channel_case -- 640 km x 80 km, ~58k vertices, ~115k triangles, nz = 12, Schoof2005
+friction, Picard to 1e-4 (calc_L2_norm_uv), BiCGStab/Jacobi to 1e-8 / 1e-5 (rtol / abstol).
+Synthetic data: the geometry is generated from formulas, not read from files.
+
+Arms
+  ours (default)   the GB300 library.  `value` = solves/s of the headline path (FP32 Krylov with
+                   FP64 refinement) with inputs resident in HBM, timed by CUDA events on the
+                   library's stream; `e2e` = the same through ufe_solve_diva with host buffers
+                   (pinned), H2D and D2H inside the timed region.  The plain FP64 GPU path is
+                   measured beside it.  L2 is flushed (256 MB write) before every timed solve.
+  reference        the CPU restatement of the reference's algorithm (oracle/, OpenMP on all host
+                   cores) timed on a bounded sample of the same workload (the first Picard
+                   iterations of the solve) and scaled to full solves by Krylov iteration count.
+
+Multi-GPU (`--gpus N` under torchrun): replicas -- every rank solves its own copy; value is the
+solves of all ranks over the slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+import __graft_entry__  # noqa: E402
+
+METRIC = "converged SSA/DIVA velocity solves/s, learned+FP32 vs plain FP64, 1xGB300"
+UNIT = "solves/s"
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in self.lines:
+            parts = [p.strip() for p in l.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[3:7]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f), "measured"
+    except OSError:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+def pinned_like(torch, a):
+    """A numpy view of pinned host memory holding a copy of `a` (same memory order)."""
+    t = torch.empty(a.size, dtype=torch.float64 if a.dtype == np.float64 else torch.int32).pin_memory()
+    v = t.numpy()
+    if a.ndim == 2:
+        v = v.reshape(a.shape[::-1]).T     # Fortran order view
+    else:
+        v = v.reshape(a.shape)
+    v[...] = a
+    return v, t
+
+
+def run_ours(args):
+    import torch
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    pkg = __graft_entry__.load_package()
+    pkg.build()
+    mesh, ice, params = pkg.geometry.channel_case(seed=0)
+    p64 = params
+    p32 = pkg.abi.default_params(**{f: getattr(params, f) for f, _ in params._fields_ if f != "reserved"})
+    p32.precision = pkg.abi.PREC_FP32_REFINE
+    solver = pkg.VelocitySolver(mesh, device=local)
+    solver.ice_upload(ice)
+    stream = torch.cuda.ExternalStream(solver.stream_handle())
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    def l2_flush():
+        with torch.cuda.stream(stream):
+            flush.zero_()
+
+    def solve(p):
+        return solver.solve_resident(p, diva=True, cold_start=True)
+
+    # warm-up (graph capture for both paths happens here)
+    for _ in range(args.warmup):
+        solve(p32)
+        solve(p64)
+    stats64 = []
+    for _ in range(args.steps):
+        l2_flush()
+        stats64.append(solve(p64))
+    # timed region: the headline path
+    barrier()
+    torch.cuda.synchronize()
+    stats32 = []
+    with ClockSampler(local) as clocks:
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            l2_flush()
+            stats32.append(solve(p32))
+        torch.cuda.synchronize()
+        barrier()
+        wall = time.perf_counter() - t0
+    dev_ms = sum(s["device_ms"] for s in stats32)
+    t_rank = dev_ms / 1000.0
+    if world > 1:
+        tt = torch.tensor([t_rank], device=f"cuda:{local}", dtype=torch.float64)
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        t_rank = float(tt.item())
+    value = world * args.steps / t_rank
+    fp64_value = len(stats64) / (sum(s["device_ms"] for s in stats64) / 1000.0)
+
+    # roofline of the dominant kernel: FP32 p-update + block SpMV (most launches of the headline path)
+    us32, (nb, nnzb) = solver.profile_krylov_kernels(pkg.abi.PREC_FP32_REFINE, repeats=50)
+    us64, _ = solver.profile_krylov_kernels(pkg.abi.PREC_FP64, repeats=50)
+    solve(p32)   # leave a consistent state
+    bytes32 = nnzb * (16 + 4) + (nb + 1) * 4 + nb * 7 * 8       # blocks+cols, ptr, 5 reads + 2 writes (float2)
+    bytes64 = nnzb * (32 + 4) + (nb + 1) * 4 + nb * 7 * 16
+    peaks, peak_kind = measured_peaks()
+    achieved = bytes32 / (us32[0] * 1e-6) / 1e9
+    traffic = None
+    try:
+        with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
+            traffic = json.load(f).get("k_p_spmv_fp32_bytes_per_launch")
+    except OSError:
+        pass
+
+    # end to end through ufe_solve_diva with pinned host buffers
+    keep = []
+    ice_h = {}
+    for k, v in ice.items():
+        if isinstance(v, np.ndarray) and k in ("Hi", "Hs", "A_flow", "fraction_gr_b", "mask_grounded_ice", "beta_sq",
+                                               "alpha_sq", "effective_pressure"):
+            ice_h[k], t = pinned_like(torch, v)
+            keep.append(t)
+    state0 = pkg.new_diva_state(mesh.nTri, mesh.nz)
+    st_h = {}
+    for k, v in state0.items():
+        st_h[k], t = pinned_like(torch, v)
+        keep.append(t)
+    h2d = sum(v.nbytes for v in ice_h.values()) + sum(st_h[k].nbytes for k in st_h if not k.endswith("3D_b")
+                                                      or k == "eta_3D_b")
+    d2h = sum(v.nbytes for v in st_h.values())
+    solver.solve_DIVA(ice_h, st_h, p32)  # warm
+    barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        for k in st_h:
+            st_h[k][...] = 0.0
+        solver.solve_DIVA(ice_h, st_h, p32)
+    torch.cuda.synchronize()
+    t_e2e = time.perf_counter() - t0
+    if world > 1:
+        tt = torch.tensor([t_e2e], device=f"cuda:{local}", dtype=torch.float64)
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        t_e2e = float(tt.item())
+    e2e_value = world * args.steps / t_e2e
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(pkg, mesh, ice, params, stats64[0]["n_Axb_its"], seconds=args.cpu_seconds)
+    kernels_per_iter = 3
+    launches = sum(s["n_Axb_its"] * kernels_per_iter + s["n_visc_its"] * 3 + 2 * s["n_refinements"] * s["n_visc_its"]
+                   for s in stats32)
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(dev_ms / args.steps, 3), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 Krylov + f64 refinement",
+            "data": "synthetic MISMIP+-shaped channel from formulas (no files)",
+            "config": {"workload": "DIVA channel 640x80 km, cold start, Schoof2005, Picard 1e-4, BiCGStab/Jacobi",
+                       "nV": mesh.nV, "nTri": mesh.nTri, "nz": mesh.nz, "unknowns": 2 * mesh.nTri,
+                       "stiffness_blocks_2x2": int(nnzb), "l2": "flushed (256 MB write) before every solve",
+                       "parallelism": f"replicas x{world}", "path": "FP32 Krylov + FP64 refinement, zero start"},
+            "plain_fp64": {"value": round(fp64_value, 4), "unit": UNIT,
+                           "picard_its": stats64[0]["n_visc_its"], "krylov_its": stats64[0]["n_Axb_its"],
+                           "ms_per_solve": round(sum(s["device_ms"] for s in stats64) / len(stats64), 3)},
+            "headline_its": {"picard": stats32[0]["n_visc_its"], "krylov_fp32": stats32[0]["n_Axb_its"],
+                             "refinements": stats32[0]["n_refinements"]},
+            "e2e": {"value": round(e2e_value, 4), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                    "d2h_bytes_per_step": int(d2h)},
+            "roofline": {"bound": "hbm", "kernel": "k_p_spmv<BsrMat<float,4>> (p update + 2x2-block SpMV)",
+                         "achieved": round(achieved, 1), "peak": peaks.get("hbm_gbs"), "unit": "GB/s",
+                         "frac": round(achieved / peaks.get("hbm_gbs"), 4), "peak_source": peak_kind,
+                         "traffic": traffic, "algorithmic_bytes_per_launch": int(bytes32),
+                         "us_per_launch": round(float(us32[0]), 3),
+                         "fp64_kernel_us": round(float(us64[0]), 3),
+                         "fp64_achieved_gbs": round(bytes64 / (us64[0] * 1e-6) / 1e9, 1),
+                         "note": "working set below L2 (129 MB): the iteration streams from L2, so frac can exceed 1"},
+            "cpu_baseline": cpu,
+            "clocks": clocks.summary(),
+            "gpu_launches": int(launches),
+            "wall_s_timed": round(wall, 3),
+        }
+        print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def cpu_baseline(pkg, mesh, ice, params, full_krylov_its, seconds=20.0, threads=None):
+    """Time the oracle (OpenMP on all host cores) on the first Picard iterations of the same solve
+    and scale by Krylov iterations to full solves."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    threads = threads or os.cpu_count()
+    os.environ["OMP_NUM_THREADS"] = str(threads)
+    orc = oracle.Oracle(mesh)
+    p = pkg.abi.default_params(**{f: getattr(params, f) for f, _ in params._fields_ if f != "reserved"})
+    done_its, elapsed, nit = 0, 0.0, 0
+    while elapsed < seconds and nit < 50:
+        p.visc_it_nit = nit
+        st = pkg.new_diva_state(mesh.nTri, mesh.nz, with_3d=False)
+        t0 = time.perf_counter()
+        nv, na, _ = orc.solve_DIVA(ice, st, p)
+        elapsed = time.perf_counter() - t0
+        done_its = na
+        nit = max(1, 2 * nit)
+    per_its = elapsed / max(done_its, 1)
+    value = 1.0 / (per_its * full_krylov_its)
+    return {"value": round(value, 6), "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"first {nv} Picard iterations ({done_its} Krylov its, {elapsed:.1f} s) of the same solve, "
+                      f"scaled to a full solve of {full_krylov_its} Krylov its"}
+
+
+def run_reference(args):
+    rank, world, local = dist_env()
+    if rank != 0:
+        return
+    pkg = __graft_entry__.load_package()
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    oracle.build()
+    mesh, ice, params = pkg.geometry.channel_case(seed=0)
+    full_its = args.full_krylov_its
+    vals = []
+    for i in range(args.warmup + args.steps):
+        c = cpu_baseline(pkg, mesh, ice, params, full_its, seconds=args.cpu_seconds)
+        if i >= args.warmup:
+            vals.append(c)
+    v = statistics.mean(c["value"] for c in vals)
+    line = {"metric": METRIC, "value": round(v, 6), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(1000.0 / v, 1), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic MISMIP+-shaped channel from formulas (no files)",
+            "config": {"workload": "DIVA channel 640x80 km, cold start, Schoof2005, Picard 1e-4, BiCGStab/Jacobi",
+                       "nV": mesh.nV, "nTri": mesh.nTri, "nz": mesh.nz},
+            "impl": "reference",
+            "cpu_baseline": {"value": round(v, 6), "unit": UNIT, "cores": vals[0]["cores"], "kind": "port",
+                             "sample": vals[0]["sample"]},
+            "e2e": {"value": round(v, 6), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "note": "the reference is Fortran with PETSc and has no compiler or PETSc here; this arm times the "
+                    "project's C restatement of its algorithm"}
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--full-krylov-its", type=int, default=44600,
+                    help="Krylov iterations of one full FP64 solve (the reference arm's scale)")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

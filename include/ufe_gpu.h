@@ -263,6 +263,15 @@ int32_t ufe_solve_diva_resident(ufe_ctx *ctx, const ufe_solver_params *p, int32_
                                 ufe_solve_stats *stats);
 int32_t ufe_velocity_download(ufe_ctx *ctx, double *u_b, double *v_b);
 
+/* ---- diagnostics ---------------------------------------------------------------------------- */
+/* Time the three BiCGStab kernels on the system assembled by the last solve on this context:
+ * each kernel is launched `repeats` times back to back between two CUDA events on the context's
+ * stream (the kernels are idempotent for fixed scalars).  us[0..2] receive the mean duration in
+ * microseconds of the p-update+SpMV, s-update+SpMV and x/r-update kernels; `precision` picks the
+ * FP64 or FP32 kernels.  geometry[0..1] receive the block rows and the stored 2x2 blocks. */
+int32_t ufe_profile_krylov_kernels(ufe_ctx *ctx, int32_t precision, int32_t repeats, double *us,
+                                   int64_t *geometry);
+
 #ifdef __cplusplus
 }
 #endif

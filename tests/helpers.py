@@ -25,7 +25,8 @@ def load_small_dome(pkg):
     ice = {k: np.ascontiguousarray(z[f"ice_{k}"]) for k in ("Hi", "Hs", "fraction_gr_b", "mask_grounded_ice", "beta_sq")}
     ice["A_flow"] = np.asfortranarray(np.full((mesh.nV, mesh.nz), float(z["ice_A"][0])))
     params = pkg.abi.default_params(choice_sliding_law="Weertman", visc_it_norm_dUV_tol=1e-4,
-                                    stress_balance_PETSc_rtol=1e-12, visc_it_nit=10)
+                                    stress_balance_PETSc_rtol=1e-12, stress_balance_PETSc_abstol=0.0,
+                                    visc_it_nit=10)
     ops = {}
     for name in pkg.abi.OPERATORS:
         ops[name] = pkg.CSR(0, 0, z[f"op_{name}_ptr"], z[f"op_{name}_ind"], z[f"op_{name}_val"], 1)

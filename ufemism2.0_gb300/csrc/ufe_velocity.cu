@@ -665,6 +665,14 @@ __global__ void k_diva_u3d(int nV, int nTri, int nz, OpRow ab, const double *F1_
 }
 
 // ---- small helpers ---------------------------------------------------------------------------
+// Sets *flag when any of the n values is NaN or infinite.
+__global__ void k_check_finite(const double *a, int64_t n, int *flag) {
+  int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  bool bad = false;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) bad |= !isfinite(a[i]);
+  if (__syncthreads_or(bad) && threadIdx.x == 0) atomicOr(flag, 1);
+}
+
 __global__ void k_interleave(int n, const double *a, const double *b, double2 *out) {
   int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
@@ -1296,6 +1304,20 @@ extern "C" int32_t ufe_ice_upload(ufe_ctx *ctx, const ufe_ice_state *ice, const 
     upload_opt(w->alpha_sq, ice->alpha_sq, nV, s);
     upload_opt(w->effp, ice->effective_pressure, nV, s);
     upload_opt(w->tys, ice->till_yield_stress, nV, s);
+    // NaN/Inf in any input field is an error (the reference's do_check_for_NaN checks)
+    {
+      int *flag = w->err;
+      UFE_CUDA(cudaMemsetAsync(flag, 0, sizeof(int), s));
+      const double *arrs[] = {w->Hi, w->Hs, w->A_flow, w->fgr_b, w->beta_sq, w->alpha_sq, w->effp, w->tys};
+      const size_t lens[] = {nV, nV, nV * nz, nTri, nV, nV, nV, nV};
+      for (int k = 0; k < 8; ++k)
+        k_check_finite<<<pick_blocks((int64_t)lens[k], kThreads, 256), kThreads, 0, s>>>(arrs[k], (int64_t)lens[k], flag);
+      UFE_CUDA(cudaGetLastError());
+      int hflag = 0;
+      UFE_CUDA(cudaMemcpyAsync(&hflag, flag, sizeof(int), cudaMemcpyDeviceToHost, s));
+      UFE_CUDA(cudaStreamSynchronize(s));
+      UFE_REQUIRE(hflag == 0, UFE_ERR_NAN, "NaN or infinite value in the ice state");
+    }
     int any = 0;
     for (size_t v = 0; v < nV && !any; ++v) any = ice->mask_grounded_ice[v] != 0;
     w->any_grounded = any;
@@ -1583,6 +1605,67 @@ extern "C" int32_t ufe_solve_linearised(ufe_ctx *ctx, const ufe_solver_params *p
     if (n_Axb_its)
       *n_Axb_its = (p->precision == UFE_PREC_FP32_REFINE) ? w->ks_host[1].total_its : w->ks_host[0].it;
     return w->ks_host[0].status;
+  });
+}
+
+extern "C" int32_t ufe_profile_krylov_kernels(ufe_ctx *ctx, int32_t precision, int32_t repeats, double *us,
+                                              int64_t *geometry) {
+  return guarded(ctx, [&]() -> int32_t {
+    UFE_REQUIRE(us && repeats >= 1, UFE_ERR_INVALID, "bad profile arguments");
+    UFE_CUDA(cudaSetDevice(ctx->device));
+    Work *w = ensure_work(ctx);
+    ufe_solver_params p;
+    ufe_default_params(&p);
+    p.precision = precision;
+    Solver S(ctx, p);
+    // a live iteration state: the scalars stay active (ttol 0, huge rnorm0 and max_it), so every
+    // launch does its full work
+    KrylovScalars ks;
+    memset(&ks, 0, sizeof(ks));
+    ks.active = 1; ks.rho = 1.0; ks.rhoold = 1.0; ks.alpha = 0.5; ks.omega = 0.5; ks.omegaold = 0.5;
+    ks.beta = 0.5; ks.ttol = 0.0; ks.rnorm0 = 1e300; ks.max_it = 1 << 30;
+    KrylovScalars *dks = w->ks + (precision == UFE_PREC_FP32_REFINE ? 1 : 0);
+    cudaStream_t s = S.s;
+    auto time_kernel = [&](auto launch) -> double {
+      UFE_CUDA(cudaMemcpyAsync(dks, &ks, sizeof(ks), cudaMemcpyHostToDevice, s));
+      launch();
+      UFE_CUDA(cudaEventRecord(ctx->ev0, s));
+      for (int r = 0; r < repeats; ++r) launch();   // the scalars stay active: ttol 0, no max_it
+      UFE_CUDA(cudaEventRecord(ctx->ev1, s));
+      UFE_CUDA(cudaEventSynchronize(ctx->ev1));
+      float ms = 0.f;
+      UFE_CUDA(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+      return 1000.0 * ms / repeats;
+    };
+    CondArg none{0, 0};
+    auto run3 = [&](auto mat, auto v) {
+      unsigned g = krylov_grid(mat, kThreads, S.grid);
+      unsigned g2 = pick_blocks(mat.items, kThreads, S.grid);
+      us[0] = time_kernel([&] { k_p_spmv<decltype(mat)><<<g, kThreads, 0, s>>>(mat, v, dks, ctx->red.partials, ctx->red.tickets); });
+      us[1] = time_kernel([&] { k_s_spmv<decltype(mat)><<<g, kThreads, 0, s>>>(mat, v, dks, ctx->red.partials, ctx->red.tickets); });
+      us[2] = time_kernel([&] { k_xr<decltype(mat)><<<g2, kThreads, 0, s>>>(mat, v, dks, ctx->red.partials, ctx->red.tickets, none); });
+    };
+    // the kernels read the matrix and vectors left by the last solve
+    if (precision == UFE_PREC_FP32_REFINE) {
+      switch (S.lanes) {
+        case 1: run3(S.mat32<1>(), S.kv32()); break;
+        case 2: run3(S.mat32<2>(), S.kv32()); break;
+        case 8: run3(S.mat32<8>(), S.kv32()); break;
+        default: run3(S.mat32<4>(), S.kv32()); break;
+      }
+    } else {
+      switch (S.lanes) {
+        case 1: run3(S.mat64<1>(), S.kv64()); break;
+        case 2: run3(S.mat64<2>(), S.kv64()); break;
+        case 8: run3(S.mat64<8>(), S.kv64()); break;
+        default: run3(S.mat64<4>(), S.kv64()); break;
+      }
+    }
+    UFE_CUDA(cudaGetLastError());
+    UFE_CUDA(cudaMemsetAsync(w->ks, 0, sizeof(KrylovScalars) * 2, s));
+    UFE_CUDA(cudaStreamSynchronize(s));
+    if (geometry) { geometry[0] = ctx->nTri; geometry[1] = w->nnzb; }
+    return UFE_OK;
   });
 }
 

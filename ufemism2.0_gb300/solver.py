@@ -244,6 +244,14 @@ class VelocitySolver:
         self._check(fn(self.ctx, C.byref(params), 1 if cold_start else 0, C.byref(stats)))
         return stats.as_dict()
 
+    def profile_krylov_kernels(self, precision: int, repeats: int = 50):
+        """Mean device time [us] of the three BiCGStab kernels on the last assembled system,
+        plus (block rows, stored 2x2 blocks)."""
+        us = np.zeros(3)
+        geo = (C.c_int64 * 2)()
+        self._check(self.lib.ufe_profile_krylov_kernels(self.ctx, precision, repeats, abi.as_d(us), geo))
+        return us, (geo[0], geo[1])
+
     def velocity_download(self):
         u, v = np.zeros(self.mesh.nTri), np.zeros(self.mesh.nTri)
         self._check(self.lib.ufe_velocity_download(self.ctx, abi.as_d(u), abi.as_d(v)))
