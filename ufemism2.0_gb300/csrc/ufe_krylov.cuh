@@ -75,11 +75,12 @@ __device__ __forceinline__ float2 v_add(float2 a, float2 b) { return make_float2
 __device__ __forceinline__ double v_add(double a, double b) { return a + b; }
 
 // ---- matrix access policies ---------------------------------------------------------------
-// 2x2-block rows (one triangle = its u and v rows), FP64 or FP32 blocks; L lanes per block row.
-template <typename Real, int L>
+// 2x2-block rows (one triangle = its u and v rows); blocks stored in MatReal (FP64 or FP32),
+// vectors and accumulation in VecReal; L lanes per block row.
+template <typename MatReal, typename VecReal, int L>
 struct BsrMat {
-  using Vec = typename std::conditional<sizeof(Real) == 8, double2, float2>::type;
-  using Blk = typename std::conditional<sizeof(Real) == 8, double4, float4>::type;
+  using Vec = typename std::conditional<sizeof(VecReal) == 8, double2, float2>::type;
+  using Blk = typename std::conditional<sizeof(MatReal) == 8, double4, float4>::type;
   static constexpr int kLanes = L;
   int32_t items;
   const int32_t *__restrict__ ptr;

@@ -278,7 +278,6 @@ struct AssembleArgs {
   double4 *blk;
   float4 *blk32;
   double2 *rhs, *dinv, *X, *R, *RP, *P0, *V0;
-  float2 *dinv32;
   double *beta_b_out, *bfc_b, *F2b1, *eta_3D_b;
   int *err;
   // Krylov
@@ -408,7 +407,6 @@ __global__ void k_assemble(AssembleArgs a, PhysParams q, CondArg cond) {
         double4 b = a.blk[k];
         a.blk32[k] = make_float4((float)b.x, (float)b.y, (float)b.z, (float)b.w);
       }
-      a.dinv32[t] = make_float2((float)di.x, (float)di.y);
     }
     // -- Krylov initial residual r = D^-1 (b - A x0)
     double2 ax = make_double2(0.0, 0.0);
@@ -452,6 +450,7 @@ __global__ void k_assemble(AssembleArgs a, PhysParams q, CondArg cond) {
     s.status = UFE_OK;
     s.tbreak = 0;
     s.refinements = 0;
+    s.pad = 0;
     s.active = 1;
     if (isnan(dp)) { s.status = UFE_ERR_NAN; s.active = 0; }
     else if (dp <= s.ttol) s.active = 0;
@@ -461,30 +460,31 @@ __global__ void k_assemble(AssembleArgs a, PhysParams q, CondArg cond) {
   }
 }
 
-// ---- FP32 inner solve with FP64 refinement --------------------------------------------------
-// inner system: (D^-1 A) d = r with r the FP64 residual, solved from d = 0 in FP32
-__global__ void k_inner_init(int nTri, const double2 *R, float2 *R32, float2 *RP32, float2 *x32,
-                             float2 *P32, float2 *V32, const KrylovScalars *outer, KrylovScalars *ks32,
+// ---- FP32-matrix inner solve with FP64 refinement ---------------------------------------------
+// The inner BiCGStab applies the FP32 copy of the stiffness blocks (FP64 vectors and sums) to
+// the correction system (D^-1 A32) d = r, with r the FP64 residual; the outer loop adds d to x
+// and recomputes r in FP64 with the FP64 blocks until the FP64 test passes.
+__global__ void k_inner_init(int nTri, const double2 *R, double2 *Rin, double2 *RPin, double2 *Xin,
+                             double2 *P0, double2 *V0, const KrylovScalars *outer, KrylovScalars *ksi,
                              double inner_rtol, int max_it, double *partials, unsigned int *tickets,
                              CondArg cond) {
   double acc[1] = {0.0};
   int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < nTri; t += stride) {
     double2 r = R[t];
-    float2 r32 = make_float2((float)r.x, (float)r.y);
-    R32[t] = r32;
-    RP32[t] = r32;
-    x32[t] = make_float2(0.f, 0.f);
-    P32[t] = make_float2(0.f, 0.f);
-    V32[t] = make_float2(0.f, 0.f);
-    acc[0] += (double)r32.x * r32.x + (double)r32.y * r32.y;
+    Rin[t] = r;
+    RPin[t] = r;
+    Xin[t] = make_double2(0.0, 0.0);
+    P0[t] = make_double2(0.0, 0.0);
+    V0[t] = make_double2(0.0, 0.0);
+    acc[0] += r.x * r.x + r.y * r.y;
   }
   double tot[1];
   if (grid_sum<1>(acc, partials, tickets + kSiteInner, tot)) {
     KrylovScalars s;
     memset(&s, 0, sizeof(s));
     const KrylovScalars o = *outer;
-    s.total_its = ks32->total_its;
+    s.total_its = ksi->total_its;
     double dp = sqrt(tot[0]);
     s.dp = dp;
     s.rnorm0 = dp;
@@ -495,26 +495,27 @@ __global__ void k_inner_init(int nTri, const double2 *R, float2 *R32, float2 *RP
     s.rhoold = s.alpha = s.omegaold = s.omega = 1.0;
     s.beta = s.rho;
     s.active = (dp > s.ttol && s.rho != 0.0) ? 1 : 0;
-    *ks32 = s;
+    *ksi = s;
     set_cond(cond, s.active);
   }
 }
 
-__global__ void k_xadd(int nTri, double2 *X, const float2 *x32) {
+// x += d, unless the inner solve failed (then x is left as it was)
+__global__ void k_xadd(int nTri, double2 *X, const double2 *Xin, const KrylovScalars *ksi) {
+  if (ksi->status < 0) return;
   int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < nTri; t += stride) {
-    double2 x = X[t];
-    float2 d = x32[t];
-    X[t] = make_double2(x.x + (double)d.x, x.y + (double)d.y);
+    double2 x = X[t], d = Xin[t];
+    X[t] = make_double2(x.x + d.x, x.y + d.y);
   }
 }
 
 // FP64 residual r = D^-1 (b - A x) and the outer (refinement) convergence test
 template <int L>
-__global__ void k_residual64(BsrMat<double, L> mat, const double2 *X, const double2 *B, const double2 *dinv,
+__global__ void k_residual64(BsrMat<double, double, L> mat, const double2 *X, const double2 *B, const double2 *dinv,
                              double2 *R, KrylovScalars *ks, const KrylovScalars *ks32, double *partials,
                              unsigned int *tickets, CondArg cond) {
-  using MT = BsrMat<double, L>;
+  using MT = BsrMat<double, double, L>;
   double acc[1] = {0.0};
   KRYLOV_ROWS(MT, i, lane) {
     const int i = (int)i_64;
@@ -536,8 +537,9 @@ __global__ void k_residual64(BsrMat<double, L> mat, const double2 *X, const doub
     s.dp = dp;
     s.refinements += 1;
     s.it += in.it;
-    if (in.status < 0 && in.status != UFE_ERR_DIVERGED) { s.status = in.status; s.active = 0; }
-    else if (isnan(dp)) { s.status = UFE_ERR_NAN; s.active = 0; }
+    if (in.status < 0) s.pad += 1;   // a failed inner solve added nothing; count it
+    if (isnan(dp)) { s.status = UFE_ERR_NAN; s.active = 0; }
+    else if (s.pad >= 3) { s.status = UFE_ERR_DIVERGED; s.active = 0; }
     else if (dp <= s.ttol) s.active = 0;
     else if (s.refinements >= kMaxRefine || s.it >= s.max_it) { s.status = UFE_WARN_KRYLOV_MAXIT; s.active = 0; }
     *ks = s;
@@ -793,8 +795,8 @@ Work *ensure_work(ufe_ctx *ctx) {
   KrylovVecs &k = w->kv;
   double2 **d2[] = {&k.X, &k.R, &k.RP, &k.S, &k.T, &k.dinv, &k.B, &k.P[0], &k.P[1], &k.V[0], &k.V[1]};
   for (auto p : d2) *p = alloc_n<double2>(nTri);
-  float2 **f2[] = {&k.x32, &k.R32, &k.RP32, &k.S32, &k.T32, &k.dinv32, &k.P32[0], &k.P32[1], &k.V32[0], &k.V32[1]};
-  for (auto p : f2) *p = alloc_n<float2>(nTri);
+  k.Xin = alloc_n<double2>(nTri);
+  k.Rin = alloc_n<double2>(nTri);
   w->uv = alloc_n<double2>(nTri);
   w->tau_d = alloc_n<double2>(nTri);
   w->fgr_b = alloc_n<double>(nTri);
@@ -848,9 +850,7 @@ void free_work(ufe_ctx *ctx) {
   if (w->graph_ssa) cudaGraphExecDestroy(w->graph_ssa);
   if (w->graph_diva) cudaGraphExecDestroy(w->graph_diva);
   void *ptrs[] = {w->blk, w->blk32, w->kv.X, w->kv.R, w->kv.RP, w->kv.S, w->kv.T, w->kv.dinv, w->kv.B,
-                  w->kv.P[0], w->kv.P[1], w->kv.V[0], w->kv.V[1], w->kv.x32, w->kv.R32, w->kv.RP32,
-                  w->kv.S32, w->kv.T32, w->kv.dinv32, w->kv.P32[0], w->kv.P32[1], w->kv.V32[0],
-                  w->kv.V32[1], w->uv, w->tau_d, w->fgr_b, w->bc_mask, w->bc_uv, w->uv_base, w->tau_b,
+                  w->kv.P[0], w->kv.P[1], w->kv.V[0], w->kv.V[1], w->kv.Xin, w->kv.Rin, w->uv, w->tau_d, w->fgr_b, w->bc_mask, w->bc_uv, w->uv_base, w->tau_b,
                   w->eta_3D_b, w->bfc_b, w->F2b1, w->beta_b, w->Hi, w->Hs, w->Avav, w->A_flow, w->beta_sq,
                   w->alpha_sq, w->effp, w->tys, w->mask_gr, w->N_a, w->beta_a, w->beta_eff_a, w->F2a1,
                   w->eta_3D_a, w->F1_3D_a, w->N_b_in, w->dNx_b_in, w->dNy_b_in, w->beta_b_in, w->ks,
@@ -921,7 +921,7 @@ struct Solver {
     a.blk = w->blk;
     a.blk32 = (p.precision == UFE_PREC_FP32_REFINE) ? w->blk32 : nullptr;
     a.rhs = w->kv.B; a.dinv = w->kv.dinv; a.X = w->kv.X; a.R = w->kv.R; a.RP = w->kv.RP;
-    a.P0 = w->kv.P[0]; a.V0 = w->kv.V[0]; a.dinv32 = w->kv.dinv32;
+    a.P0 = w->kv.P[0]; a.V0 = w->kv.V[0];
     a.beta_b_out = w->beta_b; a.bfc_b = w->bfc_b; a.F2b1 = w->F2b1; a.eta_3D_b = w->eta_3D_b;
     a.err = w->err;
     a.ks = w->ks;
@@ -953,14 +953,14 @@ struct Solver {
   }
 
   template <int L>
-  BsrMat<double, L> mat64() const {
+  BsrMat<double, double, L> mat64() const {
     const DevCSR &m2 = ctx->ops[UFE_OP_M2_DDX_B_B];
-    return BsrMat<double, L>{w->nTri, m2.ptr, m2.ind, w->blk};
+    return BsrMat<double, double, L>{w->nTri, m2.ptr, m2.ind, w->blk};
   }
   template <int L>
-  BsrMat<float, L> mat32() const {
+  BsrMat<float, double, L> mat32() const {
     const DevCSR &m2 = ctx->ops[UFE_OP_M2_DDX_B_B];
-    return BsrMat<float, L>{w->nTri, m2.ptr, m2.ind, w->blk32};
+    return BsrMat<float, double, L>{w->nTri, m2.ptr, m2.ind, w->blk32};
   }
   KV<double2> kv64() const {
     KV<double2> v;
@@ -969,14 +969,14 @@ struct Solver {
     v.P[0] = w->kv.P[0]; v.P[1] = w->kv.P[1]; v.V[0] = w->kv.V[0]; v.V[1] = w->kv.V[1];
     return v;
   }
-  KV<float2> kv32() const {
-    KV<float2> v;
-    v.X = w->kv.x32; v.R = w->kv.R32; v.RP = w->kv.RP32; v.S = w->kv.S32; v.T = w->kv.T32; v.B = nullptr;
-    v.dinv = w->kv.dinv32;
-    v.P[0] = w->kv.P32[0]; v.P[1] = w->kv.P32[1]; v.V[0] = w->kv.V32[0]; v.V[1] = w->kv.V32[1];
+  // inner (correction) solve: own x and r, the outer's other work vectors
+  KV<double2> kv_inner() const {
+    KV<double2> v;
+    v.X = w->kv.Xin; v.R = w->kv.Rin; v.RP = w->kv.RP; v.S = w->kv.S; v.T = w->kv.T; v.B = nullptr;
+    v.dinv = w->kv.dinv;
+    v.P[0] = w->kv.P[0]; v.P[1] = w->kv.P[1]; v.V[0] = w->kv.V[0]; v.V[1] = w->kv.V[1];
     return v;
   }
-
   void krylov_iter64(CondArg c) {
     switch (lanes) {
       case 1: enqueue_krylov_iter(mat64<1>(), kv64(), w->ks, c); break;
@@ -987,26 +987,26 @@ struct Solver {
   }
   void krylov_iter32(CondArg c) {
     switch (lanes) {
-      case 1: enqueue_krylov_iter(mat32<1>(), kv32(), w->ks + 1, c); break;
-      case 2: enqueue_krylov_iter(mat32<2>(), kv32(), w->ks + 1, c); break;
-      case 8: enqueue_krylov_iter(mat32<8>(), kv32(), w->ks + 1, c); break;
-      default: enqueue_krylov_iter(mat32<4>(), kv32(), w->ks + 1, c); break;
+      case 1: enqueue_krylov_iter(mat32<1>(), kv_inner(), w->ks + 1, c); break;
+      case 2: enqueue_krylov_iter(mat32<2>(), kv_inner(), w->ks + 1, c); break;
+      case 8: enqueue_krylov_iter(mat32<8>(), kv_inner(), w->ks + 1, c); break;
+      default: enqueue_krylov_iter(mat32<4>(), kv_inner(), w->ks + 1, c); break;
     }
   }
   void enqueue_inner_init(CondArg c) {
     k_inner_init<<<eblocks(w->nTri), kThreads, 0, s>>>(
-        w->nTri, w->kv.R, w->kv.R32, w->kv.RP32, w->kv.x32, w->kv.P32[0], w->kv.V32[0], w->ks, w->ks + 1,
+        w->nTri, w->kv.R, w->kv.Rin, w->kv.RP, w->kv.Xin, w->kv.P[0], w->kv.V[0], w->ks, w->ks + 1,
         p.krylov_inner_rtol, p.krylov_max_it, ctx->red.partials, ctx->red.tickets, c);
     UFE_CUDA(cudaGetLastError());
   }
   template <int L>
   void residual64_l(CondArg c) {
-    BsrMat<double, L> m = mat64<L>();
+    BsrMat<double, double, L> m = mat64<L>();
     k_residual64<L><<<krylov_grid(m, kThreads, grid), kThreads, 0, s>>>(
         m, w->kv.X, w->kv.B, w->kv.dinv, w->kv.R, w->ks, w->ks + 1, ctx->red.partials, ctx->red.tickets, c);
   }
   void enqueue_refine_update(CondArg c) {
-    k_xadd<<<eblocks(w->nTri), kThreads, 0, s>>>(w->nTri, w->kv.X, w->kv.x32);
+    k_xadd<<<eblocks(w->nTri), kThreads, 0, s>>>(w->nTri, w->kv.X, w->kv.Xin, w->ks + 1);
     switch (lanes) {
       case 1: residual64_l<1>(c); break;
       case 2: residual64_l<2>(c); break;
@@ -1648,10 +1648,10 @@ extern "C" int32_t ufe_profile_krylov_kernels(ufe_ctx *ctx, int32_t precision, i
     // the kernels read the matrix and vectors left by the last solve
     if (precision == UFE_PREC_FP32_REFINE) {
       switch (S.lanes) {
-        case 1: run3(S.mat32<1>(), S.kv32()); break;
-        case 2: run3(S.mat32<2>(), S.kv32()); break;
-        case 8: run3(S.mat32<8>(), S.kv32()); break;
-        default: run3(S.mat32<4>(), S.kv32()); break;
+        case 1: run3(S.mat32<1>(), S.kv_inner()); break;
+        case 2: run3(S.mat32<2>(), S.kv_inner()); break;
+        case 8: run3(S.mat32<8>(), S.kv_inner()); break;
+        default: run3(S.mat32<4>(), S.kv_inner()); break;
       }
     } else {
       switch (S.lanes) {

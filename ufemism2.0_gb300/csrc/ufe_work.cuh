@@ -80,9 +80,8 @@ struct BsrView {
 struct KrylovVecs {
   double2 *X, *R, *RP, *S, *T, *dinv, *B;
   double2 *P[2], *V[2];
-  // FP32 inner solve
-  float2 *x32, *R32, *RP32, *S32, *T32, *dinv32;
-  float2 *P32[2], *V32[2];
+  // inner (correction) solve of the FP32-matrix path
+  double2 *Xin, *Rin;
 };
 
 struct Work {
