@@ -30,7 +30,8 @@ extern "C" {
 /* ---- status codes -------------------------------------------------------------------------- */
 #define UFE_OK                    0
 #define UFE_WARN_PICARD_MAXIT     1   /* viscosity iteration hit visc_it_nit (SSA_main.f90:229-232) */
-#define UFE_WARN_KRYLOV_MAXIT     2   /* a Krylov solve stopped at krylov_max_it before the tolerance */
+#define UFE_WARN_KRYLOV_MAXIT     2   /* a Krylov solve stopped before its tolerance (iteration limit,
+                                         divergence or breakdown); the Picard loop went on */
 #define UFE_ERR_INVALID          -1   /* bad argument or missing setup step */
 #define UFE_ERR_NAN              -2   /* NaN/Inf in a result or an input */
 #define UFE_ERR_DIVERGED         -3   /* Picard divergence limits (SSA_main.f90:207-213) or Krylov breakdown */
@@ -264,6 +265,11 @@ int32_t ufe_solve_diva_resident(ufe_ctx *ctx, const ufe_solver_params *p, int32_
 int32_t ufe_velocity_download(ufe_ctx *ctx, double *u_b, double *v_b);
 
 /* ---- diagnostics ---------------------------------------------------------------------------- */
+/* Per-Picard-iteration record of the last solve on this context: `cap` rows of 5 values
+ * (L2 change norm, Krylov iterations, Krylov status, final Krylov residual, FP64 refinement
+ * steps); *n receives the rows written (at most 128). */
+int32_t ufe_solve_history(ufe_ctx *ctx, double *out, int32_t cap, int32_t *n);
+
 /* Time the three BiCGStab kernels on the system assembled by the last solve on this context:
  * each kernel is launched `repeats` times back to back between two CUDA events on the context's
  * stream (the kernels are idempotent for fixed scalars).  us[0..2] receive the mean duration in

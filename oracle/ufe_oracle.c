@@ -906,8 +906,9 @@ int32_t orc_solve_ssa(const ufe_mesh_desc *m, const orc_csr *ops, const ufe_solv
     int32_t its = 0;
     int32_t rc = linear_solve(m, ops, p, u_b, v_b, N_b, dN_dx_b, dN_dy_b, beta_b, tdx, tdy, up, vp, bc, &its);
     n_axb += its;
-    if (rc < 0) { status = rc; break; }
-    if (rc == UFE_WARN_KRYLOV_MAXIT) status = UFE_WARN_KRYLOV_MAXIT;
+    /* the reference does not act on PETSc's converged reason: only NaN stops the loop */
+    if (rc == UFE_ERR_NAN || rc == UFE_ERR_INVALID) { status = rc; break; }
+    if (rc != UFE_OK && status == UFE_OK) status = UFE_WARN_KRYLOV_MAXIT;
     velocity_limits(nTri, p->vel_max, u_b, v_b);
     relax(nTri, relax_applied, u_b, v_b, up, vp);
     L2_prev = L2;
@@ -1044,8 +1045,9 @@ int32_t orc_solve_diva(const ufe_mesh_desc *m, const orc_csr *ops, const ufe_sol
     int32_t rc = linear_solve(m, ops, p, ds->u_vav_b, ds->v_vav_b, N_b, dN_dx_b, dN_dy_b, beta_eff_b,
                               tdx, tdy, up, vp, bc, &its);
     n_axb += its;
-    if (rc < 0) { status = rc; break; }
-    if (rc == UFE_WARN_KRYLOV_MAXIT) status = UFE_WARN_KRYLOV_MAXIT;
+    /* the reference does not act on PETSc's converged reason: only NaN stops the loop */
+    if (rc == UFE_ERR_NAN || rc == UFE_ERR_INVALID) { status = rc; break; }
+    if (rc != UFE_OK && status == UFE_OK) status = UFE_WARN_KRYLOV_MAXIT;
     velocity_limits(nTri, p->vel_max, ds->u_vav_b, ds->v_vav_b);
     relax(nTri, relax_applied, ds->u_vav_b, ds->v_vav_b, up, vp);
     /* calc_basal_velocities */

@@ -54,11 +54,16 @@ struct KrylovScalars {
   int32_t pad;
 };
 
+constexpr int kHistMax = 128;   // Picard iterations recorded per solve
+constexpr int kHistCols = 5;    // L2, Krylov iterations, Krylov status, final residual, refinements
+
 struct PicardScalars {
   double L2, L2_prev, relax, eps0, eta_max;
   int32_t it, nit_diverg, active, status;
   int32_t n_refine;
-  int32_t pad[3];
+  int32_t prev_total_its;
+  int32_t pad[2];
+  double hist[kHistMax * kHistCols];
 };
 
 // Partial sums of one reduction stage: each block writes `nparts` values at

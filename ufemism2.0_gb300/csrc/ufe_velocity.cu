@@ -152,15 +152,18 @@ __global__ void k_prologue(int nV, int nTri, int nz, OpRow ab, const double *Hi,
       Avav[v] = a;
     }
   if (blockIdx.x == 0 && threadIdx.x == 0) {
-    PicardScalars p;
-    memset(&p, 0, sizeof(p));
+    PicardScalars &p = *ps;
     p.L2 = 1e9;
     p.L2_prev = 1e9;
     p.relax = relax0;
     p.eps0 = eps0;
     p.eta_max = 0.5 * pow(1e-18, -1.0 / n_glen) * pow(eps0, (1.0 - n_glen) / (2.0 * n_glen));
+    p.it = 0;
+    p.nit_diverg = 0;
+    p.status = UFE_OK;
+    p.n_refine = 0;
+    p.prev_total_its = 0;
     p.active = 1;
-    *ps = p;
     KrylovScalars k;
     memset(&k, 0, sizeof(k));
     *ks = k;
@@ -552,18 +555,31 @@ __global__ void k_residual64(BsrMat<double, double, L> mat, const double2 *X, co
 // iteration limit (:228-232).  Runs in the last block of the finalize reduction.
 __device__ void picard_step(PicardScalars *psp, KrylovScalars *ks, double r1, double r2, const PhysParams &q,
                             double n_glen, CondArg cond) {
-  PicardScalars p = *psp;
-  KrylovScalars k = *ks;
+  PicardScalars &p = *psp;
+  const KrylovScalars k = *ks;
+  const KrylovScalars kin = ks[1];
   p.it += 1;
   p.n_refine += k.refinements;
-  if (k.status < 0) {
+  const int total = (k.refinements > 0) ? kin.total_its : k.total_its;
+  if (p.it <= kHistMax) {
+    double *h = p.hist + (p.it - 1) * kHistCols;
+    h[0] = 2.0 * r1 / fmax(r2, 1e-8);
+    h[1] = (double)(total - p.prev_total_its);
+    h[2] = (double)k.status;
+    h[3] = k.dp;
+    h[4] = (double)k.refinements;
+  }
+  p.prev_total_its = total;
+  // A Krylov solve that did not reach its tolerance (iteration limit, divergence, breakdown)
+  // leaves its last iterate, and the viscosity iteration goes on: solve_matrix_equation_PETSc
+  // does not act on PETSc's converged reason (petsc_basic.f90:106-141).  NaN stops the solve.
+  if (k.status == UFE_ERR_NAN) {
     p.status = k.status;
     p.active = 0;
-    *psp = p;
     set_cond(cond, 0);
     return;
   }
-  if (k.status == UFE_WARN_KRYLOV_MAXIT) p.status = UFE_WARN_KRYLOV_MAXIT;
+  if (k.status != UFE_OK && p.status == UFE_OK) p.status = UFE_WARN_KRYLOV_MAXIT;
   p.L2_prev = p.L2;
   p.L2 = 2.0 * r1 / fmax(r2, 1e-8);
   if (p.L2 > p.L2_prev) p.nit_diverg += 1; else p.nit_diverg = 0;
@@ -588,7 +604,6 @@ __device__ void picard_step(PicardScalars *psp, KrylovScalars *ks, double r1, do
     p.status = UFE_WARN_PICARD_MAXIT;
   }
   p.active = (!stop && !converged) ? 1 : 0;
-  *psp = p;
   set_cond(cond, p.active);
 }
 
@@ -1403,6 +1418,21 @@ static void upload_pair(ufe_ctx *ctx, double2 *dst, const double *a, const doubl
   UFE_CUDA(cudaStreamSynchronize(s));
   dev_free(ta);
   dev_free(tb);
+}
+
+extern "C" int32_t ufe_solve_history(ufe_ctx *ctx, double *out, int32_t cap, int32_t *n) {
+  return guarded(ctx, [&]() -> int32_t {
+    UFE_REQUIRE(out && n && cap >= 0, UFE_ERR_INVALID, "bad history arguments");
+    UFE_REQUIRE(ctx->work, UFE_ERR_INVALID, "no solve has run on this context");
+    Work *w = ctx->work;
+    UFE_CUDA(cudaMemcpyAsync(w->ps_host, w->ps, sizeof(PicardScalars), cudaMemcpyDeviceToHost, ctx->stream));
+    UFE_CUDA(cudaStreamSynchronize(ctx->stream));
+    int rows = w->ps_host->it < kHistMax ? w->ps_host->it : kHistMax;
+    if (rows > cap) rows = cap;
+    memcpy(out, w->ps_host->hist, sizeof(double) * rows * kHistCols);
+    *n = rows;
+    return UFE_OK;
+  });
 }
 
 extern "C" int32_t ufe_velocity_download(ufe_ctx *ctx, double *u_b, double *v_b) {

@@ -244,6 +244,13 @@ class VelocitySolver:
         self._check(fn(self.ctx, C.byref(params), 1 if cold_start else 0, C.byref(stats)))
         return stats.as_dict()
 
+    def history(self):
+        """Per-Picard-iteration rows (L2, Krylov its, Krylov status, final residual, refinements)."""
+        out = np.zeros((128, 5))
+        n = C.c_int32()
+        self._check(self.lib.ufe_solve_history(self.ctx, abi.as_d(out), 128, C.byref(n)))
+        return out[:n.value]
+
     def profile_krylov_kernels(self, precision: int, repeats: int = 50):
         """Mean device time [us] of the three BiCGStab kernels on the last assembled system,
         plus (block rows, stored 2x2 blocks)."""
