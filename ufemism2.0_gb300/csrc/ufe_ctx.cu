@@ -45,6 +45,7 @@ static void free_mesh(ufe_ctx *ctx) {
   for (void *p : ptrs) dev_free(p);
   ctx->V = ctx->TriGC = ctx->zeta = nullptr;
   ctx->nC = ctx->C = ctx->niTri = ctx->iTri = ctx->VBI = ctx->Tri = ctx->TriC = ctx->TriBI = nullptr;
+  free_layout(ctx);
   ctx->has_mesh = false;
 }
 
@@ -193,16 +194,7 @@ extern "C" int32_t ufe_mesh_upload(ufe_ctx *ctx, const ufe_mesh_desc *m) {
     ctx->nTri = m->nTri;
     ctx->nC_mem = m->nC_mem;
     ctx->nz = m->nz;
-    ctx->V = upload(m->V, 2 * nV, s);
-    ctx->nC = upload(m->nC, nV, s);
-    ctx->C = upload(m->C, nV * nCm, s);
-    ctx->niTri = upload(m->niTri, nV, s);
-    ctx->iTri = upload(m->iTri, nV * nCm, s);
-    ctx->VBI = upload(m->VBI, nV, s);
-    ctx->Tri = upload(m->Tri, 3 * nTri, s);
-    ctx->TriC = upload(m->TriC, 3 * nTri, s);
-    ctx->TriBI = upload(m->TriBI, nTri, s);
-    ctx->TriGC = upload(m->TriGC, 2 * nTri, s);
+    layout_upload_mesh(ctx, m);   // renumbered into the internal Z-order layout
     ctx->zeta = upload(m->zeta, m->nz, s);
     ctx->zeta_host.assign(m->zeta, m->zeta + m->nz);
     UFE_CUDA(cudaStreamSynchronize(s));
@@ -254,6 +246,7 @@ extern "C" int32_t ufe_mesh_set_operator(ufe_ctx *ctx, int32_t op, int32_t m, in
     UFE_REQUIRE(m == em && n == en, UFE_ERR_INVALID, "operator shape does not match the mesh");
     UFE_REQUIRE(ptr && ind && val && nnz >= 0, UFE_ERR_INVALID, "null CSR array");
     std::vector<int32_t> hp(m + 1), hi((size_t)nnz);
+    std::vector<double> val_int;
     for (int32_t i = 0; i <= m; ++i) hp[i] = ptr[i] - index_base;
     UFE_REQUIRE(hp[0] == 0 && hp[m] == nnz, UFE_ERR_INVALID, "CSR ptr does not span nnz");
     for (int32_t i = 0; i < m; ++i) UFE_REQUIRE(hp[i] <= hp[i + 1], UFE_ERR_INVALID, "CSR ptr not monotone");
@@ -265,6 +258,14 @@ extern "C" int32_t ufe_mesh_set_operator(ufe_ctx *ctx, int32_t op, int32_t m, in
     UFE_CUDA(cudaStreamSynchronize(ctx->stream));
     free_work(ctx);
     cudaStream_t s = ctx->stream;
+    {
+      std::vector<int32_t> ip, ii;
+      std::vector<double> iv;
+      csr_to_internal(ctx, op, hp, hi, val, ip, ii, iv);
+      hp.swap(ip);
+      hi.swap(ii);
+      val_int.swap(iv);
+    }
     DevCSR A;
     A.m = m; A.n = n; A.nnz = nnz;
     // share the pattern with a family member that has the same ptr/ind
@@ -286,7 +287,7 @@ extern "C" int32_t ufe_mesh_set_operator(ufe_ctx *ctx, int32_t op, int32_t m, in
       ctx->op_allocs.push_back(A.ptr);
       ctx->op_allocs.push_back(A.ind);
     }
-    A.val = upload(val, nnz ? (size_t)nnz : 1, s);
+    A.val = upload(val_int.data(), nnz ? (size_t)nnz : 1, s);
     ctx->op_allocs.push_back(A.val);
     UFE_CUDA(cudaStreamSynchronize(s));
     ctx->ops[op] = A;
@@ -315,10 +316,13 @@ extern "C" int32_t ufe_operator_export(ufe_ctx *ctx, int32_t op, int32_t *ptr, i
     const DevCSR &A = ctx->ops[op];
     UFE_CUDA(cudaSetDevice(ctx->device));
     cudaStream_t s = ctx->stream;
-    if (ptr) UFE_CUDA(cudaMemcpyAsync(ptr, A.ptr, sizeof(int32_t) * (A.m + 1), cudaMemcpyDeviceToHost, s));
-    if (ind) UFE_CUDA(cudaMemcpyAsync(ind, A.ind, sizeof(int32_t) * A.nnz, cudaMemcpyDeviceToHost, s));
-    if (val) UFE_CUDA(cudaMemcpyAsync(val, A.val, sizeof(double) * A.nnz, cudaMemcpyDeviceToHost, s));
+    std::vector<int32_t> ip(A.m + 1), ii(A.nnz);
+    std::vector<double> iv(A.nnz);
+    UFE_CUDA(cudaMemcpyAsync(ip.data(), A.ptr, sizeof(int32_t) * (A.m + 1), cudaMemcpyDeviceToHost, s));
+    UFE_CUDA(cudaMemcpyAsync(ii.data(), A.ind, sizeof(int32_t) * A.nnz, cudaMemcpyDeviceToHost, s));
+    UFE_CUDA(cudaMemcpyAsync(iv.data(), A.val, sizeof(double) * A.nnz, cudaMemcpyDeviceToHost, s));
     UFE_CUDA(cudaStreamSynchronize(s));
+    csr_to_external(ctx, op, ip, ii, iv, ptr, ind, val);
     if (index_base) {
       if (ptr) for (int32_t i = 0; i <= A.m; ++i) ptr[i] += 1;
       if (ind) for (int64_t k = 0; k < A.nnz; ++k) ind[k] += 1;
@@ -335,11 +339,15 @@ extern "C" int32_t ufe_apply_operator(ufe_ctx *ctx, int32_t op, const double *x,
     const DevCSR &A = ctx->ops[op];
     UFE_CUDA(cudaSetDevice(ctx->device));
     cudaStream_t s = ctx->stream;
-    double *dx = upload(x, (size_t)A.n * ncols, s);
+    const bool rows_tri = !(op == UFE_OP_MAP_B_A || op == UFE_OP_DDX_B_A || op == UFE_OP_DDY_B_A ||
+                            op == UFE_OP_DDX_A_A || op == UFE_OP_DDY_A_A);
+    const bool cols_tri = !(op == UFE_OP_MAP_A_B || op == UFE_OP_DDX_A_B || op == UFE_OP_DDY_A_B ||
+                            op == UFE_OP_DDX_A_A || op == UFE_OP_DDY_A_A);
+    double *dx = (double *)dev_alloc(sizeof(double) * (size_t)A.n * ncols);
     double *dy = (double *)dev_alloc(sizeof(double) * (size_t)A.m * ncols);
+    to_internal(ctx, dx, x, cols_tri, ncols);
     launch_csr_spmv(s, A, dx, dy, ncols);
-    UFE_CUDA(cudaMemcpyAsync(y, dy, sizeof(double) * (size_t)A.m * ncols, cudaMemcpyDeviceToHost, s));
-    UFE_CUDA(cudaStreamSynchronize(s));
+    to_external(ctx, y, dy, rows_tri, ncols);
     dev_free(dx);
     dev_free(dy);
     return UFE_OK;

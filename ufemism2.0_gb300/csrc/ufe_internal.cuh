@@ -91,6 +91,10 @@ struct ufe_ctx {
   int32_t *Tri = nullptr, *TriC = nullptr, *TriBI = nullptr;
   std::vector<double> zeta_host;
 
+  // internal order: internal vertex/triangle i is the caller's perm[i] (ufe_layout.cu)
+  std::vector<int32_t> perm_v_h, iperm_v_h, perm_t_h, iperm_t_h;
+  int32_t *perm_v = nullptr, *iperm_v = nullptr, *perm_t = nullptr, *iperm_t = nullptr;
+
   DevCSR ops[UFE_OP_COUNT];
   bool op_set[UFE_OP_COUNT] = {};
   std::vector<void *> op_allocs;   // device allocations owned by the operators
@@ -128,6 +132,19 @@ int32_t pick_blocks(int64_t items, int threads, int max_blocks);
 
 // ufe_operators.cu
 void build_operators_gpu(ufe_ctx *ctx);
+
+// ufe_layout.cu: internal (Z-order) numbering and the mappings at the ABI boundary
+void layout_upload_mesh(ufe_ctx *ctx, const ufe_mesh_desc *m);
+void free_layout(ufe_ctx *ctx);
+void to_internal(ufe_ctx *ctx, double *d_dst, const double *h_src, bool tri, int ncols);
+void to_internal_i32(ufe_ctx *ctx, int32_t *d_dst, const int32_t *h_src, bool tri);
+void to_external(ufe_ctx *ctx, double *h_dst, const double *d_src, bool tri, int ncols);
+void pair_to_internal(ufe_ctx *ctx, double2 *d_dst, const double *h_a, const double *h_b);
+void pair_to_external(ufe_ctx *ctx, double *h_a, double *h_b, const double2 *d_src);
+void csr_to_internal(ufe_ctx *ctx, int op, const std::vector<int32_t> &ptr, const std::vector<int32_t> &ind,
+                     const double *val, std::vector<int32_t> &iptr, std::vector<int32_t> &iind, std::vector<double> &ival);
+void csr_to_external(ufe_ctx *ctx, int op, const std::vector<int32_t> &iptr, const std::vector<int32_t> &iind,
+                     const std::vector<double> &ival, int32_t *ptr, int32_t *ind, double *val);
 
 // ufe_spmv.cu
 void launch_csr_spmv(cudaStream_t s, const DevCSR &A, const double *x, double *y, int32_t ncols);

@@ -713,7 +713,7 @@ __device__ int bc_choice_dev(const PhysParams &q, int tbi, int uvc) {
 }
 
 __global__ void k_export_len(int nTri, const int32_t *m2_ptr, const int32_t *TriBI, const int32_t *TriC,
-                             const int32_t *bc_mask, PhysParams q, int32_t *rowlen) {
+                             const int32_t *bc_mask, PhysParams q, const int32_t *perm_t, int32_t *rowlen) {
   int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < nTri; t += stride) {
     int len_free = 2 * (m2_ptr[t + 1] - m2_ptr[t]);
@@ -728,14 +728,14 @@ __global__ void k_export_len(int nTri, const int32_t *m2_ptr, const int32_t *Tri
           len = nnb + 1;
         } else len = 1;
       } else len = len_free;
-      rowlen[2 * t + uvc] = len;
+      rowlen[2 * perm_t[t] + uvc] = len;
     }
   }
 }
 
 __global__ void k_export_fill(int nTri, const int32_t *m2_ptr, const int32_t *m2_ind, const int32_t *TriBI,
                               const int32_t *TriC, const int32_t *bc_mask, PhysParams q, const double4 *blk,
-                              const int32_t *ptr, int32_t *ind, double *val) {
+                              const int32_t *perm_t, const int32_t *ptr, int32_t *ind, double *val) {
   int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t t64 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t64 < nTri; t64 += stride) {
     const int t = (int)t64;
@@ -744,7 +744,7 @@ __global__ void k_export_fill(int nTri, const int32_t *m2_ptr, const int32_t *m2
     const int bcm = q.has_bc ? bc_mask[t] : 0;
     const double *bd = reinterpret_cast<const double *>(blk);
     for (int uvc = 0; uvc < 2; ++uvc) {
-      const int row = 2 * t + uvc;   // 0-based row of the reference's 2(ti-1)+uv
+      const int row = 2 * perm_t[t] + uvc;   // 0-based row 2(ti-1)+uv of the caller's triangle
       int p = ptr[row];
       const int comp = uvc == 0 ? 0 : 3;
       if (bcm == 1) {
@@ -756,7 +756,7 @@ __global__ void k_export_fill(int nTri, const int32_t *m2_ptr, const int32_t *m2
             int tj = TriC[(int64_t)n * nTri + t];
             if (tj == 0) continue;
             nnb++;
-            ind[p] = 2 * (tj - 1) + uvc; val[p] = 1.0; ++p;
+            ind[p] = 2 * perm_t[tj - 1] + uvc; val[p] = 1.0; ++p;
           }
           ind[p] = row; val[p] = -1.0 * (double)nnb;
         } else {
@@ -764,7 +764,7 @@ __global__ void k_export_fill(int nTri, const int32_t *m2_ptr, const int32_t *m2
         }
       } else {
         for (int k = k1; k < k2; ++k) {
-          int tj = m2_ind[k];
+          int tj = perm_t[m2_ind[k]];
           ind[p] = 2 * tj;     val[p] = bd[4 * (int64_t)k + (uvc == 0 ? 0 : 2)]; ++p;
           ind[p] = 2 * tj + 1; val[p] = bd[4 * (int64_t)k + (uvc == 0 ? 1 : 3)]; ++p;
         }
@@ -1277,9 +1277,10 @@ int32_t run_picard(ufe_ctx *ctx, const ufe_solver_params &p, bool diva, ufe_solv
 // ============================================================================================
 // entry points
 
-static void upload_opt(double *dst, const double *src, size_t n, cudaStream_t s) {
-  if (src) UFE_CUDA(cudaMemcpyAsync(dst, src, sizeof(double) * n, cudaMemcpyHostToDevice, s));
-  else UFE_CUDA(cudaMemsetAsync(dst, 0, sizeof(double) * n, s));
+// caller-ordered vertex field -> internal order (zero when absent)
+static void upload_vertex_opt(ufe_ctx *ctx, double *dst, const double *src) {
+  if (src) to_internal(ctx, dst, src, false, 1);
+  else UFE_CUDA(cudaMemsetAsync(dst, 0, sizeof(double) * ctx->nV, ctx->stream));
 }
 
 static void upload_bc(ufe_ctx *ctx, Work *w, const ufe_bc_prescribed *bc) {
@@ -1289,15 +1290,8 @@ static void upload_bc(ufe_ctx *ctx, Work *w, const ufe_bc_prescribed *bc) {
   if (bc && (bc->mask_b || bc->u_b || bc->v_b)) {
     UFE_REQUIRE(bc->mask_b && bc->u_b && bc->v_b, UFE_ERR_INVALID,
                 "need to provide prescribed u,v fields and mask");  // SSA_main.f90:147-150
-    UFE_CUDA(cudaMemcpyAsync(w->bc_mask, bc->mask_b, sizeof(int32_t) * nTri, cudaMemcpyHostToDevice, s));
-    double *tmp_u = (double *)dev_alloc(sizeof(double) * nTri), *tmp_v = (double *)dev_alloc(sizeof(double) * nTri);
-    UFE_CUDA(cudaMemcpyAsync(tmp_u, bc->u_b, sizeof(double) * nTri, cudaMemcpyHostToDevice, s));
-    UFE_CUDA(cudaMemcpyAsync(tmp_v, bc->v_b, sizeof(double) * nTri, cudaMemcpyHostToDevice, s));
-    k_interleave<<<pick_blocks(nTri, kThreads, 1024), kThreads, 0, s>>>(nTri, tmp_u, tmp_v, w->bc_uv);
-    UFE_CUDA(cudaGetLastError());
-    UFE_CUDA(cudaStreamSynchronize(s));
-    dev_free(tmp_u);
-    dev_free(tmp_v);
+    to_internal_i32(ctx, w->bc_mask, bc->mask_b, true);
+    pair_to_internal(ctx, w->bc_uv, bc->u_b, bc->v_b);
     w->has_bc = 1;
   }
 }
@@ -1310,15 +1304,15 @@ extern "C" int32_t ufe_ice_upload(ufe_ctx *ctx, const ufe_ice_state *ice, const 
     Work *w = ensure_work(ctx);
     cudaStream_t s = ctx->stream;
     const size_t nV = ctx->nV, nTri = ctx->nTri, nz = ctx->nz;
-    UFE_CUDA(cudaMemcpyAsync(w->Hi, ice->Hi, sizeof(double) * nV, cudaMemcpyHostToDevice, s));
-    UFE_CUDA(cudaMemcpyAsync(w->Hs, ice->Hs, sizeof(double) * nV, cudaMemcpyHostToDevice, s));
-    UFE_CUDA(cudaMemcpyAsync(w->A_flow, ice->A_flow, sizeof(double) * nV * nz, cudaMemcpyHostToDevice, s));
-    UFE_CUDA(cudaMemcpyAsync(w->fgr_b, ice->fraction_gr_b, sizeof(double) * nTri, cudaMemcpyHostToDevice, s));
-    UFE_CUDA(cudaMemcpyAsync(w->mask_gr, ice->mask_grounded_ice, sizeof(int32_t) * nV, cudaMemcpyHostToDevice, s));
-    upload_opt(w->beta_sq, ice->beta_sq, nV, s);
-    upload_opt(w->alpha_sq, ice->alpha_sq, nV, s);
-    upload_opt(w->effp, ice->effective_pressure, nV, s);
-    upload_opt(w->tys, ice->till_yield_stress, nV, s);
+    to_internal(ctx, w->Hi, ice->Hi, false, 1);
+    to_internal(ctx, w->Hs, ice->Hs, false, 1);
+    to_internal(ctx, w->A_flow, ice->A_flow, false, (int)nz);
+    to_internal(ctx, w->fgr_b, ice->fraction_gr_b, true, 1);
+    to_internal_i32(ctx, w->mask_gr, ice->mask_grounded_ice, false);
+    upload_vertex_opt(ctx, w->beta_sq, ice->beta_sq);
+    upload_vertex_opt(ctx, w->alpha_sq, ice->alpha_sq);
+    upload_vertex_opt(ctx, w->effp, ice->effective_pressure);
+    upload_vertex_opt(ctx, w->tys, ice->till_yield_stress);
     // NaN/Inf in any input field is an error (the reference's do_check_for_NaN checks)
     {
       int *flag = w->err;
@@ -1395,29 +1389,11 @@ extern "C" int32_t ufe_solve_diva_resident(ufe_ctx *ctx, const ufe_solver_params
 }
 
 static void download_pair(ufe_ctx *ctx, const double2 *src, double *a, double *b) {
-  cudaStream_t s = ctx->stream;
-  const int n = ctx->nTri;
-  double *ta = (double *)dev_alloc(sizeof(double) * n), *tb = (double *)dev_alloc(sizeof(double) * n);
-  k_deinterleave<<<pick_blocks(n, kThreads, 1024), kThreads, 0, s>>>(n, src, ta, tb);
-  UFE_CUDA(cudaGetLastError());
-  if (a) UFE_CUDA(cudaMemcpyAsync(a, ta, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
-  if (b) UFE_CUDA(cudaMemcpyAsync(b, tb, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
-  UFE_CUDA(cudaStreamSynchronize(s));
-  dev_free(ta);
-  dev_free(tb);
+  pair_to_external(ctx, a, b, src);
 }
 
 static void upload_pair(ufe_ctx *ctx, double2 *dst, const double *a, const double *b) {
-  cudaStream_t s = ctx->stream;
-  const int n = ctx->nTri;
-  double *ta = (double *)dev_alloc(sizeof(double) * n), *tb = (double *)dev_alloc(sizeof(double) * n);
-  upload_opt(ta, a, n, s);
-  upload_opt(tb, b, n, s);
-  k_interleave<<<pick_blocks(n, kThreads, 1024), kThreads, 0, s>>>(n, ta, tb, dst);
-  UFE_CUDA(cudaGetLastError());
-  UFE_CUDA(cudaStreamSynchronize(s));
-  dev_free(ta);
-  dev_free(tb);
+  pair_to_internal(ctx, dst, a, b);
 }
 
 extern "C" int32_t ufe_solve_history(ufe_ctx *ctx, double *out, int32_t cap, int32_t *n) {
@@ -1483,13 +1459,13 @@ extern "C" int32_t ufe_solve_diva(ufe_ctx *ctx, const ufe_solver_params *p, cons
     upload_pair(ctx, w->uv, ds->u_vav_b, ds->v_vav_b);
     upload_pair(ctx, w->uv_base, ds->u_base_b, ds->v_base_b);
     upload_pair(ctx, w->tau_b, ds->tau_bx_b, ds->tau_by_b);
-    UFE_CUDA(cudaMemcpyAsync(w->eta_3D_b, ds->eta_3D_b, sizeof(double) * nTri * nz, cudaMemcpyHostToDevice, s));
+    to_internal(ctx, w->eta_3D_b, ds->eta_3D_b, true, (int)nz);
     ufe_solve_stats st;
     int32_t r = resident_solve(ctx, p, 0, true, &st);
     download_pair(ctx, w->uv, ds->u_vav_b, ds->v_vav_b);
     download_pair(ctx, w->uv_base, ds->u_base_b, ds->v_base_b);
     download_pair(ctx, w->tau_b, ds->tau_bx_b, ds->tau_by_b);
-    UFE_CUDA(cudaMemcpyAsync(ds->eta_3D_b, w->eta_3D_b, sizeof(double) * nTri * nz, cudaMemcpyDeviceToHost, s));
+    to_external(ctx, ds->eta_3D_b, w->eta_3D_b, true, (int)nz);
     if (r >= 0 && ds->u_3D_b && ds->v_3D_b) {
       if (!w->any_grounded) {
         memset(ds->u_3D_b, 0, sizeof(double) * nTri * nz);
@@ -1502,9 +1478,8 @@ extern "C" int32_t ufe_solve_diva(ufe_ctx *ctx, const ufe_solver_params *p, cons
             ctx->nV, ctx->nTri, ctx->nz, S.ab, w->F1_3D_a, w->uv_base, w->tau_b, w->bfc_b,
             p->choice_sliding_law == UFE_SLIDING_NO_SLIDING, u3, v3);
         UFE_CUDA(cudaGetLastError());
-        UFE_CUDA(cudaMemcpyAsync(ds->u_3D_b, u3, sizeof(double) * nTri * nz, cudaMemcpyDeviceToHost, s));
-        UFE_CUDA(cudaMemcpyAsync(ds->v_3D_b, v3, sizeof(double) * nTri * nz, cudaMemcpyDeviceToHost, s));
-        UFE_CUDA(cudaStreamSynchronize(s));
+        to_external(ctx, ds->u_3D_b, u3, true, (int)nz);
+        to_external(ctx, ds->v_3D_b, v3, true, (int)nz);
         dev_free(u3);
         dev_free(v3);
       }
@@ -1525,10 +1500,11 @@ static void upload_linearised_inputs(ufe_ctx *ctx, Work *w, const double *N_b, c
               "linearised-solve input missing");
   cudaStream_t s = ctx->stream;
   const size_t n = ctx->nTri;
-  UFE_CUDA(cudaMemcpyAsync(w->N_b_in, N_b, sizeof(double) * n, cudaMemcpyHostToDevice, s));
-  UFE_CUDA(cudaMemcpyAsync(w->dNx_b_in, dN_dx_b, sizeof(double) * n, cudaMemcpyHostToDevice, s));
-  UFE_CUDA(cudaMemcpyAsync(w->dNy_b_in, dN_dy_b, sizeof(double) * n, cudaMemcpyHostToDevice, s));
-  UFE_CUDA(cudaMemcpyAsync(w->beta_b_in, beta_b, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+  (void)s; (void)n;
+  to_internal(ctx, w->N_b_in, N_b, true, 1);
+  to_internal(ctx, w->dNx_b_in, dN_dx_b, true, 1);
+  to_internal(ctx, w->dNy_b_in, dN_dy_b, true, 1);
+  to_internal(ctx, w->beta_b_in, beta_b, true, 1);
   upload_pair(ctx, w->tau_d, tau_dx_b, tau_dy_b);
   upload_bc(ctx, w, bc);
 }
@@ -1555,7 +1531,8 @@ extern "C" int32_t ufe_assemble_linearised(ufe_ctx *ctx, const ufe_solver_params
     int32_t *dptr = (int32_t *)dev_alloc(sizeof(int32_t) * (nrow + 1));
     UFE_CUDA(cudaMemsetAsync(rowlen, 0, sizeof(int32_t) * (nrow + 1), s));
     const DevCSR &m2 = ctx->ops[UFE_OP_M2_DDX_B_B];
-    k_export_len<<<S.eblocks(nTri), kThreads, 0, s>>>(nTri, m2.ptr, ctx->TriBI, ctx->TriC, w->bc_mask, S.q, rowlen);
+    k_export_len<<<S.eblocks(nTri), kThreads, 0, s>>>(nTri, m2.ptr, ctx->TriBI, ctx->TriC, w->bc_mask, S.q,
+                                                       ctx->perm_t, rowlen);
     UFE_CUDA(cudaGetLastError());
     std::vector<int32_t> hl(nrow + 1);
     UFE_CUDA(cudaMemcpyAsync(hl.data(), rowlen, sizeof(int32_t) * (nrow + 1), cudaMemcpyDeviceToHost, s));
@@ -1572,12 +1549,16 @@ extern "C" int32_t ufe_assemble_linearised(ufe_ctx *ctx, const ufe_solver_params
       int32_t *dind = (int32_t *)dev_alloc(sizeof(int32_t) * (nnz ? nnz : 1));
       double *dval = (double *)dev_alloc(sizeof(double) * (nnz ? nnz : 1));
       k_export_fill<<<S.eblocks(nTri), kThreads, 0, s>>>(nTri, m2.ptr, m2.ind, ctx->TriBI, ctx->TriC, w->bc_mask,
-                                                         S.q, w->blk, dptr, dind, dval);
+                                                         S.q, w->blk, ctx->perm_t, dptr, dind, dval);
       UFE_CUDA(cudaGetLastError());
       UFE_CUDA(cudaMemcpyAsync(ind, dind, sizeof(int32_t) * nnz, cudaMemcpyDeviceToHost, s));
       UFE_CUDA(cudaMemcpyAsync(val, dval, sizeof(double) * nnz, cudaMemcpyDeviceToHost, s));
-      UFE_CUDA(cudaMemcpyAsync(bb, w->kv.B, sizeof(double) * nrow, cudaMemcpyDeviceToHost, s));
       UFE_CUDA(cudaStreamSynchronize(s));
+      {
+        std::vector<double> bu(nTri), bv(nTri);
+        pair_to_external(ctx, bu.data(), bv.data(), w->kv.B);
+        for (int t = 0; t < nTri; ++t) { bb[2 * t] = bu[t]; bb[2 * t + 1] = bv[t]; }
+      }
       dev_free(dind);
       dev_free(dval);
       for (int i = 0; i <= nrow; ++i) ptr[i] = hp[i] + 1;
