@@ -23,10 +23,10 @@ template <> struct ScalarOf<float2> { using T = float; };
 template <> struct ScalarOf<double2> { using T = double; };
 
 // ---- vector element helpers ---------------------------------------------------------------
-__device__ __forceinline__ double v_dot(double2 a, double2 b) { return a.x * b.x + a.y * b.y; }
-__device__ __forceinline__ double v_dot(float2 a, float2 b) {
-  return (double)a.x * (double)b.x + (double)a.y * (double)b.y;
-}
+// The Krylov arithmetic uses explicit fused multiply-adds: FP64 instructions are the scarce
+// resource on GB300, and these sums need no bitwise agreement with the reference.
+__device__ __forceinline__ double v_dot(double2 a, double2 b) { return fma(a.y, b.y, a.x * b.x); }
+__device__ __forceinline__ double v_dot(float2 a, float2 b) { return (double)fmaf(a.y, b.y, a.x * b.x); }
 __device__ __forceinline__ double v_dot(double a, double b) { return a * b; }
 __device__ __forceinline__ double2 v_mul(double2 d, double2 y) { return make_double2(d.x * y.x, d.y * y.y); }
 __device__ __forceinline__ float2 v_mul(float2 d, float2 y) { return make_float2(d.x * y.x, d.y * y.y); }
@@ -37,31 +37,31 @@ template <> __device__ __forceinline__ float2 v_zero<float2>() { return make_flo
 template <> __device__ __forceinline__ double v_zero<double>() { return 0.0; }
 // p_new = r - (beta*omega)*v + beta*p   (PETSc VecAXPBYPCZ(P, 1, -beta*omega, beta, R, V))
 __device__ __forceinline__ double2 v_pupd(double2 r, double bw, double2 v, double beta, double2 p) {
-  return make_double2(r.x - bw * v.x + beta * p.x, r.y - bw * v.y + beta * p.y);
+  return make_double2(fma(beta, p.x, fma(-bw, v.x, r.x)), fma(beta, p.y, fma(-bw, v.y, r.y)));
 }
 __device__ __forceinline__ float2 v_pupd(float2 r, float bw, float2 v, float beta, float2 p) {
-  return make_float2(r.x - bw * v.x + beta * p.x, r.y - bw * v.y + beta * p.y);
+  return make_float2(fmaf(beta, p.x, fmaf(-bw, v.x, r.x)), fmaf(beta, p.y, fmaf(-bw, v.y, r.y)));
 }
 __device__ __forceinline__ double v_pupd(double r, double bw, double v, double beta, double p) {
-  return r - bw * v + beta * p;
+  return fma(beta, p, fma(-bw, v, r));
 }
 // r - a*v
 __device__ __forceinline__ double2 v_sub_scaled(double2 r, double a, double2 v) {
-  return make_double2(r.x - a * v.x, r.y - a * v.y);
+  return make_double2(fma(-a, v.x, r.x), fma(-a, v.y, r.y));
 }
 __device__ __forceinline__ float2 v_sub_scaled(float2 r, float a, float2 v) {
-  return make_float2(r.x - a * v.x, r.y - a * v.y);
+  return make_float2(fmaf(-a, v.x, r.x), fmaf(-a, v.y, r.y));
 }
-__device__ __forceinline__ double v_sub_scaled(double r, double a, double v) { return r - a * v; }
+__device__ __forceinline__ double v_sub_scaled(double r, double a, double v) { return fma(-a, v, r); }
 // x + a*p + w*s
 __device__ __forceinline__ double2 v_xupd(double2 x, double a, double2 p, double w, double2 s) {
-  return make_double2(x.x + a * p.x + w * s.x, x.y + a * p.y + w * s.y);
+  return make_double2(fma(w, s.x, fma(a, p.x, x.x)), fma(w, s.y, fma(a, p.y, x.y)));
 }
 __device__ __forceinline__ float2 v_xupd(float2 x, float a, float2 p, float w, float2 s) {
-  return make_float2(x.x + a * p.x + w * s.x, x.y + a * p.y + w * s.y);
+  return make_float2(fmaf(w, s.x, fmaf(a, p.x, x.x)), fmaf(w, s.y, fmaf(a, p.y, x.y)));
 }
 __device__ __forceinline__ double v_xupd(double x, double a, double p, double w, double s) {
-  return x + a * p + w * s;
+  return fma(w, s, fma(a, p, x));
 }
 __device__ __forceinline__ double2 v_shfl_xor(double2 a, int o) {
   return make_double2(__shfl_xor_sync(0xffffffffu, a.x, o), __shfl_xor_sync(0xffffffffu, a.y, o));
@@ -93,8 +93,8 @@ struct BsrMat {
     for (int k = __ldg(ptr + i) + lane; k < k2; k += L) {
       Blk a = blk[k];
       Vec x = get(__ldg(col + k));
-      y.x += a.x * x.x + a.y * x.y;
-      y.y += a.z * x.x + a.w * x.y;
+      y.x = fma(a.y, x.y, fma(a.x, x.x, y.x));
+      y.y = fma(a.w, x.y, fma(a.z, x.x, y.y));
     }
     return y;
   }
@@ -112,7 +112,7 @@ struct CsrMat {
   __device__ __forceinline__ double row_partial(int i, int lane, G get) const {
     double y = 0.0;
     int k2 = __ldg(ptr + i + 1);
-    for (int k = __ldg(ptr + i); k < k2; ++k) y += __ldg(val + k) * get(__ldg(col + k));
+    for (int k = __ldg(ptr + i); k < k2; ++k) y = fma(__ldg(val + k), get(__ldg(col + k)), y);
     return y;
   }
 };

@@ -281,6 +281,7 @@ struct AssembleArgs {
   double4 *blk;
   float4 *blk32;
   double2 *rhs, *dinv, *X, *R, *RP, *P0, *V0;
+  float2 *dinv32;
   double *beta_b_out, *bfc_b, *F2b1, *eta_3D_b;
   int *err;
   // Krylov
@@ -410,6 +411,7 @@ __global__ void k_assemble(AssembleArgs a, PhysParams q, CondArg cond) {
         double4 b = a.blk[k];
         a.blk32[k] = make_float4((float)b.x, (float)b.y, (float)b.z, (float)b.w);
       }
+      a.dinv32[t] = make_float2((float)di.x, (float)di.y);
     }
     // -- Krylov initial residual r = D^-1 (b - A x0)
     double2 ax = make_double2(0.0, 0.0);
@@ -463,24 +465,26 @@ __global__ void k_assemble(AssembleArgs a, PhysParams q, CondArg cond) {
   }
 }
 
-// ---- FP32-matrix inner solve with FP64 refinement ---------------------------------------------
-// The inner BiCGStab applies the FP32 copy of the stiffness blocks (FP64 vectors and sums) to
-// the correction system (D^-1 A32) d = r, with r the FP64 residual; the outer loop adds d to x
-// and recomputes r in FP64 with the FP64 blocks until the FP64 test passes.
-__global__ void k_inner_init(int nTri, const double2 *R, double2 *Rin, double2 *RPin, double2 *Xin,
-                             double2 *P0, double2 *V0, const KrylovScalars *outer, KrylovScalars *ksi,
+// ---- FP32 inner solve with FP64 refinement ---------------------------------------------------
+// The inner BiCGStab runs entirely in FP32 (blocks, vectors, Jacobi scaling; dot products summed
+// in FP64) on the correction system (D^-1 A) d = r, r the FP64 residual; the outer loop adds d to
+// x and recomputes r in FP64 with the FP64 blocks until the FP64 test passes.  FP64 instructions
+// are scarce on GB300, FP32 ones are not.
+__global__ void k_inner_init(int nTri, const double2 *R, float2 *R32, float2 *RP32, float2 *x32,
+                             float2 *P32, float2 *V32, const KrylovScalars *outer, KrylovScalars *ksi,
                              double inner_rtol, int max_it, double *partials, unsigned int *tickets,
                              CondArg cond) {
   double acc[1] = {0.0};
   int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < nTri; t += stride) {
     double2 r = R[t];
-    Rin[t] = r;
-    RPin[t] = r;
-    Xin[t] = make_double2(0.0, 0.0);
-    P0[t] = make_double2(0.0, 0.0);
-    V0[t] = make_double2(0.0, 0.0);
-    acc[0] += r.x * r.x + r.y * r.y;
+    float2 r32 = make_float2((float)r.x, (float)r.y);
+    R32[t] = r32;
+    RP32[t] = r32;
+    x32[t] = make_float2(0.f, 0.f);
+    P32[t] = make_float2(0.f, 0.f);
+    V32[t] = make_float2(0.f, 0.f);
+    acc[0] += (double)r32.x * r32.x + (double)r32.y * r32.y;
   }
   double tot[1];
   if (grid_sum<1>(acc, partials, tickets + kSiteInner, tot)) {
@@ -497,19 +501,20 @@ __global__ void k_inner_init(int nTri, const double2 *R, double2 *Rin, double2 *
     s.rho = tot[0];
     s.rhoold = s.alpha = s.omegaold = s.omega = 1.0;
     s.beta = s.rho;
-    s.active = (dp > s.ttol && s.rho != 0.0) ? 1 : 0;
+    s.active = (dp > s.ttol && s.rho != 0.0 && isfinite(dp)) ? 1 : 0;
     *ksi = s;
     set_cond(cond, s.active);
   }
 }
 
-// x += d, unless the inner solve failed (then x is left as it was)
-__global__ void k_xadd(int nTri, double2 *X, const double2 *Xin, const KrylovScalars *ksi) {
+// x += d in FP64, unless the inner solve failed or its correction is not finite
+__global__ void k_xadd(int nTri, double2 *X, const float2 *x32, const KrylovScalars *ksi) {
   if (ksi->status < 0) return;
   int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < nTri; t += stride) {
-    double2 x = X[t], d = Xin[t];
-    X[t] = make_double2(x.x + d.x, x.y + d.y);
+    double2 x = X[t];
+    float2 d = x32[t];
+    if (isfinite(d.x) && isfinite(d.y)) X[t] = make_double2(x.x + (double)d.x, x.y + (double)d.y);
   }
 }
 
@@ -810,8 +815,8 @@ Work *ensure_work(ufe_ctx *ctx) {
   KrylovVecs &k = w->kv;
   double2 **d2[] = {&k.X, &k.R, &k.RP, &k.S, &k.T, &k.dinv, &k.B, &k.P[0], &k.P[1], &k.V[0], &k.V[1]};
   for (auto p : d2) *p = alloc_n<double2>(nTri);
-  k.Xin = alloc_n<double2>(nTri);
-  k.Rin = alloc_n<double2>(nTri);
+  float2 **f2[] = {&k.x32, &k.R32, &k.RP32, &k.S32, &k.T32, &k.dinv32, &k.P32[0], &k.P32[1], &k.V32[0], &k.V32[1]};
+  for (auto p : f2) *p = alloc_n<float2>(nTri);
   w->uv = alloc_n<double2>(nTri);
   w->tau_d = alloc_n<double2>(nTri);
   w->fgr_b = alloc_n<double>(nTri);
@@ -865,7 +870,9 @@ void free_work(ufe_ctx *ctx) {
   if (w->graph_ssa) cudaGraphExecDestroy(w->graph_ssa);
   if (w->graph_diva) cudaGraphExecDestroy(w->graph_diva);
   void *ptrs[] = {w->blk, w->blk32, w->kv.X, w->kv.R, w->kv.RP, w->kv.S, w->kv.T, w->kv.dinv, w->kv.B,
-                  w->kv.P[0], w->kv.P[1], w->kv.V[0], w->kv.V[1], w->kv.Xin, w->kv.Rin, w->uv, w->tau_d, w->fgr_b, w->bc_mask, w->bc_uv, w->uv_base, w->tau_b,
+                  w->kv.P[0], w->kv.P[1], w->kv.V[0], w->kv.V[1], w->kv.x32, w->kv.R32, w->kv.RP32,
+                  w->kv.S32, w->kv.T32, w->kv.dinv32, w->kv.P32[0], w->kv.P32[1], w->kv.V32[0],
+                  w->kv.V32[1], w->uv, w->tau_d, w->fgr_b, w->bc_mask, w->bc_uv, w->uv_base, w->tau_b,
                   w->eta_3D_b, w->bfc_b, w->F2b1, w->beta_b, w->Hi, w->Hs, w->Avav, w->A_flow, w->beta_sq,
                   w->alpha_sq, w->effp, w->tys, w->mask_gr, w->N_a, w->beta_a, w->beta_eff_a, w->F2a1,
                   w->eta_3D_a, w->F1_3D_a, w->N_b_in, w->dNx_b_in, w->dNy_b_in, w->beta_b_in, w->ks,
@@ -881,8 +888,8 @@ int32_t bsr_lanes(ufe_ctx *ctx) {
   static int lanes = -1;
   if (lanes < 0) {
     const char *e = getenv("UFE_BSR_LANES");
-    int v = e ? atoi(e) : 4;
-    lanes = (v == 1 || v == 2 || v == 4 || v == 8) ? v : 4;
+    int v = e ? atoi(e) : 1;
+    lanes = (v == 1 || v == 2 || v == 4 || v == 8) ? v : 1;
   }
   (void)ctx;
   return lanes;
@@ -936,7 +943,7 @@ struct Solver {
     a.blk = w->blk;
     a.blk32 = (p.precision == UFE_PREC_FP32_REFINE) ? w->blk32 : nullptr;
     a.rhs = w->kv.B; a.dinv = w->kv.dinv; a.X = w->kv.X; a.R = w->kv.R; a.RP = w->kv.RP;
-    a.P0 = w->kv.P[0]; a.V0 = w->kv.V[0];
+    a.P0 = w->kv.P[0]; a.V0 = w->kv.V[0]; a.dinv32 = w->kv.dinv32;
     a.beta_b_out = w->beta_b; a.bfc_b = w->bfc_b; a.F2b1 = w->F2b1; a.eta_3D_b = w->eta_3D_b;
     a.err = w->err;
     a.ks = w->ks;
@@ -973,9 +980,9 @@ struct Solver {
     return BsrMat<double, double, L>{w->nTri, m2.ptr, m2.ind, w->blk};
   }
   template <int L>
-  BsrMat<float, double, L> mat32() const {
+  BsrMat<float, float, L> mat32() const {
     const DevCSR &m2 = ctx->ops[UFE_OP_M2_DDX_B_B];
-    return BsrMat<float, double, L>{w->nTri, m2.ptr, m2.ind, w->blk32};
+    return BsrMat<float, float, L>{w->nTri, m2.ptr, m2.ind, w->blk32};
   }
   KV<double2> kv64() const {
     KV<double2> v;
@@ -984,12 +991,11 @@ struct Solver {
     v.P[0] = w->kv.P[0]; v.P[1] = w->kv.P[1]; v.V[0] = w->kv.V[0]; v.V[1] = w->kv.V[1];
     return v;
   }
-  // inner (correction) solve: own x and r, the outer's other work vectors
-  KV<double2> kv_inner() const {
-    KV<double2> v;
-    v.X = w->kv.Xin; v.R = w->kv.Rin; v.RP = w->kv.RP; v.S = w->kv.S; v.T = w->kv.T; v.B = nullptr;
-    v.dinv = w->kv.dinv;
-    v.P[0] = w->kv.P[0]; v.P[1] = w->kv.P[1]; v.V[0] = w->kv.V[0]; v.V[1] = w->kv.V[1];
+  KV<float2> kv_inner() const {
+    KV<float2> v;
+    v.X = w->kv.x32; v.R = w->kv.R32; v.RP = w->kv.RP32; v.S = w->kv.S32; v.T = w->kv.T32; v.B = nullptr;
+    v.dinv = w->kv.dinv32;
+    v.P[0] = w->kv.P32[0]; v.P[1] = w->kv.P32[1]; v.V[0] = w->kv.V32[0]; v.V[1] = w->kv.V32[1];
     return v;
   }
   void krylov_iter64(CondArg c) {
@@ -1010,7 +1016,7 @@ struct Solver {
   }
   void enqueue_inner_init(CondArg c) {
     k_inner_init<<<eblocks(w->nTri), kThreads, 0, s>>>(
-        w->nTri, w->kv.R, w->kv.Rin, w->kv.RP, w->kv.Xin, w->kv.P[0], w->kv.V[0], w->ks, w->ks + 1,
+        w->nTri, w->kv.R, w->kv.R32, w->kv.RP32, w->kv.x32, w->kv.P32[0], w->kv.V32[0], w->ks, w->ks + 1,
         p.krylov_inner_rtol, p.krylov_max_it, ctx->red.partials, ctx->red.tickets, c);
     UFE_CUDA(cudaGetLastError());
   }
@@ -1021,7 +1027,7 @@ struct Solver {
         m, w->kv.X, w->kv.B, w->kv.dinv, w->kv.R, w->ks, w->ks + 1, ctx->red.partials, ctx->red.tickets, c);
   }
   void enqueue_refine_update(CondArg c) {
-    k_xadd<<<eblocks(w->nTri), kThreads, 0, s>>>(w->nTri, w->kv.X, w->kv.Xin, w->ks + 1);
+    k_xadd<<<eblocks(w->nTri), kThreads, 0, s>>>(w->nTri, w->kv.X, w->kv.x32, w->ks + 1);
     switch (lanes) {
       case 1: residual64_l<1>(c); break;
       case 2: residual64_l<2>(c); break;

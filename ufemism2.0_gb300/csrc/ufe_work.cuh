@@ -80,8 +80,9 @@ struct BsrView {
 struct KrylovVecs {
   double2 *X, *R, *RP, *S, *T, *dinv, *B;
   double2 *P[2], *V[2];
-  // inner (correction) solve of the FP32-matrix path
-  double2 *Xin, *Rin;
+  // inner (correction) solve of the mixed path: FP32 vectors
+  float2 *x32, *R32, *RP32, *S32, *T32, *dinv32;
+  float2 *P32[2], *V32[2];
 };
 
 struct Work {
