@@ -125,7 +125,8 @@ typedef struct {
   int32_t krylov_max_it;                  /* default 10000 (PETSc's default max_it)          */
   int32_t krylov_initial_guess;           /* enum ufe_initial_guess, default UFE_X0_CURRENT  */
   int32_t precision;                      /* enum ufe_precision, default UFE_PREC_FP64       */
-  double  krylov_inner_rtol;              /* FP32 inner-solve reduction per refinement step, default 1e-4 */
+  double  krylov_inner_rtol;              /* FP32 inner-solve reduction per refinement step, default 1e-2;
+                                             the linear solve finishes in FP64 if the FP32 steps fail */
   int32_t reserved[8];
 } ufe_solver_params;
 

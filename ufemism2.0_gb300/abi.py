@@ -112,7 +112,7 @@ def default_params(**overrides) -> SolverParams:
     p.krylov_max_it = 10000
     p.krylov_initial_guess = X0_CURRENT
     p.precision = PREC_FP64
-    p.krylov_inner_rtol = 1e-4
+    p.krylov_inner_rtol = 1e-2
     for k, v in overrides.items():
         if k == "choice_sliding_law" and isinstance(v, str):
             v = SLIDING[v]

@@ -84,7 +84,7 @@ extern "C" void ufe_default_params(ufe_solver_params *p) {
   p->krylov_max_it = 10000;
   p->krylov_initial_guess = UFE_X0_CURRENT;
   p->precision = UFE_PREC_FP64;
-  p->krylov_inner_rtol = 1e-4;
+  p->krylov_inner_rtol = 1e-2;
 }
 
 extern "C" int32_t ufe_ctx_create(int32_t device, ufe_ctx **out) {

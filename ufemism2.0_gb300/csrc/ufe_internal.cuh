@@ -51,7 +51,9 @@ struct KrylovScalars {
   int32_t max_it;
   int32_t refinements; // FP64 refinement steps of the current Picard iteration
   int32_t tbreak;      // t = 0 in the last iteration: x + alpha p is the final update
-  int32_t pad;
+  int32_t pad;         // failed inner solves of the current refinement loop
+  int32_t fallback;    // the FP32 refinement loop gave up: finish in FP64
+  int32_t pad2;
 };
 
 constexpr int kHistMax = 128;   // Picard iterations recorded per solve

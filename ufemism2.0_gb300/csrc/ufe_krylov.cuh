@@ -155,11 +155,16 @@ __device__ __forceinline__ Vec lane_reduce(Vec y) {
 
 // r = D^-1 (b - A x), r^ = r, p = v = 0; tests the initial residual (KSPConvergedDefault at
 // iteration 0) and primes rho = (r, r^).
+// With gate = 1 the kernel only runs when the scalars ask for an FP64 fallback solve.
 template <class M>
 __global__ void k_krylov_init(M mat, KV<typename M::Vec> v, KrylovScalars *ks, double rtol,
                               double abstol, int max_it, int x_is_zero, double *partials,
-                              unsigned int *tickets, CondArg cond) {
+                              unsigned int *tickets, CondArg cond, int gate = 0) {
   using Vec = typename M::Vec;
+  if (gate && !ks->fallback) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) set_cond(cond, 0);
+    return;
+  }
   double acc[2] = {0.0, 0.0};
   KRYLOV_ROWS(M, i, lane) {
     const int i = (int)i_64;
@@ -189,8 +194,11 @@ __global__ void k_krylov_init(M mat, KV<typename M::Vec> v, KrylovScalars *ks, d
     double rnorm0 = bnorm != 0.0 ? bnorm : dp;
     KrylovScalars s = *ks;
     s.dp = dp;
-    s.rnorm0 = rnorm0;
-    s.ttol = fmax(rtol * rnorm0, abstol);
+    if (!gate) {
+      s.rnorm0 = rnorm0;
+      s.ttol = fmax(rtol * rnorm0, abstol);   // a fallback keeps the outer solve's tolerance
+    }
+    s.fallback = 0;
     s.it = 0;
     s.max_it = max_it;
     s.rho = tot[0];

@@ -456,6 +456,7 @@ __global__ void k_assemble(AssembleArgs a, PhysParams q, CondArg cond) {
     s.tbreak = 0;
     s.refinements = 0;
     s.pad = 0;
+    s.fallback = 0;
     s.active = 1;
     if (isnan(dp)) { s.status = UFE_ERR_NAN; s.active = 0; }
     else if (dp <= s.ttol) s.active = 0;
@@ -547,9 +548,11 @@ __global__ void k_residual64(BsrMat<double, double, L> mat, const double2 *X, co
     s.it += in.it;
     if (in.status < 0) s.pad += 1;   // a failed inner solve added nothing; count it
     if (isnan(dp)) { s.status = UFE_ERR_NAN; s.active = 0; }
-    else if (s.pad >= 3) { s.status = UFE_ERR_DIVERGED; s.active = 0; }
     else if (dp <= s.ttol) s.active = 0;
-    else if (s.refinements >= kMaxRefine || s.it >= s.max_it) { s.status = UFE_WARN_KRYLOV_MAXIT; s.active = 0; }
+    else if (s.pad >= 2 || s.refinements >= kMaxRefine || s.it >= s.max_it) {
+      s.active = 0;
+      s.fallback = 1;   // finish this linear solve with FP64 BiCGStab from the current x
+    }
     *ks = s;
     set_cond(cond, s.active);
   }
@@ -565,7 +568,7 @@ __device__ void picard_step(PicardScalars *psp, KrylovScalars *ks, double r1, do
   const KrylovScalars kin = ks[1];
   p.it += 1;
   p.n_refine += k.refinements;
-  const int total = (k.refinements > 0) ? kin.total_its : k.total_its;
+  const int total = kin.total_its + k.total_its;
   if (p.it <= kHistMax) {
     double *h = p.hist + (p.it - 1) * kHistCols;
     h[0] = 2.0 * r1 / fmax(r2, 1e-8);
@@ -1037,6 +1040,23 @@ struct Solver {
     UFE_CUDA(cudaGetLastError());
   }
 
+  template <int L>
+  void fallback_init_l(CondArg c) {
+    BsrMat<double, double, L> m = mat64<L>();
+    k_krylov_init<BsrMat<double, double, L>><<<krylov_grid(m, kThreads, grid), kThreads, 0, s>>>(
+        m, kv64(), w->ks, p.stress_balance_PETSc_rtol, p.stress_balance_PETSc_abstol, p.krylov_max_it, 0,
+        ctx->red.partials, ctx->red.tickets, c, 1);
+  }
+  void enqueue_fallback_init(CondArg c) {
+    switch (lanes) {
+      case 1: fallback_init_l<1>(c); break;
+      case 2: fallback_init_l<2>(c); break;
+      case 8: fallback_init_l<8>(c); break;
+      default: fallback_init_l<4>(c); break;
+    }
+    UFE_CUDA(cudaGetLastError());
+  }
+
   void enqueue_prologue(bool diva) {
     k_prologue<<<eblocks(std::max(w->nV, w->nTri)), kThreads, 0, s>>>(
         w->nV, w->nTri, w->nz, ab, w->Hi, w->Hs, w->A_flow, ctx->zeta, w->tau_d, diva ? nullptr : w->Avav,
@@ -1144,6 +1164,14 @@ cudaGraphExec_t build_picard_graph(Solver &S, bool diva) {
       cudaGraphNode_t wi = add_while(kbody, ii, h_in32, &ibody);
       capture_into(S.s, ibody, {}, [&] { S.krylov_iter32(in32); });
       capture_into(S.s, kbody, {wi}, [&] { S.enqueue_refine_update(inner); });
+      // FP64 fallback when the refinement loop gave up
+      cudaGraphConditionalHandle h_fb;
+      UFE_CUDA(cudaGraphConditionalHandleCreate(&h_fb, body, 0, 0));
+      CondArg fb{h_fb, 1};
+      auto fi = capture_into(S.s, body, {wk}, [&] { S.enqueue_fallback_init(fb); });
+      cudaGraph_t fbody;
+      wk = add_while(body, fi, h_fb, &fbody);
+      capture_into(S.s, fbody, {}, [&] { S.krylov_iter64(fb); });
     } else {
       capture_into(S.s, kbody, {}, [&] { S.krylov_iter64(inner); });
     }
@@ -1183,6 +1211,15 @@ void run_picard_host(Solver &S, bool diva) {
         UFE_CUDA(cudaMemcpyAsync(w->ks_host, w->ks, sizeof(KrylovScalars), cudaMemcpyDeviceToHost, S.s));
         UFE_CUDA(cudaStreamSynchronize(S.s));
         if (!w->ks_host[0].active) break;
+      }
+    }
+    if (S.p.precision == UFE_PREC_FP32_REFINE) {
+      S.enqueue_fallback_init(none);
+      for (;;) {
+        UFE_CUDA(cudaMemcpyAsync(w->ks_host, w->ks, sizeof(KrylovScalars), cudaMemcpyDeviceToHost, S.s));
+        UFE_CUDA(cudaStreamSynchronize(S.s));
+        if (!w->ks_host[0].active) break;
+        for (int c = 0; c < 8; ++c) S.krylov_iter64(none);
       }
     }
     S.enqueue_picard_post(diva, none);
@@ -1264,7 +1301,7 @@ int32_t run_picard(ufe_ctx *ctx, const ufe_solver_params &p, bool diva, ufe_solv
   float ms = 0.f;
   cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
   (void)law;
-  int32_t total_its = (p.precision == UFE_PREC_FP32_REFINE) ? w->ks_host[1].total_its : ks.total_its;
+  int32_t total_its = w->ks_host[1].total_its + ks.total_its;
   if (stats) {
     memset(stats, 0, sizeof(*stats));
     stats->n_visc_its = ps.it;
@@ -1615,12 +1652,22 @@ extern "C" int32_t ufe_solve_linearised(ufe_ctx *ctx, const ufe_solver_params *p
         if (!w->ks_host[0].active) break;
       }
     }
+    if (p->precision == UFE_PREC_FP32_REFINE) {
+      S.enqueue_fallback_init(none);
+      for (;;) {
+        UFE_CUDA(cudaMemcpyAsync(w->ks_host, w->ks, sizeof(KrylovScalars), cudaMemcpyDeviceToHost, S.s));
+        UFE_CUDA(cudaStreamSynchronize(S.s));
+        if (!w->ks_host[0].active) break;
+        for (int c = 0; c < 8; ++c) S.krylov_iter64(none);
+      }
+    }
     check_err_flag(S);
     UFE_CUDA(cudaMemcpyAsync(w->ks_host, w->ks, sizeof(KrylovScalars) * 2, cudaMemcpyDeviceToHost, S.s));
     UFE_CUDA(cudaStreamSynchronize(S.s));
     download_pair(ctx, w->kv.X, u_b, v_b);
     if (n_Axb_its)
-      *n_Axb_its = (p->precision == UFE_PREC_FP32_REFINE) ? w->ks_host[1].total_its : w->ks_host[0].it;
+      *n_Axb_its = (p->precision == UFE_PREC_FP32_REFINE) ? w->ks_host[1].total_its + w->ks_host[0].total_its
+                                                          : w->ks_host[0].it;
     return w->ks_host[0].status;
   });
 }
