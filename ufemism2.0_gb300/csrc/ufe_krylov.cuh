@@ -100,6 +100,41 @@ struct BsrMat {
   }
 };
 
+// FP32 2x2-block rows in difference form: y_i = sum_j A_ij (x_j - x_i) + S_i x_i with the row
+// sums S_i = sum_j A_ij taken in FP64 at assembly.  For the smooth vectors of an elliptic
+// operator, x_j - x_i is exact in FP32 (nearby values) and the products keep full relative
+// precision, where the plain form loses the digits that cancel between diagonal and neighbours.
+template <int L>
+struct BsrDiffMat {
+  using Vec = float2;
+  using Blk = float4;
+  static constexpr int kLanes = L;
+  int32_t items;
+  const int32_t *__restrict__ ptr;
+  const int32_t *__restrict__ col;
+  const float4 *__restrict__ blk;
+  const float4 *__restrict__ rowsum;
+  template <class G>
+  __device__ __forceinline__ float2 row_partial(int i, int lane, G get) const {
+    const float2 xi = get(i);
+    float2 y = make_float2(0.f, 0.f);
+    if (lane == 0) {
+      const float4 s = rowsum[i];
+      y.x = fmaf(s.y, xi.y, s.x * xi.x);
+      y.y = fmaf(s.w, xi.y, s.z * xi.x);
+    }
+    int k2 = __ldg(ptr + i + 1);
+    for (int k = __ldg(ptr + i) + lane; k < k2; k += L) {
+      const float4 a = blk[k];
+      const float2 xj = get(__ldg(col + k));
+      const float dx = xj.x - xi.x, dy = xj.y - xi.y;
+      y.x = fmaf(a.y, dy, fmaf(a.x, dx, y.x));
+      y.y = fmaf(a.w, dy, fmaf(a.z, dx, y.y));
+    }
+    return y;
+  }
+};
+
 // scalar CSR rows (the general matrix-equation solve), one lane per row
 struct CsrMat {
   using Vec = double;

@@ -279,7 +279,7 @@ struct AssembleArgs {
   const double2 *x0;        // Krylov initial guess (or null = zero)
   // outputs
   double4 *blk;
-  float4 *blk32;
+  float4 *blk32, *rowsum32;
   double2 *rhs, *dinv, *X, *R, *RP, *P0, *V0;
   float2 *dinv32;
   double *beta_b_out, *bfc_b, *F2b1, *eta_3D_b;
@@ -407,10 +407,13 @@ __global__ void k_assemble(AssembleArgs a, PhysParams q, CondArg cond) {
     a.dinv[t] = di;
     a.rhs[t] = rhs;
     if (a.blk32) {
+      double4 rs = make_double4(0.0, 0.0, 0.0, 0.0);
       for (int k = k1; k < k2; ++k) {
         double4 b = a.blk[k];
         a.blk32[k] = make_float4((float)b.x, (float)b.y, (float)b.z, (float)b.w);
+        rs.x += b.x; rs.y += b.y; rs.z += b.z; rs.w += b.w;
       }
+      a.rowsum32[t] = make_float4((float)rs.x, (float)rs.y, (float)rs.z, (float)rs.w);
       a.dinv32[t] = make_float2((float)di.x, (float)di.y);
     }
     // -- Krylov initial residual r = D^-1 (b - A x0)
@@ -815,6 +818,7 @@ Work *ensure_work(ufe_ctx *ctx) {
   w->nnzb = ctx->ops[UFE_OP_M2_DDX_B_B].nnz;
   w->blk = alloc_n<double4>(w->nnzb);
   w->blk32 = alloc_n<float4>(w->nnzb);
+  w->rowsum32 = alloc_n<float4>(nTri);
   KrylovVecs &k = w->kv;
   double2 **d2[] = {&k.X, &k.R, &k.RP, &k.S, &k.T, &k.dinv, &k.B, &k.P[0], &k.P[1], &k.V[0], &k.V[1]};
   for (auto p : d2) *p = alloc_n<double2>(nTri);
@@ -872,7 +876,7 @@ void free_work(ufe_ctx *ctx) {
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   if (w->graph_ssa) cudaGraphExecDestroy(w->graph_ssa);
   if (w->graph_diva) cudaGraphExecDestroy(w->graph_diva);
-  void *ptrs[] = {w->blk, w->blk32, w->kv.X, w->kv.R, w->kv.RP, w->kv.S, w->kv.T, w->kv.dinv, w->kv.B,
+  void *ptrs[] = {w->blk, w->blk32, w->rowsum32, w->kv.X, w->kv.R, w->kv.RP, w->kv.S, w->kv.T, w->kv.dinv, w->kv.B,
                   w->kv.P[0], w->kv.P[1], w->kv.V[0], w->kv.V[1], w->kv.x32, w->kv.R32, w->kv.RP32,
                   w->kv.S32, w->kv.T32, w->kv.dinv32, w->kv.P32[0], w->kv.P32[1], w->kv.V32[0],
                   w->kv.V32[1], w->uv, w->tau_d, w->fgr_b, w->bc_mask, w->bc_uv, w->uv_base, w->tau_b,
@@ -945,6 +949,7 @@ struct Solver {
     a.x0 = x0;
     a.blk = w->blk;
     a.blk32 = (p.precision == UFE_PREC_FP32_REFINE) ? w->blk32 : nullptr;
+    a.rowsum32 = w->rowsum32;
     a.rhs = w->kv.B; a.dinv = w->kv.dinv; a.X = w->kv.X; a.R = w->kv.R; a.RP = w->kv.RP;
     a.P0 = w->kv.P[0]; a.V0 = w->kv.V[0]; a.dinv32 = w->kv.dinv32;
     a.beta_b_out = w->beta_b; a.bfc_b = w->bfc_b; a.F2b1 = w->F2b1; a.eta_3D_b = w->eta_3D_b;
@@ -983,9 +988,9 @@ struct Solver {
     return BsrMat<double, double, L>{w->nTri, m2.ptr, m2.ind, w->blk};
   }
   template <int L>
-  BsrMat<float, float, L> mat32() const {
+  BsrDiffMat<L> mat32() const {
     const DevCSR &m2 = ctx->ops[UFE_OP_M2_DDX_B_B];
-    return BsrMat<float, float, L>{w->nTri, m2.ptr, m2.ind, w->blk32};
+    return BsrDiffMat<L>{w->nTri, m2.ptr, m2.ind, w->blk32, w->rowsum32};
   }
   KV<double2> kv64() const {
     KV<double2> v;

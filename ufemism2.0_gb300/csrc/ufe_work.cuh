@@ -91,6 +91,7 @@ struct Work {
   // stiffness matrix
   double4 *blk = nullptr;
   float4 *blk32 = nullptr;
+  float4 *rowsum32 = nullptr;   // FP64 row sums of the blocks, rounded to FP32 (difference form)
   int32_t *diag = nullptr;      // index of the diagonal block per block row
   KrylovVecs kv{};
   // velocity state and per-solve inputs on triangles
