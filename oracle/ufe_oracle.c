@@ -16,6 +16,9 @@
 
 #include <math.h>
 #include <float.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
 #include <stdlib.h>
 #include <string.h>
 
@@ -520,6 +523,7 @@ void orc_spmv(const orc_csr *A, const double *x, double *y, int32_t ncols) {
   for (int32_t c = 0; c < ncols; ++c) {
     const double *xc = x + (int64_t)c * A->n;
     double *yc = y + (int64_t)c * A->m;
+#pragma omp parallel for schedule(static) if (A->m > 20000)
     for (int32_t i = 1; i <= A->m; ++i) {
       double s = 0.0;
       for (int32_t k = A->ptr[i - 1]; k <= A->ptr[i] - 1; ++k)
@@ -627,9 +631,23 @@ int32_t orc_assemble_linearised(const ufe_mesh_desc *m, const orc_csr *ops, cons
  * divergence when ||r|| >= 1e4 ||r0|| or NaN).  PETSc is not part of the reference tree; this is
  * the published BiCGStab recurrence in the form of PETSc's src/ksp/ksp/impls/bcgs/bcgs.c. */
 
+/* Dot product summed in fixed chunks of 4096 (each chunk sequentially, then the chunk sums in
+ * order), so the result does not depend on the number of OpenMP threads. */
 static double dot(const double *a, const double *b, int64_t n) {
+  const int64_t CH = 4096;
+  const int64_t nch = (n + CH - 1) / CH;
+  double part_stack[64];
+  double *part = nch <= 64 ? part_stack : (double *)malloc(sizeof(double) * (size_t)nch);
+#pragma omp parallel for schedule(static) if (n > 20000)
+  for (int64_t c = 0; c < nch; ++c) {
+    double s = 0.0;
+    int64_t e = (c + 1) * CH < n ? (c + 1) * CH : n;
+    for (int64_t i = c * CH; i < e; ++i) s += a[i] * b[i];
+    part[c] = s;
+  }
   double s = 0.0;
-  for (int64_t i = 0; i < n; ++i) s += a[i] * b[i];
+  for (int64_t c = 0; c < nch; ++c) s += part[c];
+  if (part != part_stack) free(part);
   return s;
 }
 
@@ -665,14 +683,18 @@ int32_t orc_bicgstab(const orc_csr *A, const double *b, double *x, double rtol, 
     double rho = dot(R, RP, n);
     if (rho == 0.0 || isnan(rho)) { status = UFE_ERR_DIVERGED; break; }
     double beta = (rho / rhoold) * (alpha / omegaold);
+#pragma omp parallel for schedule(static) if (n > 20000)
     for (int64_t i = 0; i < n; ++i) P[i] = R[i] - beta * omegaold * V[i] + beta * P[i];
     orc_spmv(A, P, W, 1);
+#pragma omp parallel for schedule(static) if (n > 20000)
     for (int64_t i = 0; i < n; ++i) V[i] = dinv[i] * W[i];
     double d1 = dot(V, RP, n);
     if (d1 == 0.0 || isnan(d1)) { status = UFE_ERR_DIVERGED; break; }
     alpha = rho / d1;
+#pragma omp parallel for schedule(static) if (n > 20000)
     for (int64_t i = 0; i < n; ++i) S[i] = R[i] - alpha * V[i];
     orc_spmv(A, S, W, 1);
+#pragma omp parallel for schedule(static) if (n > 20000)
     for (int64_t i = 0; i < n; ++i) T[i] = dinv[i] * W[i];
     d1 = dot(S, T, n);
     double d2 = dot(T, T, n);
@@ -684,7 +706,9 @@ int32_t orc_bicgstab(const orc_csr *A, const double *b, double *x, double rtol, 
       break;
     }
     double omega = d1 / d2;
+#pragma omp parallel for schedule(static) if (n > 20000)
     for (int64_t i = 0; i < n; ++i) x[i] = x[i] + alpha * P[i] + omega * S[i];
+#pragma omp parallel for schedule(static) if (n > 20000)
     for (int64_t i = 0; i < n; ++i) R[i] = S[i] - omega * T[i];
     dp = sqrt(dot(R, R, n));
     rhoold = rho; omegaold = omega;
