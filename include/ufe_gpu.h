@@ -265,6 +265,25 @@ int32_t ufe_solve_diva_resident(ufe_ctx *ctx, const ufe_solver_params *p, int32_
                                 ufe_solve_stats *stats);
 int32_t ufe_velocity_download(ufe_ctx *ctx, double *u_b, double *v_b);
 
+/* ---- allocation-free solve -------------------------------------------------------------------- */
+/* The CSR matrix-equation solve of ufe_solve_csr (same BiCGStab/Jacobi, same convergence test)
+ * for callers that cannot let a library allocate device memory -- e.g. a host model whose GPU
+ * memory is handed out by its own pool or caching allocator, or a coupled run that fixes its GPU
+ * footprint at start-up.  This entry point has no counterpart in the reference.
+ *
+ * The matrix (d_ptr m+1, d_ind/d_val nnz, `index_base` 0 or 1), right-hand side and solution are
+ * the caller's DEVICE buffers; d_xx holds the initial guess on entry and the solution on exit.
+ * Work vectors and scalars live in one fixed device array of the library (about 9.1 MiB per GPU,
+ * reserved while the library is loaded): no cudaMalloc or cudaFree happens in the call.  Systems
+ * with more than 131,072 unknowns are rejected with UFE_ERR_CAPACITY.  Work runs on `cuda_stream`
+ * (NULL: the legacy default stream) and the call returns after it finishes.  All calls on a device
+ * share the array: calls that overlap on the GPU race.  The first call on a device resolves the
+ * array's address and should come before any stream capture begins.  No context is needed. */
+int32_t ufe_solve_csr_noalloc(int32_t m, int64_t nnz, const int32_t *d_ptr, const int32_t *d_ind,
+                              const double *d_val, int32_t index_base, const double *d_bb, double *d_xx,
+                              double rtol, double abstol, int32_t max_it, int32_t *n_Axb_its,
+                              void *cuda_stream);
+
 /* ---- diagnostics ---------------------------------------------------------------------------- */
 /* Per-Picard-iteration record of the last solve on this context: `cap` rows of 5 values
  * (L2 change norm, Krylov iterations, Krylov status, final Krylov residual, FP64 refinement

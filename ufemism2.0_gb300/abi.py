@@ -193,6 +193,9 @@ EXPORTS = {
     "ufe_solve_ssa_resident": (C.c_int32, [C.c_void_p, C.POINTER(SolverParams), C.c_int32, C.POINTER(SolveStats)]),
     "ufe_solve_diva_resident": (C.c_int32, [C.c_void_p, C.POINTER(SolverParams), C.c_int32, C.POINTER(SolveStats)]),
     "ufe_velocity_download": (C.c_int32, [C.c_void_p, dptr, dptr]),
+    "ufe_solve_csr_noalloc": (C.c_int32, [C.c_int32, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32,
+                                          C.c_void_p, C.c_void_p, C.c_double, C.c_double, C.c_int32, iptr,
+                                          C.c_void_p]),
     "ufe_solve_history": (C.c_int32, [C.c_void_p, dptr, C.c_int32, iptr]),
     "ufe_profile_krylov_kernels": (C.c_int32, [C.c_void_p, C.c_int32, C.c_int32, dptr, C.POINTER(C.c_int64)]),
 }

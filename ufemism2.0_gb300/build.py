@@ -16,7 +16,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libufe_gpu.so")
-SOURCES = ["ufe_ctx.cu", "ufe_layout.cu", "ufe_operators.cu", "ufe_spmv.cu", "ufe_velocity.cu"]
+SOURCES = ["ufe_ctx.cu", "ufe_layout.cu", "ufe_operators.cu", "ufe_spmv.cu", "ufe_velocity.cu", "ufe_noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
