@@ -265,6 +265,112 @@ int32_t ufe_solve_diva_resident(ufe_ctx *ctx, const ufe_solver_params *p, int32_
                                 ufe_solve_stats *stats);
 int32_t ufe_velocity_download(ufe_ctx *ctx, double *u_b, double *v_b);
 
+/* ---- thermodynamics: implicit column temperature solve ---------------------------------------- */
+enum ufe_heat_capacity { UFE_CP_UNIFORM = 0, UFE_CP_POUNDER1965 = 1 };   /* choice_ice_heat_capacity        */
+enum ufe_conductivity  { UFE_K_UNIFORM = 0, UFE_K_RITZ1987 = 1 };        /* choice_ice_thermal_conductivity */
+enum ufe_gl_temp_bc    { UFE_GLBC_GROUNDED = 0, UFE_GLBC_SUBGRID = 1, UFE_GLBC_PMP = 2 }; /* choice_GL_temperature_BC */
+/* Per-vertex column type: the reference's mask_gl_gr (grounded side of the grounding line, which is
+ * also grounded), mask_grounded_ice and mask_floating_ice, tested in that order
+ * (thermodynamics_3D_heat_equation.f90:168,198,207). */
+enum ufe_column_mask   { UFE_COL_NONE = 0, UFE_COL_GROUNDED = 1, UFE_COL_FLOATING = 2, UFE_COL_GL_GR = 3 };
+
+/* Configuration scalars solve_3D_heat_equation reads (model_configuration.f90:578-584). */
+typedef struct {
+  double  dt;                               /* [yr] thermodynamics time step                        */
+  double  Hi_min_thermo;                    /* [m]  default 10                                      */
+  int32_t choice_ice_heat_capacity;         /* default UFE_CP_POUNDER1965                           */
+  int32_t choice_ice_thermal_conductivity;  /* default UFE_K_RITZ1987                               */
+  double  uniform_ice_heat_capacity;        /* [J kg^-1 K^-1]       default 2009                    */
+  double  uniform_ice_thermal_conductivity; /* [J m^-1 K^-1 yr^-1]  default 6.626958e7              */
+  int32_t choice_GL_temperature_BC;         /* default UFE_GLBC_GROUNDED                            */
+  int32_t reserved[7];
+} ufe_thermo_params;
+
+void ufe_default_thermo_params(ufe_thermo_params *p);
+
+/* Column level.  The per-column inputs of the column loop of solve_3D_heat_equation
+ * (thermodynamics_3D_heat_equation.f90:133-290) once its prelude has run: nV x nz arrays are
+ * column-major (layer k of vertex vi at k*nV + vi), as ice%Ti(vi,k) is. */
+typedef struct {
+  const double  *Ti;                     /* nV x nz  temperature at time t [K]; Cp and K follow it   */
+  const double  *u_3D, *v_3D, *w_3D;     /* nV x nz  [m yr^-1]                                       */
+  const double  *u_times_dTdxp_upwind;   /* nV x nz  [K yr^-1] (calc_upwind_heat_flux_derivatives)   */
+  const double  *v_times_dTdyp_upwind;   /* nV x nz  [K yr^-1]                                       */
+  const double  *dzeta_dx, *dzeta_dy;    /* nV x nz  ice%dzeta_dx_ak, dzeta_dy_ak [m^-1]             */
+  const double  *dzeta_dz, *dzeta_dt;    /* nV x nz  ice%dzeta_dz_ak [m^-1], dzeta_dt_ak [yr^-1]     */
+  const double  *internal_heating;       /* nV x nz  Phi [J kg^-1 yr^-1]                             */
+  const double  *Hi_eff;                 /* nV [m]                                                   */
+  const double  *T_surf_annual;          /* nV [K]                                                   */
+  const double  *Q_base_grnd;            /* nV [J m^-2 yr^-1] frictional + geothermal heating        */
+  const int32_t *mask;                   /* nV enum ufe_column_mask                                  */
+  const double  *fraction_gr;            /* nV (read for UFE_GLBC_SUBGRID only; may be NULL else)    */
+  const double  *geothermal_heat_flux;   /* nV [J m^-2 yr^-1] (Robin profile)                        */
+  const double  *SMB;                    /* nV [m yr^-1]      (Robin profile)                        */
+} ufe_thermo_columns;
+
+/* One step for nV independent columns (host arrays in and out): per column the implicit solve
+ * of solve_1D_heat_equation (:309-479) with the per-column dt halving (up to 10 levels,
+ * :163-239) and the stability check (NaN, < 180 K, > T0, :226-232); then the Robin profile
+ * (replace_Ti_with_robin_solution, thermodynamics_utilities.f90:256-337) for the columns that
+ * stayed unstable when they are fewer than ceil(nV/100), else UFE_ERR_THERMO_UNSTABLE (:251-290).
+ * *n_unstable receives the number of such columns.  No mesh needs to be uploaded. */
+int32_t ufe_thermo_step(ufe_ctx *ctx, const ufe_thermo_params *p, int32_t nV, int32_t nz,
+                        const double *zeta, const ufe_thermo_columns *cols, double *Ti_next,
+                        int32_t *n_unstable);
+
+/* Mesh level: the fields solve_3D_heat_equation(mesh, ice, climate, SMB, dt) reads
+ * (thermodynamics_3D_heat_equation.f90:33).  The prelude runs on the GPU from these: the zeta
+ * gradients of calc_zeta_gradients (zeta_gradients.f90:19, vertex terms), Cp, K and T_pmp
+ * (thermodynamics_utilities.f90:130-229), the upwind advection terms of
+ * calc_upwind_heat_flux_derivatives (:339-434) and the annual-mean surface temperature.
+ * Strain and frictional heating are inputs (calc_strain_heating / calc_frictional_heating). */
+typedef struct {
+  const double  *Ti;                     /* nV x nz  [K]                                            */
+  const double  *Hi, *Hi_eff, *Hs;       /* nV [m]                                                  */
+  const double  *dHi_dt, *dHs_dt;        /* nV [m yr^-1]                                            */
+  const double  *u_vav, *v_vav;          /* nV [m yr^-1] vertically averaged velocity on vertices  */
+  const double  *u_3D, *v_3D, *w_3D;     /* nV x nz   [m yr^-1]                                     */
+  const double  *u_3D_b, *v_3D_b;        /* nTri x nz [m yr^-1]                                     */
+  const double  *internal_heating;       /* nV x nz   [J kg^-1 yr^-1]                               */
+  const double  *frictional_heating;     /* nV [J m^-2 yr^-1]                                       */
+  const double  *geothermal_heat_flux;   /* nV [J m^-2 yr^-1]                                       */
+  const double  *T2m;                    /* nV x n_months [K] (climate%T2m)                         */
+  int32_t        n_months;
+  int32_t        pad;
+  const double  *SMB;                    /* nV [m yr^-1]                                            */
+  const int32_t *mask;                   /* nV enum ufe_column_mask                                 */
+  const double  *fraction_gr;            /* nV (UFE_GLBC_SUBGRID only; may be NULL else)            */
+} ufe_heat_fields;
+
+/* solve_3D_heat_equation on the uploaded mesh (operators built or set; the mesh's nz and zeta):
+ * host fields in, ice%Ti_next out. */
+int32_t ufe_solve_3D_heat_equation(ufe_ctx *ctx, const ufe_thermo_params *p, const ufe_heat_fields *f,
+                                   double *Ti_next, int32_t *n_unstable);
+
+/* Device-resident time stepping: ufe_heat_upload copies the fields once; each of the `nsteps`
+ * steps of ufe_heat_step_resident is one solve_3D_heat_equation followed by Ti <- Ti_next, with
+ * velocities, geometry, heating and climate held fixed.  *n_unstable_total sums the Robin
+ * columns over the steps; a step with too many unstable columns stops the stepping
+ * (UFE_ERR_THERMO_UNSTABLE, the resident Ti left at that step's input).  ufe_heat_download
+ * copies the resident temperature out. */
+int32_t ufe_heat_upload(ufe_ctx *ctx, const ufe_heat_fields *f);
+int32_t ufe_heat_step_resident(ufe_ctx *ctx, const ufe_thermo_params *p, int32_t nsteps,
+                               int32_t *n_unstable_total, double *device_ms);
+int32_t ufe_heat_download(ufe_ctx *ctx, double *Ti);
+
+/* The tridiagonal d/dzeta and d2/dzeta2 operators of the column solve (calc_zeta_operators_tridiagonal,
+ * mesh_zeta.f90:487-605, from calc_vertical_operators_reg_1D, :288-366).  Each array has nz
+ * entries indexed by row: *_l[k] couples row k to k-1 (*_l[0] = 0), *_u[k] couples k to k+1
+ * (*_u[nz-1] = 0).  Host computation. */
+int32_t ufe_zeta_operators(int32_t nz, const double *zeta, double *ddz_l, double *ddz_d,
+                           double *ddz_u, double *d2dz2_l, double *d2dz2_d, double *d2dz2_u);
+
+/* solve_tridiagonal_matrix_equation (tridiagonal_solver.f90:13-51) for `nsys` systems of size n on
+ * the GPU: system j in column j of the n x nsys column-major host arrays a (a[0] unused), b, c
+ * (c[n-1] unused) and d; x receives the solutions.  Thomas algorithm, one thread per system. */
+int32_t ufe_tridiagonal_solve(ufe_ctx *ctx, int32_t n, int32_t nsys, const double *a, const double *b,
+                              const double *c, const double *d, double *x);
+
 /* ---- allocation-free solve -------------------------------------------------------------------- */
 /* The CSR matrix-equation solve of ufe_solve_csr (same BiCGStab/Jacobi, same convergence test)
  * for callers that cannot let a library allocate device memory -- e.g. a host model whose GPU

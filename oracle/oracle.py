@@ -66,6 +66,12 @@ def load():
         "orc_csr_solve": (C.c_int32, [C.c_int32, C.c_int64, ip, ip, dp, dp, dp, C.c_double, C.c_double,
                                       C.c_int32, ip]),
         "orc_csr_spmv": (C.c_int32, [C.c_int32, C.c_int32, C.c_int64, ip, ip, dp, dp, dp, C.c_int32]),
+        "orc_zeta_operators": (C.c_int32, [C.c_int32, dp, dp, dp, dp, dp, dp, dp]),
+        "orc_tridiagonal_batched": (C.c_int32, [C.c_int32, C.c_int32, dp, dp, dp, dp, dp]),
+        "orc_thermo_step": (C.c_int32, [C.POINTER(abi.ThermoParams), C.c_int32, C.c_int32, dp,
+                                        C.POINTER(abi.ThermoColumns), dp, ip, ip]),
+        "orc_ops_solve_3D_heat_equation": (C.c_int32, [vp, C.POINTER(abi.ThermoParams), C.POINTER(abi.HeatFields),
+                                                       dp, ip, ip]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -204,3 +210,56 @@ class Oracle:
         if rc < 0:
             raise OracleError(rc)
         return stats.n_visc_its, stats.n_Axb_its, stats.as_dict()
+
+    def solve_3D_heat_equation(self, fields: dict, params):
+        """orc_ops_solve_3D_heat_equation on this mesh: (Ti_next, n_unstable, status, flags)."""
+        f, keep = self.abi.heat_fields(fields)
+        out = np.zeros((self.mesh.nV, self.mesh.nz), order="F")
+        n = C.c_int32()
+        flags = np.zeros(self.mesh.nV, np.int32)
+        rc = self.lib.orc_ops_solve_3D_heat_equation(self.h, C.byref(params), C.byref(f), self.abi.as_d(out),
+                                                     C.byref(n), self.abi.as_i(flags))
+        return out, n.value, rc, flags
+
+
+# -- thermodynamics ------------------------------------------------------------------------------
+def zeta_operators(zeta):
+    """orc_zeta_operators: (ddz_l, ddz_d, ddz_u, d2_l, d2_d, d2_u) indexed by row."""
+    lib = load()
+    zeta = _d(zeta)
+    out = [np.zeros(zeta.size) for _ in range(6)]
+    rc = lib.orc_zeta_operators(zeta.size, zeta.ctypes.data_as(_pkg().abi.dptr),
+                                *[o.ctypes.data_as(_pkg().abi.dptr) for o in out])
+    if rc != 0:
+        raise OracleError(rc, "zeta operators")
+    return tuple(out)
+
+
+def tridiagonal(a, b, c, d):
+    """solve_tridiagonal_matrix_equation for each column of the (n, nsys) arrays."""
+    lib = load()
+    abi = _pkg().abi
+    arrs = [np.asfortranarray(v, dtype=np.float64) for v in (a, b, c, d)]
+    n = arrs[0].shape[0]
+    nsys = 1 if arrs[0].ndim == 1 else arrs[0].shape[1]
+    x = np.zeros_like(arrs[1], order="F")
+    rc = lib.orc_tridiagonal_batched(n, nsys, *[v.ctypes.data_as(abi.dptr) for v in arrs], x.ctypes.data_as(abi.dptr))
+    if rc != 0:
+        raise OracleError(rc, "tridiagonal")
+    return x
+
+
+def thermo_step(params, zeta, cols: dict):
+    """orc_thermo_step: returns (Ti_next, n_unstable, status, flags); flags per column are
+    0 stable, 2 stable after dt halving, 1 unstable (Robin profile)."""
+    lib = load()
+    abi = _pkg().abi
+    zeta = _d(zeta)
+    nV, nz = np.asarray(cols["Ti"]).shape
+    st, keep = abi.thermo_columns(cols)
+    out = np.zeros((nV, nz), order="F")
+    n = C.c_int32()
+    flags = np.zeros(nV, np.int32)
+    rc = lib.orc_thermo_step(C.byref(params), nV, nz, zeta.ctypes.data_as(abi.dptr), C.byref(st),
+                             out.ctypes.data_as(abi.dptr), C.byref(n), flags.ctypes.data_as(abi.iptr))
+    return out, n.value, rc, flags

@@ -1134,6 +1134,9 @@ orc_ops *orc_ops_create(const ufe_mesh_desc *mesh, int32_t *status) {
   return h;
 }
 
+const ufe_mesh_desc *orc_ops_mesh(const orc_ops *h) { return &h->mesh; }
+const orc_csr *orc_ops_op(const orc_ops *h, int32_t op) { return &h->ops[op]; }
+
 void orc_ops_destroy(orc_ops *h) {
   if (!h) return;
   for (int op = 0; op < UFE_OP_COUNT; ++op) orc_csr_free(&h->ops[op]);

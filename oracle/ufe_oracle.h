@@ -82,6 +82,20 @@ int32_t  orc_csr_solve(int32_t m, int64_t nnz, const int32_t *ptr, const int32_t
 int32_t  orc_csr_spmv(int32_t m, int32_t n, int64_t nnz, const int32_t *ptr, const int32_t *ind,
                       const double *val, const double *x, double *y, int32_t ncols);
 
+/* Thermodynamics (ufe_oracle_thermo.c) */
+int32_t orc_zeta_operators(int32_t nz, const double *zeta, double *l1, double *d1, double *u1,
+                           double *l2, double *d2, double *u2);
+void    orc_tridiagonal(int32_t n, const double *a, double *b, const double *c, double *d, double *x);
+int32_t orc_tridiagonal_batched(int32_t n, int32_t nsys, const double *a, const double *b,
+                                const double *c, const double *d, double *x);
+int32_t orc_thermo_step(const ufe_thermo_params *p, int32_t nV, int32_t nz, const double *zeta,
+                        const ufe_thermo_columns *s, double *Ti_next, int32_t *n_unstable,
+                        int32_t *is_unstable);
+int32_t orc_ops_solve_3D_heat_equation(orc_ops *h, const ufe_thermo_params *p, const ufe_heat_fields *f,
+                                       double *Ti_next, int32_t *n_unstable, int32_t *is_unstable);
+const ufe_mesh_desc *orc_ops_mesh(const orc_ops *h);
+const orc_csr *orc_ops_op(const orc_ops *h, int32_t op);
+
 #ifdef __cplusplus
 }
 #endif

@@ -75,12 +75,20 @@ def test_default_params_match(gpu_lib, pkg):
     assert bytes(p) == bytes(q)
 
 
+def test_default_thermo_params_match(gpu_lib, pkg):
+    p = pkg.abi.ThermoParams()
+    gpu_lib.ufe_default_thermo_params(C.byref(p))
+    q = pkg.abi.default_thermo_params()
+    assert bytes(p) == bytes(q)
+
+
 def test_struct_layout_matches_header(pkg, tmp_path):
     """Compile a C probe against include/ufe_gpu.h and compare sizes/offsets with ctypes."""
     abi = pkg.abi
     structs = {"ufe_mesh_desc": abi.MeshDesc, "ufe_solver_params": abi.SolverParams, "ufe_ice_state": abi.IceState,
                "ufe_bc_prescribed": abi.BCPrescribed, "ufe_diva_state": abi.DivaState,
-               "ufe_solve_stats": abi.SolveStats}
+               "ufe_solve_stats": abi.SolveStats, "ufe_thermo_params": abi.ThermoParams,
+               "ufe_thermo_columns": abi.ThermoColumns, "ufe_heat_fields": abi.HeatFields}
     lines = ["#include <stdio.h>", "#include <stddef.h>", f'#include "{HEADER}"', "int main(void){"]
     for cname, cls in structs.items():
         lines.append(f'printf("{cname} %zu\\n", sizeof({cname}));')

@@ -120,6 +120,92 @@ def default_params(**overrides) -> SolverParams:
     return p
 
 
+# -- thermodynamics ------------------------------------------------------------------------------
+CP = {"uniform": 0, "Pounder1965": 1}
+KI = {"uniform": 0, "Ritz1987": 1}
+GLBC = {"grounded": 0, "subgrid": 1, "pmp": 2}
+COL_NONE, COL_GROUNDED, COL_FLOATING, COL_GL_GR = 0, 1, 2, 3
+
+
+class ThermoParams(C.Structure):
+    _fields_ = [("dt", C.c_double), ("Hi_min_thermo", C.c_double),
+                ("choice_ice_heat_capacity", C.c_int32), ("choice_ice_thermal_conductivity", C.c_int32),
+                ("uniform_ice_heat_capacity", C.c_double), ("uniform_ice_thermal_conductivity", C.c_double),
+                ("choice_GL_temperature_BC", C.c_int32), ("reserved", C.c_int32 * 7)]
+
+
+class ThermoColumns(C.Structure):
+    _fields_ = [(n, dptr) for n in ("Ti", "u_3D", "v_3D", "w_3D", "u_times_dTdxp_upwind", "v_times_dTdyp_upwind",
+                                    "dzeta_dx", "dzeta_dy", "dzeta_dz", "dzeta_dt", "internal_heating", "Hi_eff",
+                                    "T_surf_annual", "Q_base_grnd")] + \
+              [("mask", iptr), ("fraction_gr", dptr), ("geothermal_heat_flux", dptr), ("SMB", dptr)]
+
+
+class HeatFields(C.Structure):
+    _fields_ = [(n, dptr) for n in ("Ti", "Hi", "Hi_eff", "Hs", "dHi_dt", "dHs_dt", "u_vav", "v_vav", "u_3D",
+                                    "v_3D", "w_3D", "u_3D_b", "v_3D_b", "internal_heating", "frictional_heating",
+                                    "geothermal_heat_flux", "T2m")] + \
+              [("n_months", C.c_int32), ("pad", C.c_int32), ("SMB", dptr), ("mask", iptr), ("fraction_gr", dptr)]
+
+
+def default_thermo_params(**overrides) -> ThermoParams:
+    """The defaults of UFEMISM's model_configuration.f90 (same values as ufe_default_thermo_params)."""
+    p = ThermoParams()
+    p.dt = 1.0
+    p.Hi_min_thermo = 10.0
+    p.choice_ice_heat_capacity = CP["Pounder1965"]
+    p.choice_ice_thermal_conductivity = KI["Ritz1987"]
+    p.uniform_ice_heat_capacity = 2009.0
+    p.uniform_ice_thermal_conductivity = 6.626958e7
+    p.choice_GL_temperature_BC = GLBC["grounded"]
+    names = {"choice_ice_heat_capacity": CP, "choice_ice_thermal_conductivity": KI, "choice_GL_temperature_BC": GLBC}
+    for k, v in overrides.items():
+        if k in names and isinstance(v, str):
+            v = names[k][v]
+        setattr(p, k, v)
+    return p
+
+
+def _fcol(a):
+    """Column-major float64 copy of an (n, nz) or (n,) array; None stays None."""
+    if a is None:
+        return None
+    return np.asfortranarray(a, dtype=np.float64)
+
+
+def thermo_columns(cols: dict) -> tuple[ThermoColumns, list]:
+    """ThermoColumns over a dict of the ufe_thermo_columns fields (numpy arrays, (nV, nz) or (nV,))."""
+    keep, vals = [], {}
+    for name, typ in ThermoColumns._fields_:
+        a = cols.get(name)
+        if a is None:
+            vals[name] = None
+            continue
+        a = np.asfortranarray(a, dtype=np.int32) if typ is iptr else _fcol(a)
+        keep.append(a)
+        vals[name] = a.ctypes.data_as(typ)
+    return ThermoColumns(**vals), keep
+
+
+def heat_fields(f: dict) -> tuple[HeatFields, list]:
+    """HeatFields over a dict of the ufe_heat_fields fields (T2m as (nV, n_months))."""
+    keep, vals = [], {}
+    for name, typ in HeatFields._fields_:
+        if name in ("n_months", "pad"):
+            continue
+        a = f.get(name)
+        if a is None:
+            vals[name] = None
+            continue
+        a = np.asfortranarray(a, dtype=np.int32) if typ is iptr else _fcol(a)
+        keep.append(a)
+        vals[name] = a.ctypes.data_as(typ)
+    T2m = np.asarray(f["T2m"])
+    vals["n_months"] = T2m.shape[1] if T2m.ndim == 2 else 1
+    vals["pad"] = 0
+    return HeatFields(**vals), keep
+
+
 # -- numpy <-> ctypes helpers -------------------------------------------------------------------
 def as_d(a):
     """Pointer to a contiguous float64 buffer (Fortran-ordered arrays are flattened column-major)."""
@@ -198,6 +284,15 @@ EXPORTS = {
                                           C.c_void_p]),
     "ufe_solve_history": (C.c_int32, [C.c_void_p, dptr, C.c_int32, iptr]),
     "ufe_profile_krylov_kernels": (C.c_int32, [C.c_void_p, C.c_int32, C.c_int32, dptr, C.POINTER(C.c_int64)]),
+    "ufe_default_thermo_params": (None, [C.POINTER(ThermoParams)]),
+    "ufe_thermo_step": (C.c_int32, [C.c_void_p, C.POINTER(ThermoParams), C.c_int32, C.c_int32, dptr,
+                                    C.POINTER(ThermoColumns), dptr, iptr]),
+    "ufe_solve_3D_heat_equation": (C.c_int32, [C.c_void_p, C.POINTER(ThermoParams), C.POINTER(HeatFields), dptr, iptr]),
+    "ufe_heat_upload": (C.c_int32, [C.c_void_p, C.POINTER(HeatFields)]),
+    "ufe_heat_step_resident": (C.c_int32, [C.c_void_p, C.POINTER(ThermoParams), C.c_int32, iptr, dptr]),
+    "ufe_heat_download": (C.c_int32, [C.c_void_p, dptr]),
+    "ufe_zeta_operators": (C.c_int32, [C.c_int32, dptr, dptr, dptr, dptr, dptr, dptr, dptr]),
+    "ufe_tridiagonal_solve": (C.c_int32, [C.c_void_p, C.c_int32, C.c_int32, dptr, dptr, dptr, dptr, dptr]),
 }
 
 _LIB = None

@@ -1,8 +1,9 @@
 """Build the GB300 library (libufe_gpu.so) in-tree with nvcc, for sm_103a only.
 
 Each translation unit compiles in parallel; the shared object lands in ``_build/`` next to this
-file.  ``--fmad=false`` keeps every a*b+c as two roundings, so operator applications reproduce the
-reference's Fortran arithmetic bit for bit.
+file.  ``--fmad=false`` (device code) and ``-ffp-contract=off`` (host code; gcc contracts a*b+c
+into one fused rounding on aarch64 by default) keep every a*b+c as two roundings, so operator
+applications reproduce the reference's Fortran arithmetic bit for bit on any host.
 """
 from __future__ import annotations
 
@@ -16,7 +17,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libufe_gpu.so")
-SOURCES = ["ufe_ctx.cu", "ufe_layout.cu", "ufe_operators.cu", "ufe_spmv.cu", "ufe_velocity.cu", "ufe_noalloc.cu"]
+SOURCES = ["ufe_ctx.cu", "ufe_layout.cu", "ufe_operators.cu", "ufe_spmv.cu", "ufe_velocity.cu", "ufe_noalloc.cu",
+           "ufe_thermo.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -28,7 +30,7 @@ def nvcc_path() -> str:
 
 
 def _flags(ptxas_verbose: bool) -> list[str]:
-    f = ARCH + ["-O3", "-lineinfo", "--fmad=false", "-std=c++17", "-Xcompiler", "-fPIC,-O2",
+    f = ARCH + ["-O3", "-lineinfo", "--fmad=false", "-std=c++17", "-Xcompiler", "-fPIC,-O2,-ffp-contract=off",
                 "-I" + os.path.join(HERE, "..", "include")]
     if ptxas_verbose:
         f += ["-Xptxas", "-v"]

@@ -103,6 +103,8 @@ struct ufe_ctx {
 
   // solver workspace (allocated lazily for the mesh size)
   struct Work *work = nullptr;
+  // thermodynamics workspace and resident heat-equation state (ufe_thermo.cu)
+  struct ThermoWork *thermo = nullptr;
 
   ReduceArea red;
 };
@@ -134,6 +136,9 @@ int32_t pick_blocks(int64_t items, int threads, int max_blocks);
 
 // ufe_operators.cu
 void build_operators_gpu(ufe_ctx *ctx);
+
+// ufe_thermo.cu
+void free_thermo(ufe_ctx *ctx);
 
 // ufe_layout.cu: internal (Z-order) numbering and the mappings at the ABI boundary
 void layout_upload_mesh(ufe_ctx *ctx, const ufe_mesh_desc *m);

@@ -871,6 +871,7 @@ Work *ensure_work(ufe_ctx *ctx) {
 }
 
 void free_work(ufe_ctx *ctx) {
+  free_thermo(ctx);   // the resident heat state depends on the mesh and its operators
   Work *w = ctx->work;
   if (!w) return;
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);

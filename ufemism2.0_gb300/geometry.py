@@ -159,3 +159,160 @@ def small_dome(seed=0, nz=12):
 def small_channel(seed=0, nz=8, sliding="Schoof2005"):
     """A ~2,000-vertex channel for DIVA tests."""
     return channel_case(seed=seed, nz=nz, res_scale=6.5, sliding=sliding)
+
+
+# ---- thermodynamics workloads ----------------------------------------------------------------
+SEC_PER_YEAR = 31556943.36
+T0 = 273.16
+CC_GRADIENT = 8.7e-4
+
+
+def quadratic_zeta(nz):
+    """nz zeta values from 0 (surface) to 1 (base), spaced quadratically closer toward the base."""
+    s = np.linspace(0.0, 1.0, nz)
+    return 1.0 - (1.0 - s) ** 2
+
+
+def smooth_field(x, y, corr_len, seed, n_modes=96):
+    """A smooth, roughly standard-normal random field: a sum of random plane waves whose
+    wavenumbers are drawn with scale 1/corr_len."""
+    rng = np.random.default_rng(seed)
+    k = rng.normal(0.0, 1.0 / corr_len, size=(n_modes, 2))
+    ph = rng.uniform(0.0, 2.0 * np.pi, n_modes)
+    f = np.zeros(np.shape(x))
+    for j in range(n_modes):
+        f += np.cos(k[j, 0] * x + k[j, 1] * y + ph[j])
+    return f * np.sqrt(2.0 / n_modes)
+
+
+def _uniform_marginal(f):
+    """Map a field to values uniform in (0, 1) by rank."""
+    r = np.empty(f.size)
+    r[np.argsort(f, kind="stable")] = np.arange(f.size)
+    return (r + 0.5) / f.size
+
+
+def thermo_case(nV=200_000, nz=30, seed=0, corr_len=50e3, thick_corr_len=200e3, dt=10.0):
+    """Batched column thermodynamics: a uniform-resolution mesh of about ``nV`` vertices (7 km
+    spacing, so that the explicit horizontal advection keeps u dt / dx < 1; 2,750 km x 2,750 km
+    at 200,000 vertices) with ``nz`` quadratic zeta layers; thickness
+    uniform in [0, 4000] m with 15 % of the columns ice-free (and a taper to zero over the 40 km
+    next to the domain border); surface
+    temperature uniform in [-50, -10] degC; geothermal flux normal(55, 10) mW m^-2; velocities from
+    smooth random fields with ``corr_len`` correlation, |u| <= 500 m/yr; thickness and the
+    floating mask vary over ``thick_corr_len``; about a sixth of the ice floating, with
+    grounding-line columns between.  Returns (mesh, fields, params): the fields of
+    ufe_heat_fields and an abi.ThermoParams with the given dt [yr]."""
+    # explicit horizontal advection (calc_upwind_heat_flux_derivatives) needs u dt / dx < 1:
+    # 500 m/yr x 10 yr on a 7 km mesh.  The generator places ~1.3 (L/res)^2 vertices.
+    res = 7.0e3
+    L = res * np.sqrt(nV / 1.3)
+    mesh = generate_mesh(-L / 2, L / 2, -L / 2, L / 2, lambda x, y: np.full(np.shape(x), res), seed=seed,
+                         nz=nz, zeta=quadratic_zeta(nz))
+    n = mesh.nV
+    x, y = mesh.V[:, 0], mesh.V[:, 1]
+    zeta = mesh.zeta
+    q = _uniform_marginal(smooth_field(x, y, thick_corr_len, seed + 1))
+    H = 4000.0 * np.clip((q - 0.15) / 0.85, 0.0, 1.0)
+    # the ice thins to zero over the 40 km next to the domain border (no ice on the border, where
+    # an upwind triangle can be missing)
+    dist = np.minimum(np.minimum(x + L / 2, L / 2 - x), np.minimum(y + L / 2, L / 2 - y))
+    H *= np.clip((dist - 0.5 * res) / 40e3, 0.0, 1.0)
+    H[mesh.VBI > 0] = 0.0
+    ice = H > 0.0
+    floating = (smooth_field(x, y, thick_corr_len, seed + 2) > 1.0) & ice
+    grounded = ice & ~floating
+    # grounded vertices with a floating neighbour: the grounded side of the grounding line
+    C = mesh.C - 1
+    has_fl_nb = np.zeros(n, bool)
+    for c in range(mesh.nC_mem):
+        nb = C[:, c]
+        ok = (c < mesh.nC) & (nb >= 0)
+        has_fl_nb |= ok & floating[np.where(ok, nb, 0)]
+    gl = grounded & has_fl_nb
+    mask = np.zeros(n, np.int32)
+    mask[grounded] = abi.COL_GROUNDED
+    mask[floating] = abi.COL_FLOATING
+    mask[gl] = abi.COL_GL_GR
+    Hs = np.where(floating, H * (1.0 - ICE_DENSITY / SEAWATER_DENSITY), H)
+
+    T_surf = 273.15 - 50.0 + 40.0 * _uniform_marginal(smooth_field(x, y, corr_len, seed + 3))
+    months = np.arange(12)
+    T2m = T_surf[:, None] + 10.0 * np.cos(2.0 * np.pi * (months[None, :] + 0.5) / 12.0)
+    geo = (55.0 + 10.0 * smooth_field(x, y, corr_len, seed + 4)) * 1e-3 * SEC_PER_YEAR
+    u = smooth_field(x, y, corr_len, seed + 5)
+    v = smooth_field(x, y, corr_len, seed + 6)
+    scale = 495.0 / max(np.sqrt(u * u + v * v).max(), 1e-12)
+    u_vav, v_vav = u * scale, v * scale
+    SMB = 0.3 + 0.4 * smooth_field(x, y, corr_len, seed + 7)
+    shape = 1.1 - 0.5 * zeta ** 4                       # vertical mean 1
+    u_3D = np.asfortranarray(u_vav[:, None] * shape[None, :])
+    v_3D = np.asfortranarray(v_vav[:, None] * shape[None, :])
+    w_3D = np.asfortranarray(-SMB[:, None] * (1.0 - zeta[None, :]))
+    T = mesh.Tri - 1
+    u_3D_b = np.asfortranarray(u_3D[T].mean(axis=1))
+    v_3D_b = np.asfortranarray(v_3D[T].mean(axis=1))
+    speed = np.sqrt(u_vav ** 2 + v_vav ** 2) / 500.0
+    phi = np.asfortranarray(2000.0 * speed[:, None] * zeta[None, :] ** 4)
+    fric = np.where(mask == abi.COL_FLOATING, 0.0, 0.05 * speed * SEC_PER_YEAR)
+    fric[~ice] = 0.0
+    dHi_dt = 0.05 * smooth_field(x, y, corr_len, seed + 8)
+    dHs_dt = np.where(floating, 0.115 * dHi_dt, 0.05 * smooth_field(x, y, corr_len, seed + 9))
+    fr = np.where(mask == abi.COL_FLOATING, 0.0, 1.0)
+    fr[gl] = 0.5 + 0.5 * _uniform_marginal(smooth_field(x, y, corr_len, seed + 10))[gl]
+    fr[~ice] = 0.0
+    Ts = np.minimum(T_surf, T0)
+    pmp_b = T0 - CC_GRADIENT * H
+    Tb = np.minimum(pmp_b, Ts + 25.0 + 5.0 * smooth_field(x, y, corr_len, seed + 11))
+    Ti = np.asfortranarray(Ts[:, None] + (Tb - Ts)[:, None] * zeta[None, :])
+    Ti[H < 10.0, :] = T_surf[H < 10.0, None]
+    fields = dict(Ti=Ti, Hi=H, Hi_eff=H.copy(), Hs=Hs, dHi_dt=dHi_dt, dHs_dt=dHs_dt, u_vav=u_vav, v_vav=v_vav,
+                  u_3D=u_3D, v_3D=v_3D, w_3D=w_3D, u_3D_b=u_3D_b, v_3D_b=v_3D_b, internal_heating=phi,
+                  frictional_heating=fric, geothermal_heat_flux=geo, T2m=np.asfortranarray(T2m), SMB=SMB,
+                  mask=mask, fraction_gr=fr)
+    params = abi.default_thermo_params(dt=dt)
+    return mesh, fields, params
+
+
+def small_thermo(seed=0, nz=30, nV=3000):
+    """A ~3,000-vertex thermodynamics case for tests the CPU oracle finishes in seconds."""
+    return thermo_case(nV=nV, nz=nz, seed=seed)
+
+
+def random_columns(nV, nz, seed=0, stiff_frac=0.0, stiffness=300.0):
+    """Per-column inputs of ufe_thermo_columns without a mesh (random but physical values); a
+    fraction ``stiff_frac`` of the ice columns gets vertical velocities ``stiffness`` times larger,
+    which makes some of them need dt halving and some fail the stability check."""
+    rng = np.random.default_rng(seed)
+    zeta = quadratic_zeta(nz)
+    H = rng.uniform(0.0, 4000.0, nV)
+    H[rng.random(nV) < 0.15] = rng.uniform(0.0, 9.0, 1)[0]
+    mask = np.where(rng.random(nV) < 0.7, abi.COL_GROUNDED, abi.COL_FLOATING).astype(np.int32)
+    mask[rng.random(nV) < 0.1] = abi.COL_GL_GR
+    T_surf = rng.uniform(223.15, 263.15, nV)
+    Ts = np.minimum(T_surf, T0)
+    pmp = T0 - CC_GRADIENT * H[:, None] * zeta[None, :]
+    Tb = np.minimum(pmp[:, -1], Ts + rng.uniform(5.0, 40.0, nV))
+    Ti = Ts[:, None] + (Tb - Ts)[:, None] * zeta[None, :]
+    Hc = np.maximum(H, 10.0)
+    u = rng.uniform(-300, 300, nV)[:, None] * (1.1 - 0.5 * zeta[None, :] ** 4)
+    v = rng.uniform(-300, 300, nV)[:, None] * (1.1 - 0.5 * zeta[None, :] ** 4)
+    w = -rng.uniform(-0.2, 0.6, nV)[:, None] * (1.0 - zeta[None, :])
+    stiff = (rng.random(nV) < stiff_frac) & (H >= 10.0)
+    w[stiff] *= stiffness * rng.uniform(0.5, 2.0, stiff.sum())[:, None]
+    gx, gy = rng.normal(0, 2e-3, nV), rng.normal(0, 2e-3, nV)
+    hx, hy = rng.normal(0, 2e-3, nV), rng.normal(0, 2e-3, nV)
+    dzx = (gx[:, None] - zeta[None, :] * hx[:, None]) / Hc[:, None]
+    dzy = (gy[:, None] - zeta[None, :] * hy[:, None]) / Hc[:, None]
+    dzz = np.repeat((-1.0 / Hc)[:, None], nz, axis=1)
+    dzt = (rng.normal(0, 0.05, nV)[:, None] - zeta[None, :] * rng.normal(0, 0.05, nV)[:, None]) / Hc[:, None]
+    udx = rng.normal(0, 2e-3, (nV, nz))
+    vdy = rng.normal(0, 2e-3, (nV, nz))
+    phi = rng.uniform(0, 3000, nV)[:, None] * zeta[None, :] ** 4
+    geo = rng.normal(55.0, 10.0, nV) * 1e-3 * SEC_PER_YEAR
+    fric = np.where(mask == abi.COL_FLOATING, 0.0, rng.uniform(0, 0.05, nV) * SEC_PER_YEAR)
+    cols = dict(Ti=Ti, u_3D=u, v_3D=v, w_3D=w, u_times_dTdxp_upwind=udx, v_times_dTdyp_upwind=vdy, dzeta_dx=dzx,
+                dzeta_dy=dzy, dzeta_dz=dzz, dzeta_dt=dzt, internal_heating=phi, Hi_eff=H, T_surf_annual=T_surf,
+                Q_base_grnd=fric + geo, mask=mask, fraction_gr=rng.uniform(0.0, 1.0, nV), geothermal_heat_flux=geo,
+                SMB=rng.uniform(-0.5, 1.0, nV))
+    return zeta, {k: (np.asfortranarray(v) if isinstance(v, np.ndarray) else v) for k, v in cols.items()}

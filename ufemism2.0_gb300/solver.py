@@ -264,6 +264,32 @@ class VelocitySolver:
         self._check(self.lib.ufe_velocity_download(self.ctx, abi.as_d(u), abi.as_d(v)))
         return u, v
 
+    # -- thermodynamics on this mesh ---------------------------------------------------------
+    def solve_3D_heat_equation(self, fields: dict, params):
+        """solve_3D_heat_equation (thermodynamics_3D_heat_equation.f90:33): the prelude and the
+        column loop on the GPU; returns (Ti_next (nV, nz), n_unstable)."""
+        f, keep = abi.heat_fields(fields)
+        out = np.zeros((self.mesh.nV, self.mesh.nz), order="F")
+        n = C.c_int32()
+        self._check(self.lib.ufe_solve_3D_heat_equation(self.ctx, C.byref(params), C.byref(f), abi.as_d(out),
+                                                        C.byref(n)))
+        return out, n.value
+
+    def heat_upload(self, fields: dict):
+        f, keep = abi.heat_fields(fields)
+        self._check(self.lib.ufe_heat_upload(self.ctx, C.byref(f)))
+
+    def heat_step_resident(self, params, nsteps: int):
+        """Advance the resident temperature nsteps steps; returns (n_unstable_total, device_ms)."""
+        n, ms = C.c_int32(), C.c_double()
+        self._check(self.lib.ufe_heat_step_resident(self.ctx, C.byref(params), nsteps, C.byref(n), C.byref(ms)))
+        return n.value, ms.value
+
+    def heat_download(self):
+        out = np.zeros((self.mesh.nV, self.mesh.nz), order="F")
+        self._check(self.lib.ufe_heat_download(self.ctx, abi.as_d(out)))
+        return out
+
 
 def new_ssa_state(nTri):
     return {"u_b": np.zeros(nTri), "v_b": np.zeros(nTri)}
