@@ -18,6 +18,9 @@ Arms
 
 Multi-GPU (`--gpus N` under torchrun): replicas -- every rank solves its own copy; value is the
 solves of all ranks over the slowest rank's time.
+
+`--workload thermo` measures the batched column thermodynamics instead (200k vertices x 30 layers,
+100 steps of 10 yr per run; column-steps/s), with the same arms.
 """
 from __future__ import annotations
 
@@ -282,6 +285,177 @@ def run_ours(args):
         torch.distributed.destroy_process_group()
 
 
+THERMO_METRIC = "column temperature solves (column-steps)/s, 200k columns x 30 layers, 1xGB300"
+THERMO_UNIT = "column-steps/s"
+THERMO_WORKLOAD = ("batched column thermodynamics: 200k vertices x 30 quadratic zeta layers, 100 steps of 10 yr, "
+                   "15% ice-free columns, floating and grounding-line columns, upwind advection on the mesh")
+
+
+def heat_bytes(nz, n_active, n_inactive):
+    """Algorithmic bytes of one column pass (k_heat_columns on the mesh path): per column with ice
+    the starting temperature, u, v, w, internal heating and the upwind triangle's u_b, v_b per
+    layer (7 reads) and the result (1 write), 10 per-vertex scalars, the ti_up index and the
+    upwind triangle's two operator rows (3 values each, 3 columns, 2 row pointers); per column
+    without ice Hi_eff and T_surf in and the surface temperature out per layer."""
+    active = 8 * nz * 8 + 10 * 8 + 4 + 2 * 3 * 8 + 3 * 4 + 2 * 4
+    inactive = nz * 8 + 2 * 8
+    return n_active * active + n_inactive * inactive
+
+
+def run_thermo(args):
+    import torch
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    pkg = __graft_entry__.load_package()
+    pkg.build()
+    mesh, fields, p = pkg.geometry.thermo_case(seed=0)
+    nsteps = args.thermo_steps
+    solver = pkg.VelocitySolver(mesh, device=local)
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    for _ in range(args.warmup):
+        solver.heat_upload(fields)
+        solver.heat_step_resident(p, nsteps)
+    times, unstable = [], []
+    barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clocks:
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            solver.heat_upload(fields)            # back to the initial temperature, outside the events
+            n, ms = solver.heat_step_resident(p, nsteps)
+            times.append(ms)
+            unstable.append(n)
+        torch.cuda.synchronize()
+        barrier()
+        wall = time.perf_counter() - t0
+    t_rank = sum(times) / 1000.0
+    if world > 1:
+        tt = torch.tensor([t_rank], device=f"cuda:{local}", dtype=torch.float64)
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        t_rank = float(tt.item())
+    value = world * args.steps * nsteps * mesh.nV / t_rank
+
+    # roofline of the column pass
+    solver.heat_upload(fields)
+    us, (n_act, n_inact) = solver.profile_heat_kernels(p, repeats=20)
+    nbytes = heat_bytes(mesh.nz, n_act, n_inact)
+    peaks, peak_kind = measured_peaks()
+    achieved = nbytes / (us[0] * 1e-6) / 1e9
+    traffic = None
+    try:
+        with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
+            traffic = json.load(f).get("k_heat_columns_bytes_per_launch")
+    except OSError:
+        pass
+
+    # end to end: solve_3D_heat_equation with pinned host buffers, one thermodynamics step per call
+    keep, fh = [], {}
+    for k, v in fields.items():
+        fh[k], t = pinned_like(torch, np.asfortranarray(v))
+        keep.append(t)
+    out, t_out = pinned_like(torch, np.zeros((mesh.nV, mesh.nz), order="F"))
+    h2d = sum(v.nbytes for v in fh.values())
+    d2h = out.nbytes
+    solver.solve_3D_heat_equation(fh, p)
+    barrier()
+    torch.cuda.synchronize()
+    n_e2e = max(3, args.steps)
+    t0 = time.perf_counter()
+    for _ in range(n_e2e):
+        T, _ = solver.solve_3D_heat_equation(fh, p)
+    torch.cuda.synchronize()
+    t_e2e = time.perf_counter() - t0
+    e2e_value = world * n_e2e * mesh.nV / t_e2e
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu = thermo_cpu_baseline(pkg, mesh, fields, p, seconds=args.cpu_seconds)
+    if rank == 0:
+        line = {
+            "metric": THERMO_METRIC, "value": round(value, 1), "unit": THERMO_UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(sum(times) / args.steps, 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic fields from seeded smooth random fields on a generated mesh (no files)",
+            "config": {"workload": THERMO_WORKLOAD, "nV": mesh.nV, "nTri": mesh.nTri, "nz": mesh.nz,
+                       "time_steps_per_run": nsteps, "dt_yr": p.dt, "columns_with_ice": int(n_act),
+                       "l2": "inputs larger than L2 (8 arrays of nV x nz doubles per step)",
+                       "parallelism": f"replicas x{world}",
+                       "path": "resident heat state, one column-pass + retry + Robin + bookkeeping launch per step"},
+            "robin_columns_per_run": unstable[0],
+            "e2e": {"value": round(e2e_value, 1), "unit": THERMO_UNIT, "h2d_bytes_per_step": int(h2d),
+                    "d2h_bytes_per_step": int(d2h),
+                    "note": "ufe_solve_3D_heat_equation: one thermodynamics step per call, all fields uploaded"},
+            "roofline": {"bound": "hbm", "kernel": "k_heat_columns<HeatMesh> (prelude + Thomas per column)",
+                         "achieved": round(achieved, 1), "peak": peaks.get("hbm_gbs"), "unit": "GB/s",
+                         "frac": round(achieved / peaks.get("hbm_gbs"), 4), "peak_source": peak_kind,
+                         "traffic": traffic, "algorithmic_bytes_per_launch": int(nbytes),
+                         "us_per_launch": round(float(us[0]), 2),
+                         "step_kernels_us": [round(float(x), 2) for x in us]},
+            "cpu_baseline": cpu,
+            "clocks": clocks.summary(),
+            "gpu_launches": int(4 * nsteps * args.steps),
+            "wall_s_timed": round(wall, 3),
+        }
+        print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def thermo_cpu_baseline(pkg, mesh, fields, params, seconds=15.0, threads=None):
+    """The oracle's solve_3D_heat_equation (OpenMP column loop on all host cores) stepped on the
+    same workload until `seconds` have passed."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    threads = threads or os.cpu_count()
+    os.environ["OMP_NUM_THREADS"] = str(threads)
+    orc = oracle.Oracle(mesh)
+    f = dict(fields)
+    steps, t0 = 0, time.perf_counter()
+    while time.perf_counter() - t0 < seconds and steps < 100:
+        T, n, rc, _ = orc.solve_3D_heat_equation(f, params)
+        f = dict(f, Ti=T)
+        steps += 1
+    elapsed = time.perf_counter() - t0
+    return {"value": round(steps * mesh.nV / elapsed, 1), "unit": THERMO_UNIT, "cores": threads, "kind": "port",
+            "sample": f"{steps} time steps of the same workload in {elapsed:.1f} s"}
+
+
+def run_thermo_reference(args):
+    rank, world, local = dist_env()
+    if rank != 0:
+        return
+    pkg = __graft_entry__.load_package()
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    oracle.build()
+    mesh, fields, p = pkg.geometry.thermo_case(seed=0)
+    vals = []
+    for i in range(args.warmup + args.steps):
+        c = thermo_cpu_baseline(pkg, mesh, fields, p, seconds=args.cpu_seconds)
+        if i >= args.warmup:
+            vals.append(c)
+    v = statistics.mean(c["value"] for c in vals)
+    line = {"metric": THERMO_METRIC, "value": round(v, 1), "unit": THERMO_UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1000.0 * mesh.nV / v, 1),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic fields from seeded smooth random fields on a generated mesh (no files)",
+            "config": {"workload": THERMO_WORKLOAD, "nV": mesh.nV, "nz": mesh.nz},
+            "impl": "reference",
+            "cpu_baseline": {"value": round(v, 1), "unit": THERMO_UNIT, "cores": vals[0]["cores"], "kind": "port",
+                             "sample": vals[0]["sample"]},
+            "e2e": {"value": round(v, 1), "unit": THERMO_UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "note": "the reference is Fortran; this arm times the project's C restatement of its algorithm"}
+    print(json.dumps(line))
+
+
 def cpu_baseline(pkg, mesh, ice, params, full_krylov_its, seconds=20.0, threads=None):
     """Time the oracle (OpenMP on all host cores) on the first Picard iterations of the same solve
     and scale by Krylov iterations to full solves."""
@@ -349,8 +523,13 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--mixed-steps", type=int, default=1,
                     help="solves of the FP32+refinement path measured beside the headline")
+    ap.add_argument("--workload", default="diva", choices=["diva", "thermo"],
+                    help="diva: the headline velocity solve; thermo: the batched column thermodynamics")
+    ap.add_argument("--thermo-steps", type=int, default=100, help="time steps per thermodynamics run")
     args = ap.parse_args()
-    if args.impl == "reference":
+    if args.workload == "thermo":
+        (run_thermo_reference if args.impl == "reference" else run_thermo)(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_ours(args)

@@ -358,6 +358,14 @@ int32_t ufe_heat_step_resident(ufe_ctx *ctx, const ufe_thermo_params *p, int32_t
                                int32_t *n_unstable_total, double *device_ms);
 int32_t ufe_heat_download(ufe_ctx *ctx, double *Ti);
 
+/* Time the kernels of one heat-equation step on the resident state of ufe_heat_upload without
+ * advancing it: each is launched `repeats` times between two CUDA events on the context's stream.
+ * us[0..3] receive the mean microseconds of the column pass, the dt-halving retry pass, the Robin
+ * pass and the end-of-step bookkeeping; counts[0..1] the columns with ice (Hi_eff >= Hi_min_thermo)
+ * and the columns without.  Measurement only; no reference counterpart. */
+int32_t ufe_profile_heat_kernels(ufe_ctx *ctx, const ufe_thermo_params *p, int32_t repeats, double *us,
+                                 int64_t *counts);
+
 /* The tridiagonal d/dzeta and d2/dzeta2 operators of the column solve (calc_zeta_operators_tridiagonal,
  * mesh_zeta.f90:487-605, from calc_vertical_operators_reg_1D, :288-366).  Each array has nz
  * entries indexed by row: *_l[k] couples row k to k-1 (*_l[0] = 0), *_u[k] couples k to k+1

@@ -292,6 +292,8 @@ EXPORTS = {
     "ufe_heat_step_resident": (C.c_int32, [C.c_void_p, C.POINTER(ThermoParams), C.c_int32, iptr, dptr]),
     "ufe_heat_download": (C.c_int32, [C.c_void_p, dptr]),
     "ufe_zeta_operators": (C.c_int32, [C.c_int32, dptr, dptr, dptr, dptr, dptr, dptr, dptr]),
+    "ufe_profile_heat_kernels": (C.c_int32, [C.c_void_p, C.POINTER(ThermoParams), C.c_int32, dptr,
+                                             C.POINTER(C.c_int64)]),
     "ufe_tridiagonal_solve": (C.c_int32, [C.c_void_p, C.c_int32, C.c_int32, dptr, dptr, dptr, dptr, dptr]),
 }
 

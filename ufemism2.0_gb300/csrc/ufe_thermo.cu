@@ -11,8 +11,8 @@
 //   k_heat_columns  all columns with the full dt; columns that fail the stability check
 //                   (NaN, < 180 K, > T0; :226-232) are appended to a retry list;
 //   k_heat_retry    the listed columns with dt/2, dt/4, ... (2^(it-1) substeps, up to 10
-//                   levels, :163-239), each restarting from the profile the last level left;
-//                   columns still unstable go to a second list;
+//                   levels, :163-239), each restarting from the profile the last level left,
+//                   one warp per column; columns still unstable go to a second list;
 //   k_heat_finish   the Robin profile (replace_Ti_with_robin_solution,
 //                   thermodynamics_utilities.f90:256-337) for the listed columns when they are
 //                   fewer than ceil(nV/100), else the step's error flag (:251-290).
@@ -317,43 +317,145 @@ __global__ void __launch_bounds__(128) k_heat_columns(In in, ZOps z, Consts c, V
   }
 }
 
+// The dt-halving retries (:161-239), one warp per listed column.  Per column the row
+// coefficients that do not depend on dt or on the current profile (c_ddzeta, c_d2dzeta2, the
+// off-diagonals, the advection and heating terms) are computed once, one row per lane.  Per dt
+// level the matrix part of the Thomas elimination (w = a / b', b' = b - w c) is done once: it is
+// the same in every substep, so hoisting it changes no value.  Per substep the lanes build the
+// right-hand side in parallel, lane 0 runs the two short recurrences (d' and the back
+// substitution), and the lanes clamp, mix and check the rows in parallel.
+constexpr int kRetryArrays = 14;
+constexpr int kRetryWarps = 1;
+constexpr int kRetryBlocks = 4 * 152;
+
 template <class In>
-__global__ void __launch_bounds__(128) k_heat_retry(In in, ZOps z, Consts c, VertexFields vf, int64_t nV,
-                                                    double *__restrict__ Ti_next, Lists lists, Counters *cnt) {
+__global__ void __launch_bounds__(32 * kRetryWarps) k_heat_retry(In in, ZOps z, Consts c, VertexFields vf,
+                                                                  int64_t nV, double *__restrict__ Ti_next,
+                                                                  Lists lists, Counters *cnt) {
   if (cnt->err) return;
   extern __shared__ double sm[];
-  const int T = blockDim.x;
-  double *Bs = sm + threadIdx.x, *Cs = Bs + z.nz * T, *Ds = Cs + z.nz * T;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int nz = z.nz;
+  double *base = sm + (size_t)warp * kRetryArrays * nz;
+  double *C1 = base, *C2 = C1 + nz, *UDX = C2 + nz, *VDY = UDX + nz, *PHI = VDY + nz, *A = PHI + nz,
+         *Cc = A + nz, *Bp = Cc + nz, *W = Bp + nz, *D = W + nz, *X = D + nz, *PMP = X + nz, *XG = PMP + nz,
+         *XF = XG + nz;
   const int32_t n = cnt->n_retry;
-  for (int32_t j = blockIdx.x * T + threadIdx.x; j < n; j += gridDim.x * T) {
+  const int warps_total = gridDim.x * kRetryWarps;
+  for (int32_t j = blockIdx.x * kRetryWarps + warp; j < n; j += warps_total) {
     const int64_t vi = lists.retry[j];
     const double Hi_eff = __ldg(vf.Hi_eff + vi);
     const double Ts = __ldg(vf.T_surf + vi);
     const int32_t mask = __ldg(vf.mask + vi);
     const double Q = __ldg(vf.Q + vi);
     const double fr = (c.glbc == UFE_GLBC_SUBGRID) ? __ldg(vf.fr + vi) : 0.0;
-    double *cur = lists.scratch + (int64_t)j * z.nz;
-    double *out = Ti_next + vi;
+    const bool two_solves = mask == UFE_COL_GL_GR && c.glbc == UFE_GLBC_SUBGRID;
+    const bool grounded = mask == UFE_COL_GROUNDED || (mask == UFE_COL_GL_GR && c.glbc == UFE_GLBC_GROUNDED);
+    const typename In::Col col = in.col(vi);
+    for (int k = lane; k < nz; k += 32) {
+      const double zk = __ldg(z.zeta + k);
+      PMP[k] = melting_point(Hi_eff, zk);
+      X[k] = Ti_next[(int64_t)k * nV + vi];   // the profile the full-dt solve left (:222)
+      if (k >= 1 && k < nz - 1) {
+        Layer L;
+        in.layer(col, vi, k, zk, L);
+        const double Cpi = heat_capacity(c, L.Ti0);
+        const double Ki = conductivity(c, L.Ti0);
+        const double c1 = L.dzt + (L.u * L.dzx) + (L.v * L.dzy) + (L.w * L.dzz);
+        const double c2 = -(Ki / (kIceDensity * Cpi) * (L.dzz * L.dzz));
+        C1[k] = c1;
+        C2[k] = c2;
+        UDX[k] = L.udx;
+        VDY[k] = L.vdy;
+        PHI[k] = L.phi / (kIceDensity * Cpi);
+        A[k] = (c1 * __ldg(z.l1 + k)) + (c2 * __ldg(z.l2 + k));
+        Cc[k] = (c1 * __ldg(z.u1 + k)) + (c2 * __ldg(z.u2 + k));
+      } else {
+        A[k] = 0.0;    // boundary rows: AA_ldiag / AA_udiag stay zero (:389-391)
+        Cc[k] = 0.0;
+      }
+    }
+    // basal row inputs (grounded flux condition)
+    const int kb = nz - 1;
+    const double pmp_b = melting_point(Hi_eff, __ldg(z.zeta + kb));
+    double Ti0b, dzzb;
+    in.basal(col, vi, kb, __ldg(z.zeta + kb), Ti0b, dzzb);
+    const double Kb = conductivity(c, Ti0b);
+    const double dzeta_b = __ldg(z.zeta + kb) - __ldg(z.zeta + kb - 1);
+    __syncwarp();
     bool found = false;
     for (int it_dt = 2; it_dt <= 10 && !found; ++it_dt) {
-      // the level restarts from the profile the previous level ended with (:161-218)
-      for (int k = 0; k < z.nz; ++k) cur[k] = out[(int64_t)k * nV];
       double half = 1.0;
       for (int i = 1; i < it_dt; ++i) half *= 0.5;   // 0.5**(it_dt-1), exact
-      const double dt_applied = c.dt * half;
+      const double dt = c.dt * half;
+      const double inv_dt = 1.0 / dt;
+      if (lane == 0) {
+        // matrix part of the forward elimination for this dt
+        double bprev = 1.0, cprev = 0.0;
+        Bp[0] = 1.0;
+        for (int k = 1; k < nz - 1; ++k) {
+          double b = inv_dt + (C1[k] * __ldg(z.d1 + k)) + (C2[k] * __ldg(z.d2 + k));
+          const double wgt = A[k] / bprev;
+          b = b - wgt * cprev;
+          W[k] = wgt;
+          Bp[k] = b;
+          bprev = b;
+          cprev = Cc[k];
+        }
+        const double wgt = 0.0 / bprev;
+        W[kb] = wgt;
+        Bp[kb] = 1.0 - wgt * cprev;
+      }
+      __syncwarp();
       const int nsub = 1 << (it_dt - 1);
       bool ok = true;
-      for (int s = 0; s < nsub; ++s) {
-        ok = column_substep(in, z, c, vi, mask, cur, 1, out, nV, dt_applied, Hi_eff, Ts, Q, fr, Bs, Cs, Ds, T);
-        if (s + 1 < nsub)
-          for (int k = 0; k < z.nz; ++k) cur[k] = out[(int64_t)k * nV];
+      for (int sub = 0; sub < nsub; ++sub) {
+        for (int k = lane; k < nz - 1; k += 32)
+          D[k] = (k == 0) ? fmin(Ts, kT0) : X[k] / dt - UDX[k] - VDY[k] + PHI[k];
+        __syncwarp();
+        if (lane == 0) {
+          double dprev = D[0];
+          for (int k = 1; k < nz - 1; ++k) {
+            dprev = D[k] - W[k] * dprev;
+            D[k] = dprev;
+          }
+          // back substitution for one basal value, unclamped x into out[]
+          auto backward = [&](double d_b, double *out) {
+            const double dl = d_b - W[kb] * dprev;
+            double x = dl / Bp[kb];
+            out[kb] = x;
+            for (int k = nz - 2; k >= 0; --k) {
+              x = (D[k] - Cc[k] * x) / Bp[k];
+              out[k] = x;
+            }
+          };
+          const double d_gr = fmin(pmp_b, X[nz - 2] - dzeta_b * Q / (dzzb * Kb));
+          if (two_solves) {
+            backward(pmp_b, XF);
+            backward(d_gr, XG);
+          } else {
+            backward(grounded ? d_gr : pmp_b, XG);
+          }
+        }
+        __syncwarp();
+        bool bad = false;
+        for (int k = lane; k < nz; k += 32) {
+          double v = fmin(XG[k], PMP[k]);
+          if (two_solves) v = fr * v + (1.0 - fr) * fmin(XF[k], PMP[k]);
+          X[k] = v;
+          bad |= unstable_value(v);
+        }
+        ok = !__any_sync(0xffffffffu, bad);
+        __syncwarp();
       }
       found = ok;
     }
-    if (!found) {
+    for (int k = lane; k < nz; k += 32) Ti_next[(int64_t)k * nV + vi] = X[k];
+    if (!found && lane == 0) {
       const int32_t u = atomicAdd(&cnt->n_unstable, 1);
       lists.unstable[u] = (int32_t)vi;
     }
+    __syncwarp();
   }
 }
 
@@ -690,14 +792,15 @@ void launch_step(ufe_ctx *ctx, ThermoWork *t, const In &in, const Consts &c, con
   const ZOps z = zops_of(t);
   const int T = threads_for(z.nz);
   const size_t smem = (size_t)3 * z.nz * T * sizeof(double);
+  const size_t smem_retry = (size_t)kRetryArrays * z.nz * kRetryWarps * sizeof(double);
   UFE_CUDA(cudaFuncSetAttribute(k_heat_columns<In>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  UFE_CUDA(cudaFuncSetAttribute(k_heat_retry<In>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  UFE_CUDA(cudaFuncSetAttribute(k_heat_retry<In>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_retry));
   cudaStream_t s = ctx->stream;
   const unsigned blocks = (unsigned)((nV + T - 1) / T);
   k_heat_columns<In><<<blocks, T, smem, s>>>(in, z, c, vf, nV, Ti_cur, Ti_next, t->lists, t->cnt);
   UFE_CUDA(cudaGetLastError());
-  // the retry list is short: a fixed grid strides over it
-  k_heat_retry<In><<<152, T, smem, s>>>(in, z, c, vf, nV, Ti_next, t->lists, t->cnt);
+  // the retry list is short: a fixed grid of warps (4 per SM) strides over it
+  k_heat_retry<In><<<kRetryBlocks, 32 * kRetryWarps, smem_retry, s>>>(in, z, c, vf, nV, Ti_next, t->lists, t->cnt);
   UFE_CUDA(cudaGetLastError());
   k_heat_finish<<<152, 128, 0, s>>>(z, c, vf, nV, Ti_next, t->lists, t->cnt);
   UFE_CUDA(cudaGetLastError());
@@ -986,6 +1089,79 @@ extern "C" int32_t ufe_heat_step_resident(ufe_ctx *ctx, const ufe_thermo_params 
       *device_ms = ms;
     }
     return rc;
+  });
+}
+
+namespace {
+__global__ void k_count_active(int64_t nV, const double *__restrict__ Hi_eff, double Hi_min,
+                               unsigned long long *count) {
+  const int64_t vi = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const bool active = vi < nV && !(Hi_eff[vi] < Hi_min);
+  const unsigned ballot = __ballot_sync(0xffffffffu, active);
+  if ((threadIdx.x & 31) == 0 && ballot) atomicAdd(count, (unsigned long long)__popc(ballot));
+}
+}  // namespace
+
+extern "C" int32_t ufe_profile_heat_kernels(ufe_ctx *ctx, const ufe_thermo_params *p, int32_t repeats, double *us,
+                                            int64_t *counts) {
+  return guarded(ctx, [&]() -> int32_t {
+    validate_thermo_params(p);
+    UFE_REQUIRE(repeats >= 1 && us, UFE_ERR_INVALID, "heat profile: need repeats >= 1 and us[4]");
+    ThermoWork *t = ctx->thermo;
+    UFE_REQUIRE(t && t->mesh_ready, UFE_ERR_INVALID, "heat profile: call ufe_heat_upload first");
+    UFE_CUDA(cudaSetDevice(ctx->device));
+    cudaStream_t s = ctx->stream;
+    const Consts c = make_consts(p);
+    const VertexFields vf = heat_vertex_fields(t);
+    const HeatMesh in = heat_mesh_inputs(ctx, t, t->Ti[t->cur]);
+    double *out = t->Ti[t->cur ^ 1];
+    const ZOps z = zops_of(t);
+    const int T = threads_for(z.nz);
+    const size_t smem = (size_t)3 * z.nz * T * sizeof(double);
+    const size_t smem_retry = (size_t)kRetryArrays * z.nz * kRetryWarps * sizeof(double);
+    UFE_CUDA(cudaFuncSetAttribute(k_heat_columns<HeatMesh>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    UFE_CUDA(cudaFuncSetAttribute(k_heat_retry<HeatMesh>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)smem_retry));
+    const int64_t nV = t->nV;
+    const unsigned blocks = (unsigned)((nV + T - 1) / T);
+    reset_counters(ctx, t, nV);
+    float ms[4] = {0, 0, 0, 0};
+    for (int which = 0; which < 4; ++which) {
+      UFE_CUDA(cudaEventRecord(ctx->ev0, s));
+      for (int r = 0; r < repeats; ++r) {
+        if (which == 0) {
+          k_heat_columns<HeatMesh><<<blocks, T, smem, s>>>(in, z, c, vf, nV, in.Ti0, out, t->lists, t->cnt);
+        } else if (which == 1) {
+          k_heat_retry<HeatMesh><<<kRetryBlocks, 32 * kRetryWarps, smem_retry, s>>>(in, z, c, vf, nV, out,
+                                                                                      t->lists, t->cnt);
+        } else if (which == 2) {
+          k_heat_finish<<<152, 128, 0, s>>>(z, c, vf, nV, out, t->lists, t->cnt);
+        } else {
+          k_heat_close<<<1, 1, 0, s>>>(t->cnt);
+        }
+        UFE_CUDA(cudaGetLastError());
+        // keep the retry list from growing across repeats of the column pass
+        if (which == 0) UFE_CUDA(cudaMemsetAsync(&t->cnt->n_retry, 0, sizeof(int32_t), s));
+      }
+      UFE_CUDA(cudaEventRecord(ctx->ev1, s));
+      UFE_CUDA(cudaEventSynchronize(ctx->ev1));
+      UFE_CUDA(cudaEventElapsedTime(&ms[which], ctx->ev0, ctx->ev1));
+    }
+    for (int i = 0; i < 4; ++i) us[i] = 1000.0 * ms[i] / repeats;
+    if (counts) {
+      unsigned long long *d = (unsigned long long *)dev_alloc(sizeof(unsigned long long));
+      unsigned long long h = 0;
+      UFE_CUDA(cudaMemsetAsync(d, 0, sizeof(h), s));
+      k_count_active<<<(unsigned)((nV + 255) / 256), 256, 0, s>>>(nV, vf.Hi_eff, c.Hi_min, d);
+      UFE_CUDA(cudaMemcpyAsync(&h, d, sizeof(h), cudaMemcpyDeviceToHost, s));
+      UFE_CUDA(cudaStreamSynchronize(s));
+      dev_free(d);
+      counts[0] = (int64_t)h;
+      counts[1] = nV - (int64_t)h;
+    }
+    reset_counters(ctx, t, nV);
+    UFE_CUDA(cudaStreamSynchronize(s));
+    return UFE_OK;
   });
 }
 

@@ -194,8 +194,8 @@ def _uniform_marginal(f):
 
 def thermo_case(nV=200_000, nz=30, seed=0, corr_len=50e3, thick_corr_len=200e3, dt=10.0):
     """Batched column thermodynamics: a uniform-resolution mesh of about ``nV`` vertices (7 km
-    spacing, so that the explicit horizontal advection keeps u dt / dx < 1; 2,750 km x 2,750 km
-    at 200,000 vertices) with ``nz`` quadratic zeta layers; thickness
+    spacing, so that the explicit horizontal advection keeps u dt / dx < 1;
+    at 200,000 vertices: 2,400 km x 2,400 km) with ``nz`` quadratic zeta layers; thickness
     uniform in [0, 4000] m with 15 % of the columns ice-free (and a taper to zero over the 40 km
     next to the domain border); surface
     temperature uniform in [-50, -10] degC; geothermal flux normal(55, 10) mW m^-2; velocities from
@@ -204,9 +204,9 @@ def thermo_case(nV=200_000, nz=30, seed=0, corr_len=50e3, thick_corr_len=200e3, 
     grounding-line columns between.  Returns (mesh, fields, params): the fields of
     ufe_heat_fields and an abi.ThermoParams with the given dt [yr]."""
     # explicit horizontal advection (calc_upwind_heat_flux_derivatives) needs u dt / dx < 1:
-    # 500 m/yr x 10 yr on a 7 km mesh.  The generator places ~1.3 (L/res)^2 vertices.
+    # 500 m/yr x 10 yr on a 7 km mesh.  The generator places ~1.7 (L/res)^2 vertices.
     res = 7.0e3
-    L = res * np.sqrt(nV / 1.3)
+    L = res * np.sqrt(nV / 1.7)
     mesh = generate_mesh(-L / 2, L / 2, -L / 2, L / 2, lambda x, y: np.full(np.shape(x), res), seed=seed,
                          nz=nz, zeta=quadratic_zeta(nz))
     n = mesh.nV

@@ -285,6 +285,14 @@ class VelocitySolver:
         self._check(self.lib.ufe_heat_step_resident(self.ctx, C.byref(params), nsteps, C.byref(n), C.byref(ms)))
         return n.value, ms.value
 
+    def profile_heat_kernels(self, params, repeats: int = 20):
+        """Mean device time [us] of the column, retry, Robin and bookkeeping kernels of one step on
+        the resident state, plus (columns with ice, columns without)."""
+        us = np.zeros(4)
+        counts = (C.c_int64 * 2)()
+        self._check(self.lib.ufe_profile_heat_kernels(self.ctx, C.byref(params), repeats, abi.as_d(us), counts))
+        return us, (counts[0], counts[1])
+
     def heat_download(self):
         out = np.zeros((self.mesh.nV, self.mesh.nz), order="F")
         self._check(self.lib.ufe_heat_download(self.ctx, abi.as_d(out)))
