@@ -379,6 +379,53 @@ int32_t ufe_zeta_operators(int32_t nz, const double *zeta, double *ddz_l, double
 int32_t ufe_tridiagonal_solve(ufe_ctx *ctx, int32_t n, int32_t nsys, const double *a, const double *b,
                               const double *c, const double *d, double *x);
 
+/* ---- learned Picard start: tensor-core building block ----------------------------------------- */
+/* Y[M x N] = X[M x K] * W[N x K]^T with BF16 X and W (raw 16-bit patterns, row-major) and FP32 Y,
+ * on the tcgen05 tensor cores (one 128-row tile per CTA, accumulator in tensor memory).  M a
+ * multiple of 128, N 64 or 128, K a multiple of 64 up to 256.  The network's layers are built on
+ * the same tile; this entry point exercises it alone.  No reference counterpart. */
+int32_t ufe_umma_gemm_bf16(ufe_ctx *ctx, int32_t M, int32_t N, int32_t K, const uint16_t *X, const uint16_t *W,
+                           float *Y);
+
+/* ---- learned Picard start: the mesh-graph network ---------------------------------------------- */
+/* A network on the triangle b-grid (nodes: triangles, edges: TriC neighbours) that predicts the
+ * velocity a Picard solve starts from.  Width 64: an encoder from 16 per-triangle features, four
+ * message-passing layers h <- h + W2 relu(W1 [h, mean of the neighbours' h] + b1) + b2, and a
+ * linear decoder to (u, v) / 1000 m/yr.  Forward and backward run in hand-written kernels on the
+ * tcgen05 tensor cores (BF16 operands, FP32 accumulation); Adam in FP32.  The solve still iterates
+ * to its own tolerance: the prediction only replaces the zero (or previous-step) start.  No
+ * reference counterpart; it feeds solve_SSA / solve_DIVA (SSA_main.f90:87, DIVA_main.f90:88). */
+typedef struct ufe_gnn ufe_gnn;
+
+int32_t ufe_gnn_param_count(void);
+int32_t ufe_gnn_create(ufe_ctx *ctx, uint64_t seed, ufe_gnn **out);   /* lives on ctx's device/stream;  */
+void    ufe_gnn_destroy(ufe_gnn *g);                                   /* call other ufe_gnn_* only while ctx lives */
+int32_t ufe_gnn_get_params(ufe_gnn *g, float *params);                /* ufe_gnn_param_count() floats */
+int32_t ufe_gnn_set_params(ufe_gnn *g, const float *params);          /* also resets the Adam state   */
+
+/* Explicit graphs (host arrays): n nodes, nbr n x 3 row-major (-1: no neighbour; the adjacency must
+ * be symmetric), x n x 16 features, y / target n x 2, w n loss weights.  loss = sum_i w_i |y_i - t_i|^2;
+ * grad receives its gradient with respect to the parameters. */
+int32_t ufe_gnn_forward(ufe_gnn *g, int64_t n, const int32_t *nbr, const float *x, float *y);
+int32_t ufe_gnn_loss_grad(ufe_gnn *g, int64_t n, const int32_t *nbr, const float *x, const float *target,
+                          const float *w, double *loss, float *grad);
+
+/* The mesh path.  ufe_gnn_features: the 16 features of a mesh context's resident ice state (after
+ * ufe_ice_upload), nTri x 16 in the caller's triangle order; use_prev_velocity = 0 zeroes the
+ * previous-velocity features (a cold start).  ufe_gnn_dataset_add: store one training member on the
+ * device -- the features (given, as taken before the solve, or NULL to take them now with a zero
+ * previous velocity) and the context's resident solution as the target; returns the member count.
+ * ufe_gnn_train: `epochs` passes over the stored members, one Adam step per member.
+ * ufe_gnn_predict_velocity: write the predicted velocity into the context's resident state for a
+ * following resident solve with cold_start = 0. */
+int32_t ufe_gnn_features(ufe_gnn *g, ufe_ctx *mesh_ctx, int32_t use_prev_velocity, float *x);
+int32_t ufe_gnn_dataset_add(ufe_gnn *g, ufe_ctx *mesh_ctx, const float *features_before);
+int32_t ufe_gnn_dataset_clear(ufe_gnn *g);
+int32_t ufe_gnn_train(ufe_gnn *g, int32_t epochs, float lr, uint64_t seed, float *loss_per_epoch,
+                      double *device_ms);
+int32_t ufe_gnn_evaluate(ufe_gnn *g, double *mean_loss);
+int32_t ufe_gnn_predict_velocity(ufe_gnn *g, ufe_ctx *mesh_ctx, int32_t use_prev_velocity, double *device_ms);
+
 /* ---- allocation-free solve -------------------------------------------------------------------- */
 /* The CSR matrix-equation solve of ufe_solve_csr (same BiCGStab/Jacobi, same convergence test)
  * for callers that cannot let a library allocate device memory -- e.g. a host model whose GPU

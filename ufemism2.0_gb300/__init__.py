@@ -10,3 +10,5 @@ from .build import build  # noqa: F401
 from .solver import CSR, UfeError, VelocitySolver, new_diva_state, new_ssa_state  # noqa: F401
 from .thermo import ColumnSolver, zeta_operators  # noqa: F401
 from . import thermo  # noqa: F401
+from . import learned  # noqa: F401
+from .learned import LearnedStart  # noqa: F401

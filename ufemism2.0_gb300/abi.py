@@ -36,6 +36,7 @@ X0_ZERO, X0_CURRENT = 0, 1
 
 dptr = C.POINTER(C.c_double)
 iptr = C.POINTER(C.c_int32)
+fptr = C.POINTER(C.c_float)
 
 
 class MeshDesc(C.Structure):
@@ -295,6 +296,21 @@ EXPORTS = {
     "ufe_profile_heat_kernels": (C.c_int32, [C.c_void_p, C.POINTER(ThermoParams), C.c_int32, dptr,
                                              C.POINTER(C.c_int64)]),
     "ufe_tridiagonal_solve": (C.c_int32, [C.c_void_p, C.c_int32, C.c_int32, dptr, dptr, dptr, dptr, dptr]),
+    "ufe_umma_gemm_bf16": (C.c_int32, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p,
+                                       C.c_void_p]),
+    "ufe_gnn_param_count": (C.c_int32, []),
+    "ufe_gnn_create": (C.c_int32, [C.c_void_p, C.c_uint64, C.POINTER(C.c_void_p)]),
+    "ufe_gnn_destroy": (None, [C.c_void_p]),
+    "ufe_gnn_get_params": (C.c_int32, [C.c_void_p, fptr]),
+    "ufe_gnn_set_params": (C.c_int32, [C.c_void_p, fptr]),
+    "ufe_gnn_forward": (C.c_int32, [C.c_void_p, C.c_int64, iptr, fptr, fptr]),
+    "ufe_gnn_loss_grad": (C.c_int32, [C.c_void_p, C.c_int64, iptr, fptr, fptr, fptr, dptr, fptr]),
+    "ufe_gnn_features": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_int32, fptr]),
+    "ufe_gnn_dataset_add": (C.c_int32, [C.c_void_p, C.c_void_p, fptr]),
+    "ufe_gnn_dataset_clear": (C.c_int32, [C.c_void_p]),
+    "ufe_gnn_train": (C.c_int32, [C.c_void_p, C.c_int32, C.c_float, C.c_uint64, fptr, dptr]),
+    "ufe_gnn_evaluate": (C.c_int32, [C.c_void_p, dptr]),
+    "ufe_gnn_predict_velocity": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_int32, dptr]),
 }
 
 _LIB = None

@@ -140,6 +140,11 @@ void build_operators_gpu(ufe_ctx *ctx);
 // ufe_thermo.cu
 void free_thermo(ufe_ctx *ctx);
 
+// ufe_velocity.cu: the mesh side of the learned Picard start (internal order, on stream s)
+void gnn_mesh_features(ufe_ctx *ctx, cudaStream_t s, int use_prev, float *x, float *mask);
+void gnn_mesh_graph(ufe_ctx *ctx, cudaStream_t s, int32_t *nbr);
+void gnn_mesh_velocity(ufe_ctx *ctx, cudaStream_t s, float *y, bool to_state, const float *mask);
+
 // ufe_layout.cu: internal (Z-order) numbering and the mappings at the ABI boundary
 void layout_upload_mesh(ufe_ctx *ctx, const ufe_mesh_desc *m);
 void free_layout(ufe_ctx *ctx);

@@ -1427,6 +1427,91 @@ static int32_t resident_solve(ufe_ctx *ctx, const ufe_solver_params *p, int32_t 
   return run_picard(ctx, *p, diva, stats);
 }
 
+// ---- learned Picard start: the mesh side ------------------------------------------------------
+// Features per triangle (16 floats) from the resident ice state, in internal order:
+//  0 Hi_b/1e3   1 Hs_b/1e3   2,3 dHs/dx, dHs/dy x100 (clipped to +-10)   4 fraction_gr_b
+//  5 log10(max(beta_sq_b,1)) - 4   6,7 driving stress / 1e5   8,9 previous velocity / 1e3
+//  10,11 local sliding balance (|tau_d| / beta_sq)^3 along tau_d, times fraction_gr_b, / 1e3
+//  12 log10(1 + |that|) / 3   13 ice present (Hi_b > 0)   14,15 zero
+__global__ void k_gnn_features(int nTri, OpRow ab, const double *Hi, const double *Hs, const double *beta_sq,
+                               const double *fgr_b, const double2 *uv, int use_prev, float *x, float *mask) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nTri) return;
+  double Hib = 0.0, Hsb = 0.0, dx = 0.0, dy = 0.0, bb = 0.0;
+  for (int k = ab.ptr[t]; k < ab.ptr[t + 1]; ++k) {
+    const int v = ab.ind[k];
+    Hib += ab.v0[k] * Hi[v];
+    Hsb += ab.v0[k] * Hs[v];
+    dx += ab.v1[k] * Hs[v];
+    dy += ab.v2[k] * Hs[v];
+    if (beta_sq) bb += ab.v0[k] * beta_sq[v];
+  }
+  const double tx = -kIceDensity * kGrav * Hib * dx, ty = -kIceDensity * kGrav * Hib * dy;
+  const double tau = sqrt(tx * tx + ty * ty);
+  const double fg = fgr_b[t];
+  double usl = fg * pow(tau / fmax(bb, 1.0), 3.0);
+  usl = fmin(usl, 1e4);
+  const double ux = tau > 0.0 ? usl * tx / tau : 0.0, uy = tau > 0.0 ? usl * ty / tau : 0.0;
+  float *o = x + t * 16;
+  o[0] = (float)(Hib / 1e3);
+  o[1] = (float)(Hsb / 1e3);
+  o[2] = (float)fmax(-10.0, fmin(10.0, dx * 100.0));
+  o[3] = (float)fmax(-10.0, fmin(10.0, dy * 100.0));
+  o[4] = (float)fg;
+  o[5] = (float)(log10(fmax(bb, 1.0)) - 4.0);
+  o[6] = (float)(tx / 1e5);
+  o[7] = (float)(ty / 1e5);
+  o[8] = use_prev ? (float)(uv[t].x / 1e3) : 0.f;
+  o[9] = use_prev ? (float)(uv[t].y / 1e3) : 0.f;
+  o[10] = (float)(ux / 1e3);
+  o[11] = (float)(uy / 1e3);
+  o[12] = (float)(log10(1.0 + usl) / 3.0);
+  o[13] = Hib > 0.0 ? 1.f : 0.f;
+  o[14] = 0.f;
+  o[15] = 0.f;
+  if (mask) mask[t] = Hib > 0.0 ? 1.f : 0.f;
+}
+
+__global__ void k_gnn_graph(int nTri, const int32_t *TriC, int32_t *nbr) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nTri) return;
+  for (int q = 0; q < 3; ++q) nbr[t * 3 + q] = TriC[(int64_t)q * nTri + t] - 1;   // 1-based, 0: none
+}
+
+__global__ void k_gnn_velocity(int nTri, double2 *uv, float *y, int to_state, const float *mask) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nTri) return;
+  if (to_state) {
+    const bool ice = !mask || mask[t] > 0.f;
+    uv[t] = ice ? make_double2((double)y[2 * t] * 1e3, (double)y[2 * t + 1] * 1e3) : make_double2(0.0, 0.0);
+  } else {
+    y[2 * t] = (float)(uv[t].x / 1e3);
+    y[2 * t + 1] = (float)(uv[t].y / 1e3);
+  }
+}
+
+void gnn_mesh_features(ufe_ctx *ctx, cudaStream_t s, int use_prev, float *x, float *mask) {
+  Work *w = ctx->work;
+  UFE_REQUIRE(w, UFE_ERR_INVALID, "learned start: upload the ice state first");
+  const DevCSR &mab = ctx->ops[UFE_OP_MAP_A_B];
+  OpRow ab{mab.ptr, mab.ind, mab.val, ctx->ops[UFE_OP_DDX_A_B].val, ctx->ops[UFE_OP_DDY_A_B].val};
+  k_gnn_features<<<(ctx->nTri + 255) / 256, 256, 0, s>>>(ctx->nTri, ab, w->Hi, w->Hs, w->beta_sq, w->fgr_b, w->uv,
+                                                          use_prev, x, mask);
+  UFE_CUDA(cudaGetLastError());
+}
+
+void gnn_mesh_graph(ufe_ctx *ctx, cudaStream_t s, int32_t *nbr) {
+  k_gnn_graph<<<(ctx->nTri + 255) / 256, 256, 0, s>>>(ctx->nTri, ctx->TriC, nbr);
+  UFE_CUDA(cudaGetLastError());
+}
+
+void gnn_mesh_velocity(ufe_ctx *ctx, cudaStream_t s, float *y, bool to_state, const float *mask) {
+  Work *w = ctx->work;
+  UFE_REQUIRE(w, UFE_ERR_INVALID, "learned start: upload the ice state first");
+  k_gnn_velocity<<<(ctx->nTri + 255) / 256, 256, 0, s>>>(ctx->nTri, w->uv, y, to_state ? 1 : 0, mask);
+  UFE_CUDA(cudaGetLastError());
+}
+
 extern "C" int32_t ufe_solve_ssa_resident(ufe_ctx *ctx, const ufe_solver_params *p, int32_t cold_start,
                                           ufe_solve_stats *stats) {
   return guarded(ctx, [&]() -> int32_t { return resident_solve(ctx, p, cold_start, false, stats); });

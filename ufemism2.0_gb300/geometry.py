@@ -316,3 +316,51 @@ def random_columns(nV, nz, seed=0, stiff_frac=0.0, stiffness=300.0):
                 Q_base_grnd=fric + geo, mask=mask, fraction_gr=rng.uniform(0.0, 1.0, nV), geothermal_heat_flux=geo,
                 SMB=rng.uniform(-0.5, 1.0, nV))
     return zeta, {k: (np.asfortranarray(v) if isinstance(v, np.ndarray) else v) for k, v in cols.items()}
+
+
+# ---- learned-start ensemble (config 3) --------------------------------------------------------
+def grounded_fraction_b_vertex(mesh, taf, nsub=6):
+    """grounded_fraction_b with the thickness above flotation given at vertices (linear within
+    each triangle)."""
+    a, b, c = _tri_vertices(mesh)
+    cnt = np.zeros(mesh.nTri)
+    npts = 0
+    for i in range(nsub):
+        for j in range(nsub - i):
+            l1 = (i + 1 / 3) / nsub
+            l2 = (j + 1 / 3) / nsub
+            cnt += (l1 * taf[a] + l2 * taf[b] + (1 - l1 - l2) * taf[c]) > 0
+            npts += 1
+    return np.ascontiguousarray(cnt / npts)
+
+
+def ensemble_mesh(nV=30_000, L=1500e3, seed=0, nz=12):
+    """One mesh of about nV vertices (uniform resolution) over an L x L domain."""
+    res = L / np.sqrt(nV / 1.7)
+    return generate_mesh(-L / 2, L / 2, -L / 2, L / 2, lambda x, y: np.full(np.shape(x), res), seed=seed, nz=nz)
+
+
+def ensemble_member(mesh, member, A=1e-16, H0=3000.0, R=600e3, bed_sigma=400.0, bed_corr=20e3,
+                    beta_mu=np.log(1e4), beta_sigma=0.5, beta_corr=50e3):
+    """Geometry `member` of the learned-start ensemble on `mesh`: bed -200 m plus a Gaussian random
+    field (sigma 400 m, correlation 20 km, seeded by the member), the dome thickness of config 0
+    with R = 600 km, floating where the ice is thinner than flotation (sea level 0), and a
+    log-normal friction coefficient beta^2 (log-mean ln 1e4, log-sd 0.5, correlation 50 km).
+    Returns (ice, params) for an SSA solve (Weertman m = 3, n = 3, A = 1e-16, Picard 1e-4,
+    BiCGStab 1e-8)."""
+    x, y = mesh.V[:, 0], mesh.V[:, 1]
+    bed = -200.0 + bed_sigma * smooth_field(x, y, bed_corr, 1000 + member)
+    Hi = np.ascontiguousarray(dome_thickness(x, y, H0=H0, R=R))
+    SL = np.zeros(mesh.nV)
+    taf = thickness_above_flotation(Hi, bed, SL)
+    Hs = np.ascontiguousarray(surface_elevation(Hi, bed, SL))
+    grounded = (Hi > 0) & (taf > 0)
+    fgr = grounded_fraction_b_vertex(mesh, np.where(Hi > 0, taf, -1.0))
+    beta_sq = np.exp(beta_mu + beta_sigma * smooth_field(x, y, beta_corr, 2000 + member))
+    ice = dict(Hi=Hi, Hs=Hs, Hb=bed, SL=SL,
+               A_flow=np.asfortranarray(np.full((mesh.nV, mesh.nz), A)),
+               fraction_gr_b=fgr, mask_grounded_ice=np.ascontiguousarray(grounded.astype(np.int32)),
+               beta_sq=np.ascontiguousarray(beta_sq))
+    params = abi.default_params(choice_sliding_law="Weertman", slid_Weertman_m=3.0,
+                                visc_it_norm_dUV_tol=1e-4, stress_balance_PETSc_rtol=1e-8)
+    return ice, params

@@ -82,6 +82,8 @@ class VelocitySolver:
 
     # -- plumbing ----------------------------------------------------------------------------
     def close(self):
+        for child in list(getattr(self, "_children", [])):   # networks created on this context first
+            child.close()
         if getattr(self, "ctx", None):
             self.lib.ufe_ctx_destroy(self.ctx)
             self.ctx = None

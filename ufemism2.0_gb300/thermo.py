@@ -49,6 +49,8 @@ class ColumnSolver:
         self.ctx = ctx
 
     def close(self):
+        for child in list(getattr(self, "_children", [])):   # networks created on this context first
+            child.close()
         if getattr(self, "ctx", None):
             self.lib.ufe_ctx_destroy(self.ctx)
             self.ctx = None
