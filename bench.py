@@ -409,6 +409,115 @@ def run_thermo(args):
         torch.distributed.destroy_process_group()
 
 
+LEARNED_WORKLOAD = ("learned Picard start, SSA ensemble: 30k-vertex mesh over 1500 km x 1500 km, bed -200 m + "
+                    "GRF(400 m, 20 km), dome R = 600 km, floating below flotation, log-normal beta^2; 256 training "
+                    "and 32 held-out geometries; Weertman m = 3, Picard 1e-4, BiCGStab/Jacobi 1e-8")
+
+
+def run_learned(args):
+    """Config 3: data from plain FP64 GPU solves, GPU training, held-out solves from the learned start."""
+    import torch
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    pkg = __graft_entry__.load_package()
+    pkg.build()
+    mesh = pkg.geometry.ensemble_mesh(nV=args.learned_nv, seed=0)
+    T = mesh.Tri - 1
+    train_ids = range(args.learned_train)
+    test_ids = range(100000, 100000 + args.learned_test)
+    p32_of = lambda p: _with(pkg, p, precision=pkg.abi.PREC_FP32_REFINE)
+    out = {}
+    with pkg.VelocitySolver(mesh, device=local) as s:
+        net = pkg.LearnedStart(s, seed=1)
+        gen_ms, gen_its = 0.0, []
+        t0 = time.perf_counter()
+        for m in train_ids:
+            ice, p = pkg.geometry.ensemble_member(mesh, m)
+            s.ice_upload(ice)
+            x = net.features(s)
+            st = s.solve_resident(p, diva=False, cold_start=True)
+            gen_ms += st["device_ms"]
+            gen_its.append((st["n_visc_its"], st["n_Axb_its"]))
+            net.dataset_add(s, x)
+            if m % 16 == 0:
+                print(f"training solve {m}: {st['n_visc_its']} Picard, {st['n_Axb_its']} Krylov, "
+                      f"{st['device_ms']:.0f} ms", file=sys.stderr, flush=True)
+        gen_wall = time.perf_counter() - t0
+        losses, train_ms = net.train(epochs=args.learned_epochs, lr=args.learned_lr)
+        net.dataset_clear()
+        rows = {"cold_fp64": [], "learned_fp64": [], "learned_fp32": []}
+        errs = {"cold_fp64": [], "learned_fp64": [], "learned_fp32": []}
+        pred_ms = []
+        with ClockSampler(local) as clocks:
+            for m in test_ids:
+                ice, p = pkg.geometry.ensemble_member(mesh, m)
+                on_ice = (ice["Hi"][T] > 0).all(axis=1)
+                sel = np.r_[on_ice, on_ice]
+                s.ice_upload(ice)
+                st = s.solve_resident(p, diva=False, cold_start=True)
+                rows["cold_fp64"].append(st)
+                uc = np.r_[s.velocity_download()]
+                ut = None
+                if len(errs["cold_fp64"]) < args.learned_err_members:
+                    # reference for the errors: the same solve continued to 1e-8
+                    tight = _with(pkg, p, visc_it_norm_dUV_tol=1e-8, visc_it_nit=400)
+                    try:
+                        s.solve_resident(tight, diva=False, cold_start=False)
+                    except pkg.UfeError:   # divergence control near round-off: settle for 1e-6
+                        s.ice_upload(ice)
+                        s.solve_resident(_with(pkg, p, visc_it_norm_dUV_tol=1e-6, visc_it_nit=400), diva=False)
+                    ut = np.r_[s.velocity_download()]
+                    errs["cold_fp64"].append(np.linalg.norm((uc - ut)[sel]) / np.linalg.norm(ut[sel]))
+                for key, pp in (("learned_fp64", p), ("learned_fp32", p32_of(p))):
+                    pred_ms.append(net.predict(s))
+                    st = s.solve_resident(pp, diva=False, cold_start=False)
+                    rows[key].append(st)
+                    if ut is not None:
+                        u = np.r_[s.velocity_download()]
+                        errs[key].append(np.linalg.norm((u - ut)[sel]) / np.linalg.norm(ut[sel]))
+                print(f"held-out {m}: cold {rows['cold_fp64'][-1]['n_visc_its']} learned "
+                      f"{rows['learned_fp64'][-1]['n_visc_its']} / {rows['learned_fp32'][-1]['n_visc_its']}",
+                      file=sys.stderr, flush=True)
+        net.close()
+    n = len(test_ids)
+    mean_pred = float(np.mean(pred_ms))
+    def rate(key, extra_ms=0.0):
+        return n / ((sum(r["device_ms"] for r in rows[key]) + n * extra_ms) / 1000.0)
+    vals = {"cold_fp64": rate("cold_fp64"), "learned_fp64": rate("learned_fp64", mean_pred),
+            "learned_fp32": rate("learned_fp32", mean_pred)}
+    best = max(("learned_fp64", "learned_fp32"), key=lambda k: vals[k])
+    peaks, peak_kind = measured_peaks()
+    line = {
+        "metric": METRIC, "value": round(vals[best], 4), "unit": UNIT, "n_gpus": world, "steps": n, "warmup": 0,
+        "ms_per_step": round(1000.0 / vals[best], 3), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64 (network bf16)",
+        "data": "synthetic ensemble geometries from seeded random fields on a generated mesh (no files)",
+        "config": {"workload": LEARNED_WORKLOAD, "nV": mesh.nV, "nTri": mesh.nTri,
+                   "train": len(train_ids), "held_out": n, "epochs": args.learned_epochs, "path": best},
+        "speedup_vs_plain_fp64": round(vals[best] / vals["cold_fp64"], 3),
+        "paths": {k: {"value": round(vals[k], 4), "unit": UNIT,
+                      "picard_its_mean": float(np.mean([r["n_visc_its"] for r in rows[k]])),
+                      "krylov_its_mean": float(np.mean([r["n_Axb_its"] for r in rows[k]])),
+                      "rel_l2_vs_tight_solve_mean": float(np.mean(errs[k])),
+                      "rel_l2_vs_tight_solve_max": float(np.max(errs[k]))} for k in rows},
+        "network": {"inference_ms_mean": round(mean_pred, 3), "train_ms": round(train_ms, 1),
+                    "loss_first_last": [float(losses[0]), float(losses[-1])], "params": int(net.nparams)},
+        "data_generation": {"solves": len(train_ids), "device_s": round(gen_ms / 1000.0, 2),
+                            "wall_s": round(gen_wall, 1),
+                            "picard_its_mean": float(np.mean([a for a, b in gen_its]))},
+        "clocks": clocks.summary(),
+    }
+    print(json.dumps(line))
+
+
+def _with(pkg, p, **kw):
+    q = pkg.abi.default_params(**{f: getattr(p, f) for f, _ in p._fields_ if f != "reserved"})
+    for k, v in kw.items():
+        setattr(q, k, v)
+    return q
+
+
 def thermo_cpu_baseline(pkg, mesh, fields, params, seconds=15.0, threads=None):
     """The oracle's solve_3D_heat_equation (OpenMP column loop on all host cores) stepped on the
     same workload until `seconds` have passed."""
@@ -523,12 +632,22 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--mixed-steps", type=int, default=1,
                     help="solves of the FP32+refinement path measured beside the headline")
-    ap.add_argument("--workload", default="diva", choices=["diva", "thermo"],
-                    help="diva: the headline velocity solve; thermo: the batched column thermodynamics")
+    ap.add_argument("--workload", default="diva", choices=["diva", "thermo", "learned"],
+                    help="diva: the headline velocity solve; thermo: the batched column thermodynamics; "
+                         "learned: the learned Picard start on the SSA ensemble")
+    ap.add_argument("--learned-nv", type=int, default=30000)
+    ap.add_argument("--learned-train", type=int, default=256)
+    ap.add_argument("--learned-test", type=int, default=32)
+    ap.add_argument("--learned-epochs", type=int, default=40)
+    ap.add_argument("--learned-lr", type=float, default=2e-3)
+    ap.add_argument("--learned-err-members", type=int, default=8,
+                    help="held-out members also solved to 1e-8 as the reference for the velocity errors")
     ap.add_argument("--thermo-steps", type=int, default=100, help="time steps per thermodynamics run")
     args = ap.parse_args()
     if args.workload == "thermo":
         (run_thermo_reference if args.impl == "reference" else run_thermo)(args)
+    elif args.workload == "learned":
+        run_learned(args)
     elif args.impl == "reference":
         run_reference(args)
     else:

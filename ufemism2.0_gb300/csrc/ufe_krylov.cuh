@@ -390,3 +390,226 @@ inline unsigned krylov_grid(const M &mat, int threads, int max_blocks) {
   if (b < 1) b = 1;
   return (unsigned)b;
 }
+
+// ---- persistent BiCGStab: the whole iteration loop in one (co-resident) launch ----------------
+// The same recurrence as k_p_spmv / k_s_spmv / k_xr, with the launches replaced by grid
+// barriers.  After each phase every block writes its partial sums; after the barrier every block
+// sums all blocks' partials in the same fixed order, so all blocks hold identical scalars and
+// take identical decisions without another round trip.  The barrier's spin is bounded: a block
+// that waits too long records the failure and every block leaves the loop.
+constexpr int kPersistMaxBlocks = 8 * 152;
+constexpr int kPersistSlots = 3;     // partial sums per block per phase
+
+struct GridSync {
+  unsigned int count;
+  unsigned int gen;
+  int err;
+  int pad;
+};
+
+__device__ __forceinline__ unsigned int ld_acquire_u32(const unsigned int *p) {
+  unsigned int v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+// false (block-uniform) when the wait gave up
+__device__ __forceinline__ bool grid_barrier(GridSync *gs, unsigned int &gen) {
+  __shared__ int ok_s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int ok = 1;
+    const unsigned int my = gen;
+    __threadfence();
+    if (atomicAdd(&gs->count, 1u) == gridDim.x - 1) {
+      atomicExch(&gs->count, 0u);
+      __threadfence();
+      atomicAdd(&gs->gen, 1u);
+    } else {
+      long long spins = 0;
+      while (ld_acquire_u32(&gs->gen) == my) {
+        if (++spins > (1ll << 26) || *((volatile int *)&gs->err)) {
+          ok = 0;
+          atomicExch(&gs->err, 1);
+          break;
+        }
+      }
+    }
+    __threadfence();
+    gen = my + 1;
+    ok_s = ok;
+  }
+  __syncthreads();
+  return ok_s != 0;
+}
+
+// block sum of NP values (fixed tree), written by thread 0 to part[blockIdx.x * NP + k]
+template <int NP>
+__device__ __forceinline__ void block_partials(double *acc, double *part) {
+  __shared__ double red[NP][32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+  for (int k = 0; k < NP; ++k) {
+    double v = acc[k];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (lane == 0) red[k][warp] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < 32) {
+#pragma unroll
+    for (int k = 0; k < NP; ++k) {
+      double v = lane < nw ? red[k][lane] : 0.0;
+      for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+      if (lane == 0) part[(int64_t)blockIdx.x * NP + k] = v;
+    }
+  }
+}
+
+// every block: the sum over all blocks' partials in one fixed order (warp 0; broadcast)
+template <int NP>
+__device__ __forceinline__ void all_partials(const double *part, double *tot) {
+  __shared__ double res[NP];
+  if (threadIdx.x < 32) {
+    const int lane = threadIdx.x;
+#pragma unroll
+    for (int k = 0; k < NP; ++k) {
+      double v = 0.0;
+      for (int b = lane; b < (int)gridDim.x; b += 32) v += __ldcg(part + (int64_t)b * NP + k);
+      for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+      if (lane == 0) res[k] = v;
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int k = 0; k < NP; ++k) tot[k] = res[k];
+}
+
+// Starts from the state k_krylov_init / k_inner_init left in *ks (and P[0], V[0]); runs until the
+// scalars stop the solve; leaves x, r, the counters and the status as the three-kernel loop does.
+template <class M>
+__global__ void __launch_bounds__(256) k_bicgstab_persist(M mat, KV<typename M::Vec> v, KrylovScalars *ks,
+                                                          double *part, GridSync *gs) {
+  using Vec = typename M::Vec;
+  using R = typename ScalarOf<Vec>::T;
+  KrylovScalars s = *ks;
+  if (!s.active) return;
+  double *partP = part, *partS = part + kPersistMaxBlocks * kPersistSlots,
+         *partX = part + 2 * kPersistMaxBlocks * kPersistSlots;
+  unsigned int gen = ld_acquire_u32(&gs->gen);
+  const int lane0 = threadIdx.x % M::kLanes;
+  const int64_t gstride = ((int64_t)gridDim.x * blockDim.x) / M::kLanes;
+  const int64_t nrows_pad = ((mat.items + gstride - 1) / gstride) * gstride;
+  const int64_t row0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / M::kLanes;
+  bool ok = true;
+  while (s.active) {
+    const int cur = s.it & 1, nxt = cur ^ 1;
+    // -- p <- r - beta omega v + beta p;  v <- D^-1 A p;  (v, r^)
+    {
+      const R beta = (R)s.beta, bw = (R)(s.beta * s.omegaold);
+      const Vec *__restrict__ Po = v.P[cur];
+      const Vec *__restrict__ Vo = v.V[cur];
+      const Vec *__restrict__ Rr = v.R;
+      double acc[1] = {0.0};
+      for (int64_t i64 = row0; i64 < nrows_pad; i64 += gstride) {
+        const int i = (int)i64;
+        const bool live = i < mat.items;
+        Vec pt = live ? mat.row_partial(i, lane0, [&](int j) { return v_pupd(Rr[j], bw, Vo[j], beta, Po[j]); })
+                      : v_zero<Vec>();
+        Vec y = lane_reduce<M::kLanes>(pt);
+        if (live && lane0 == 0) {
+          v.P[nxt][i] = v_pupd(Rr[i], bw, Vo[i], beta, Po[i]);
+          const Vec vn = v_mul(v.dinv[i], y);
+          v.V[nxt][i] = vn;
+          acc[0] += v_dot(vn, v.RP[i]);
+        }
+      }
+      block_partials<1>(acc, partP);
+      if (!(ok = grid_barrier(gs, gen))) break;
+      double tot[1];
+      all_partials<1>(partP, tot);
+      const double d1 = tot[0];
+      if (d1 == 0.0 || isnan(d1)) {
+        s.status = isnan(d1) ? UFE_ERR_NAN : UFE_ERR_DIVERGED;
+        s.active = 0;
+        break;
+      }
+      s.alpha = s.rho / d1;
+    }
+    // -- s <- r - alpha v;  t <- D^-1 A s;  (s,t), (t,t), (s,s)
+    {
+      const R alpha = (R)s.alpha;
+      const Vec *__restrict__ Vn = v.V[nxt];
+      const Vec *__restrict__ Rr = v.R;
+      double acc[3] = {0.0, 0.0, 0.0};
+      for (int64_t i64 = row0; i64 < nrows_pad; i64 += gstride) {
+        const int i = (int)i64;
+        const bool live = i < mat.items;
+        Vec pt = live ? mat.row_partial(i, lane0, [&](int j) { return v_sub_scaled(Rr[j], alpha, Vn[j]); })
+                      : v_zero<Vec>();
+        Vec y = lane_reduce<M::kLanes>(pt);
+        if (live && lane0 == 0) {
+          const Vec si = v_sub_scaled(Rr[i], alpha, Vn[i]);
+          const Vec ti = v_mul(v.dinv[i], y);
+          v.S[i] = si;
+          v.T[i] = ti;
+          acc[0] += v_dot(si, ti);
+          acc[1] += v_dot(ti, ti);
+          acc[2] += v_dot(si, si);
+        }
+      }
+      block_partials<3>(acc, partS);
+      if (!(ok = grid_barrier(gs, gen))) break;
+      double tot[3];
+      all_partials<3>(partS, tot);
+      if (tot[1] == 0.0) {
+        if (tot[2] != 0.0) { s.status = UFE_ERR_DIVERGED; s.active = 0; break; }
+        s.omega = 0.0;
+        s.tbreak = 1;
+      } else if (isnan(tot[1])) {
+        s.status = UFE_ERR_NAN;
+        s.active = 0;
+        break;
+      } else {
+        s.omega = tot[0] / tot[1];
+      }
+    }
+    // -- x <- x + alpha p + omega s;  r <- s - omega t;  (r, r^), (r, r)
+    {
+      const R alpha = (R)s.alpha, omega = (R)s.omega;
+      double acc[2] = {0.0, 0.0};
+      const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+      for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < mat.items; i += stride) {
+        const Vec pi = v.P[nxt][i], si = v.S[i], ti = v.T[i];
+        v.X[i] = v_xupd(v.X[i], alpha, pi, omega, si);
+        const Vec ri = v_sub_scaled(si, omega, ti);
+        v.R[i] = ri;
+        acc[0] += v_dot(ri, v.RP[i]);
+        acc[1] += v_dot(ri, ri);
+      }
+      block_partials<2>(acc, partX);
+      if (!(ok = grid_barrier(gs, gen))) break;
+      double tot[2];
+      all_partials<2>(partX, tot);
+      s.it += 1;
+      s.total_its += 1;
+      const double dp = sqrt(tot[1]);
+      s.dp = dp;
+      const double rho_new = tot[0];
+      s.rhoold = s.rho;
+      s.omegaold = s.omega;
+      s.rho = rho_new;
+      if (s.tbreak) { s.active = 0; s.status = UFE_OK; s.dp = 0.0; }
+      else if (isnan(dp)) { s.status = UFE_ERR_NAN; s.active = 0; }
+      else if (dp <= s.ttol) { s.active = 0; }
+      else if (dp >= 1e4 * s.rnorm0) { s.status = UFE_ERR_DIVERGED; s.active = 0; }
+      else if (s.it >= s.max_it) { s.status = UFE_WARN_KRYLOV_MAXIT; s.active = 0; }
+      else if (rho_new == 0.0) { s.status = UFE_ERR_DIVERGED; s.active = 0; }
+      else s.beta = (s.rho / s.rhoold) * (s.alpha / s.omegaold);
+    }
+  }
+  if (!ok) {
+    s.status = UFE_ERR_DEVICE;
+    s.active = 0;
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) *ks = s;
+}

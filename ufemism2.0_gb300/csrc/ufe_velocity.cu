@@ -477,7 +477,9 @@ __global__ void k_assemble(AssembleArgs a, PhysParams q, CondArg cond) {
 __global__ void k_inner_init(int nTri, const double2 *R, float2 *R32, float2 *RP32, float2 *x32,
                              float2 *P32, float2 *V32, const KrylovScalars *outer, KrylovScalars *ksi,
                              double inner_rtol, int max_it, double *partials, unsigned int *tickets,
-                             CondArg cond) {
+                             CondArg cond, GridSync *gsync) {
+  // reset the persistent solve's grid barrier (nothing else uses it now)
+  if (gsync && blockIdx.x == 0 && threadIdx.x == 0) *gsync = GridSync{0u, 0u, 0, 0};
   double acc[1] = {0.0};
   int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < nTri; t += stride) {
@@ -849,6 +851,8 @@ Work *ensure_work(ufe_ctx *ctx) {
   w->beta_eff_a = alloc_n<double>(nV);
   w->F2a1 = alloc_n<double>(nV);
   w->eta_3D_a = alloc_n<double>((size_t)nV * nz);
+  w->ppart = alloc_n<double>((size_t)3 * kPersistMaxBlocks * kPersistSlots);
+  w->gsync = alloc_n<GridSync>(1);
   w->F1_3D_a = alloc_n<double>((size_t)nV * nz);
   w->N_b_in = alloc_n<double>(nTri);
   w->dNx_b_in = alloc_n<double>(nTri);
@@ -884,7 +888,7 @@ void free_work(ufe_ctx *ctx) {
                   w->eta_3D_b, w->bfc_b, w->F2b1, w->beta_b, w->Hi, w->Hs, w->Avav, w->A_flow, w->beta_sq,
                   w->alpha_sq, w->effp, w->tys, w->mask_gr, w->N_a, w->beta_a, w->beta_eff_a, w->F2a1,
                   w->eta_3D_a, w->F1_3D_a, w->N_b_in, w->dNx_b_in, w->dNy_b_in, w->beta_b_in, w->ks,
-                  w->ps, w->err};
+                  w->ps, w->err, w->ppart, w->gsync};
   for (void *p : ptrs) dev_free(p);
   if (w->ks_host) cudaFreeHost(w->ks_host);
   if (w->ps_host) cudaFreeHost(w->ps_host);
@@ -908,12 +912,36 @@ int32_t bsr_lanes(ufe_ctx *ctx) {
 
 namespace {
 
+// The FP32 inner BiCGStab runs as one persistent launch unless UFE_NO_PERSIST=1.
+bool persistent_krylov() {
+  static int v = -1;
+  if (v < 0) {
+    const char *e = getenv("UFE_NO_PERSIST");
+    v = (e && *e && *e != '0') ? 0 : 1;
+  }
+  return v == 1;
+}
+
+// Blocks of 256 threads for a persistent kernel: all co-resident, at most kPersistMaxBlocks,
+// no more than the rows need.
+unsigned persist_blocks(const void *kernel, int64_t lanes_total) {
+  int dev = 0, sms = 0, per_sm = 0;
+  UFE_CUDA(cudaGetDevice(&dev));
+  UFE_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  UFE_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, 256, 0));
+  int64_t nb = (int64_t)std::max(per_sm, 1) * sms;
+  nb = std::min<int64_t>(nb, kPersistMaxBlocks);
+  nb = std::min<int64_t>(nb, (lanes_total + 255) / 256);
+  return (unsigned)std::max<int64_t>(nb, 1);
+}
+
 struct Solver {
   ufe_ctx *ctx;
   Work *w;
   ufe_solver_params p;
   PhysParams q;
   int grid, lanes;
+  unsigned persist_grid = 1;   // co-resident blocks of the persistent Krylov kernel
   OpRow ab, ba;
   cudaStream_t s;
 
@@ -923,6 +951,12 @@ struct Solver {
     grid = max_grid(ctx);
     lanes = bsr_lanes(ctx);
     s = ctx->stream;
+    switch (lanes) {
+      case 1: persist_grid = persist_blocks(reinterpret_cast<const void *>(k_bicgstab_persist<BsrDiffMat<1>>), 1ll << 40); break;
+      case 2: persist_grid = persist_blocks(reinterpret_cast<const void *>(k_bicgstab_persist<BsrDiffMat<2>>), 1ll << 40); break;
+      case 8: persist_grid = persist_blocks(reinterpret_cast<const void *>(k_bicgstab_persist<BsrDiffMat<8>>), 1ll << 40); break;
+      default: persist_grid = persist_blocks(reinterpret_cast<const void *>(k_bicgstab_persist<BsrDiffMat<4>>), 1ll << 40); break;
+    }
     const DevCSR &mab = ctx->ops[UFE_OP_MAP_A_B];
     ab = OpRow{mab.ptr, mab.ind, mab.val, ctx->ops[UFE_OP_DDX_A_B].val, ctx->ops[UFE_OP_DDY_A_B].val};
     const DevCSR &mba = ctx->ops[UFE_OP_MAP_B_A];
@@ -1026,8 +1060,43 @@ struct Solver {
   void enqueue_inner_init(CondArg c) {
     k_inner_init<<<eblocks(w->nTri), kThreads, 0, s>>>(
         w->nTri, w->kv.R, w->kv.R32, w->kv.RP32, w->kv.x32, w->kv.P32[0], w->kv.V32[0], w->ks, w->ks + 1,
-        p.krylov_inner_rtol, p.krylov_max_it, ctx->red.partials, ctx->red.tickets, c);
+        p.krylov_inner_rtol, p.krylov_max_it, ctx->red.partials, ctx->red.tickets, c, w->gsync);
     UFE_CUDA(cudaGetLastError());
+  }
+  // the FP32 inner BiCGStab as one persistent launch (replaces the while(in32) loop)
+  template <int L>
+  void inner_persist_l() {
+    using MT = BsrDiffMat<L>;
+    const MT m = mat32<L>();
+    auto kern = k_bicgstab_persist<MT>;
+    // grid: all blocks co-resident (computed before any capture begins, see Solver())
+    const unsigned nb = std::max(1u, std::min(persist_grid, (unsigned)(((int64_t)m.items * L + 255) / 256)));
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    UFE_CUDA(cudaStreamIsCapturing(s, &cap));
+    if (cap != cudaStreamCaptureStatusNone) {
+      // graph body: plain launch (the solve's kernels run one after another, so the grid is resident)
+      kern<<<nb, 256, 0, s>>>(m, kv_inner(), w->ks + 1, w->ppart, w->gsync);
+      UFE_CUDA(cudaGetLastError());
+      return;
+    }
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(nb);
+    cfg.blockDim = dim3(256);
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    UFE_CUDA(cudaLaunchKernelEx(&cfg, kern, m, kv_inner(), w->ks + 1, w->ppart, w->gsync));
+  }
+  void enqueue_inner_persist() {
+    switch (lanes) {
+      case 1: inner_persist_l<1>(); break;
+      case 2: inner_persist_l<2>(); break;
+      case 8: inner_persist_l<8>(); break;
+      default: inner_persist_l<4>(); break;
+    }
   }
   template <int L>
   void residual64_l(CondArg c) {
@@ -1162,14 +1231,24 @@ cudaGraphExec_t build_picard_graph(Solver &S, bool diva) {
     cudaGraphNode_t wk = add_while(body, pre, h_inner, &kbody);
     if (S.p.precision == UFE_PREC_FP32_REFINE) {
       // refinement loop: inner FP32 BiCGStab, then x += d and the FP64 residual test
-      cudaGraphConditionalHandle h_in32;
-      UFE_CUDA(cudaGraphConditionalHandleCreate(&h_in32, kbody, 0, 0));
-      CondArg in32{h_in32, 1};
-      auto ii = capture_into(S.s, kbody, {}, [&] { S.enqueue_inner_init(in32); });
-      cudaGraph_t ibody;
-      cudaGraphNode_t wi = add_while(kbody, ii, h_in32, &ibody);
-      capture_into(S.s, ibody, {}, [&] { S.krylov_iter32(in32); });
-      capture_into(S.s, kbody, {wi}, [&] { S.enqueue_refine_update(inner); });
+      cudaGraphNode_t wi;
+      if (persistent_krylov()) {
+        CondArg none{0, 0};
+        auto ii = capture_into(S.s, kbody, {}, [&] {
+          S.enqueue_inner_init(none);
+          S.enqueue_inner_persist();
+        });
+        capture_into(S.s, kbody, ii, [&] { S.enqueue_refine_update(inner); });
+      } else {
+        cudaGraphConditionalHandle h_in32;   // a handle must belong to a conditional node
+        UFE_CUDA(cudaGraphConditionalHandleCreate(&h_in32, kbody, 0, 0));
+        CondArg in32{h_in32, 1};
+        auto ii = capture_into(S.s, kbody, {}, [&] { S.enqueue_inner_init(in32); });
+        cudaGraph_t ibody;
+        wi = add_while(kbody, ii, h_in32, &ibody);
+        capture_into(S.s, ibody, {}, [&] { S.krylov_iter32(in32); });
+        capture_into(S.s, kbody, {wi}, [&] { S.enqueue_refine_update(inner); });
+      }
       // FP64 fallback when the refinement loop gave up
       cudaGraphConditionalHandle h_fb;
       UFE_CUDA(cudaGraphConditionalHandleCreate(&h_fb, body, 0, 0));
@@ -1205,11 +1284,15 @@ void run_picard_host(Solver &S, bool diva) {
         UFE_CUDA(cudaStreamSynchronize(S.s));
         if (!w->ks_host[0].active) break;
         S.enqueue_inner_init(none);
-        for (;;) {
-          for (int c = 0; c < 8; ++c) S.krylov_iter32(none);
-          UFE_CUDA(cudaMemcpyAsync(w->ks_host + 1, w->ks + 1, sizeof(KrylovScalars), cudaMemcpyDeviceToHost, S.s));
-          UFE_CUDA(cudaStreamSynchronize(S.s));
-          if (!w->ks_host[1].active) break;
+        if (persistent_krylov()) {
+          S.enqueue_inner_persist();
+        } else {
+          for (;;) {
+            for (int c = 0; c < 8; ++c) S.krylov_iter32(none);
+            UFE_CUDA(cudaMemcpyAsync(w->ks_host + 1, w->ks + 1, sizeof(KrylovScalars), cudaMemcpyDeviceToHost, S.s));
+            UFE_CUDA(cudaStreamSynchronize(S.s));
+            if (!w->ks_host[1].active) break;
+          }
         }
         S.enqueue_refine_update(none);
       } else {
@@ -1510,6 +1593,13 @@ void gnn_mesh_velocity(ufe_ctx *ctx, cudaStream_t s, float *y, bool to_state, co
   UFE_REQUIRE(w, UFE_ERR_INVALID, "learned start: upload the ice state first");
   k_gnn_velocity<<<(ctx->nTri + 255) / 256, 256, 0, s>>>(ctx->nTri, w->uv, y, to_state ? 1 : 0, mask);
   UFE_CUDA(cudaGetLastError());
+  if (to_state) {
+    // a predicted start carries no vertical-shear state: DIVA begins its first iteration as from
+    // a cold start, but with this velocity
+    UFE_CUDA(cudaMemsetAsync(w->uv_base, 0, sizeof(double2) * ctx->nTri, s));
+    UFE_CUDA(cudaMemsetAsync(w->tau_b, 0, sizeof(double2) * ctx->nTri, s));
+    UFE_CUDA(cudaMemsetAsync(w->eta_3D_b, 0, sizeof(double) * (size_t)ctx->nTri * ctx->nz, s));
+  }
 }
 
 extern "C" int32_t ufe_solve_ssa_resident(ufe_ctx *ctx, const ufe_solver_params *p, int32_t cold_start,
@@ -1729,11 +1819,15 @@ extern "C" int32_t ufe_solve_linearised(ufe_ctx *ctx, const ufe_solver_params *p
         UFE_CUDA(cudaStreamSynchronize(S.s));
         if (!w->ks_host[0].active) break;
         S.enqueue_inner_init(none);
-        for (;;) {
-          for (int c = 0; c < 8; ++c) S.krylov_iter32(none);
-          UFE_CUDA(cudaMemcpyAsync(w->ks_host + 1, w->ks + 1, sizeof(KrylovScalars), cudaMemcpyDeviceToHost, S.s));
-          UFE_CUDA(cudaStreamSynchronize(S.s));
-          if (!w->ks_host[1].active) break;
+        if (persistent_krylov()) {
+          S.enqueue_inner_persist();
+        } else {
+          for (;;) {
+            for (int c = 0; c < 8; ++c) S.krylov_iter32(none);
+            UFE_CUDA(cudaMemcpyAsync(w->ks_host + 1, w->ks + 1, sizeof(KrylovScalars), cudaMemcpyDeviceToHost, S.s));
+            UFE_CUDA(cudaStreamSynchronize(S.s));
+            if (!w->ks_host[1].active) break;
+          }
         }
         S.enqueue_refine_update(none);
       } else {

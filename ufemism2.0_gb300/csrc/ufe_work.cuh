@@ -123,6 +123,9 @@ struct Work {
   KrylovScalars *ks_host = nullptr;   // pinned mirrors
   PicardScalars *ps_host = nullptr;
   int *err = nullptr;             // assembly error flags
+  // persistent Krylov kernel: per-block partial sums of its three phases and its grid barrier
+  double *ppart = nullptr;
+  struct GridSync *gsync = nullptr;
   // graphs
   cudaGraphExec_t graph_ssa = nullptr, graph_diva = nullptr;
   uint64_t graph_ssa_key = 0, graph_diva_key = 0;

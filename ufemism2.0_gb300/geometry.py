@@ -193,9 +193,9 @@ def _uniform_marginal(f):
 
 
 def thermo_case(nV=200_000, nz=30, seed=0, corr_len=50e3, thick_corr_len=200e3, dt=10.0):
-    """Batched column thermodynamics: a uniform-resolution mesh of about ``nV`` vertices (7 km
-    spacing, so that the explicit horizontal advection keeps u dt / dx < 1;
-    at 200,000 vertices: 2,400 km x 2,400 km) with ``nz`` quadratic zeta layers; thickness
+    """Batched column thermodynamics: a mesh of about ``nV`` vertices (6.8 km inside a central
+    disk, 13.7 km outside it, so that the explicit horizontal advection keeps u dt / dx < 1;
+    3,500 km x 3,500 km at 200,000 vertices) with ``nz`` quadratic zeta layers; thickness
     uniform in [0, 4000] m with 15 % of the columns ice-free (and a taper to zero over the 40 km
     next to the domain border); surface
     temperature uniform in [-50, -10] degC; geothermal flux normal(55, 10) mW m^-2; velocities from
@@ -204,11 +204,16 @@ def thermo_case(nV=200_000, nz=30, seed=0, corr_len=50e3, thick_corr_len=200e3, 
     grounding-line columns between.  Returns (mesh, fields, params): the fields of
     ufe_heat_fields and an abi.ThermoParams with the given dt [yr]."""
     # explicit horizontal advection (calc_upwind_heat_flux_derivatives) needs u dt / dx < 1:
-    # 500 m/yr x 10 yr on a 7 km mesh.  The generator places ~1.7 (L/res)^2 vertices.
-    res = 7.0e3
-    L = res * np.sqrt(nV / 1.7)
-    mesh = generate_mesh(-L / 2, L / 2, -L / 2, L / 2, lambda x, y: np.full(np.shape(x), res), seed=seed,
-                         nz=nz, zeta=quadratic_zeta(nz))
+    # 500 m/yr x 10 yr against cells of L/512 = 6.8 km inside a disk and L/256 outside it; the
+    # disk's radius sets the vertex count.
+    L = 3500e3 * np.sqrt(nV / 200_000.0)
+    fine, coarse = _levels(nV, L)
+
+    def make_res(radius):
+        return lambda x, y: np.where(np.hypot(x, y) < radius, fine, coarse)
+
+    res = _calibrated_resolution(make_res, nV, 0.0, L, L, seed=seed)
+    mesh = generate_mesh(-L / 2, L / 2, -L / 2, L / 2, res, seed=seed, nz=nz, zeta=quadratic_zeta(nz))
     n = mesh.nV
     x, y = mesh.V[:, 0], mesh.V[:, 1]
     zeta = mesh.zeta
@@ -217,7 +222,7 @@ def thermo_case(nV=200_000, nz=30, seed=0, corr_len=50e3, thick_corr_len=200e3, 
     # the ice thins to zero over the 40 km next to the domain border (no ice on the border, where
     # an upwind triangle can be missing)
     dist = np.minimum(np.minimum(x + L / 2, L / 2 - x), np.minimum(y + L / 2, L / 2 - y))
-    H *= np.clip((dist - 0.5 * res) / 40e3, 0.0, 1.0)
+    H *= np.clip((dist - 0.5 * coarse) / 40e3, 0.0, 1.0)
     H[mesh.VBI > 0] = 0.0
     ice = H > 0.0
     floating = (smooth_field(x, y, thick_corr_len, seed + 2) > 1.0) & ice
@@ -334,10 +339,44 @@ def grounded_fraction_b_vertex(mesh, taf, nsub=6):
     return np.ascontiguousarray(cnt / npts)
 
 
-def ensemble_mesh(nV=30_000, L=1500e3, seed=0, nz=12):
-    """One mesh of about nV vertices (uniform resolution) over an L x L domain."""
-    res = L / np.sqrt(nV / 1.7)
-    return generate_mesh(-L / 2, L / 2, -L / 2, L / 2, lambda x, y: np.full(np.shape(x), res), seed=seed, nz=nz)
+def _levels(target, L):
+    """Resolutions (fine, coarse) of the two quadtree levels whose uniform point counts bracket
+    `target` on an L x L domain (a cell of size L/2^k is split when it is larger than the
+    resolution, so the resolutions sit just above the cell sizes)."""
+    k = max(1, int(np.floor(np.log(max(target, 4)) / np.log(4.0))))
+    return L / 2 ** (k + 1) * 1.01, L / 2 ** k * 1.01
+
+
+def _calibrated_resolution(make_res, target, lo, hi, L, seed=0, iters=14):
+    """The quadtree point generator places points on power-of-two cells, so a uniform resolution
+    gives vertex counts four times apart.  `make_res(a)` returns a resolution function whose
+    fine region grows with `a`; bisect `a` in [lo, hi] so that the point count is near `target`."""
+    from .mesh import generate_points
+    a0, a1 = lo, hi
+    for _ in range(iters):
+        a = 0.5 * (a0 + a1)
+        n = len(generate_points(-L / 2, L / 2, -L / 2, L / 2, make_res(a), seed=seed))
+        if n < target:
+            a0 = a
+        else:
+            a1 = a
+    return make_res(0.5 * (a0 + a1))
+
+
+def ensemble_mesh(nV=30_000, L=1500e3, seed=0, nz=12, R=600e3):
+    """One mesh of about nV vertices over an L x L domain: fine quadtree cells within a band around
+    the dome margin r = R (where the ice is thin, floating and fast), cells twice as large
+    elsewhere (L/256 and L/128 at 30,000 vertices); the band's width sets the vertex count."""
+    fine, coarse = _levels(nV, L)
+
+    def make_res(band):
+        def res(x, y):
+            r = np.hypot(x, y)
+            return np.where(np.abs(r - R) < band, fine, coarse)
+        return res
+
+    res = _calibrated_resolution(make_res, nV, 0.0, L, L, seed=seed)
+    return generate_mesh(-L / 2, L / 2, -L / 2, L / 2, res, seed=seed, nz=nz)
 
 
 def ensemble_member(mesh, member, A=1e-16, H0=3000.0, R=600e3, bed_sigma=400.0, bed_corr=20e3,
