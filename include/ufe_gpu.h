@@ -169,7 +169,9 @@ typedef struct {
   double  L2_uv;            /* last Picard change norm (calc_L2_norm_uv)                  */
   double  visc_it_relax_applied;
   double  device_ms;        /* device time of the solve                                   */
-  int32_t reserved[6];
+  int32_t n_fp64_its;       /* of n_Axb_its: FP64 BiCGStab iterations (all of them with    */
+                            /* UFE_PREC_FP64; the fallback solves with UFE_PREC_FP32_REFINE) */
+  int32_t reserved[5];
 } ufe_solve_stats;
 
 /* ---- context ------------------------------------------------------------------------------- */
@@ -417,14 +419,16 @@ int32_t ufe_gnn_loss_grad(ufe_gnn *g, int64_t n, const int32_t *nbr, const float
  * previous velocity) and the context's resident solution as the target; returns the member count.
  * ufe_gnn_train: `epochs` passes over the stored members, one Adam step per member.
  * ufe_gnn_predict_velocity: write the predicted velocity into the context's resident state for a
- * following resident solve with cold_start = 0. */
+ * following resident solve with cold_start = 0, after `smooth_passes` (0: none) averaging passes over
+ * each triangle and its neighbours (noise in the prediction roughens the first viscosity field). */
 int32_t ufe_gnn_features(ufe_gnn *g, ufe_ctx *mesh_ctx, int32_t use_prev_velocity, float *x);
 int32_t ufe_gnn_dataset_add(ufe_gnn *g, ufe_ctx *mesh_ctx, const float *features_before);
 int32_t ufe_gnn_dataset_clear(ufe_gnn *g);
 int32_t ufe_gnn_train(ufe_gnn *g, int32_t epochs, float lr, uint64_t seed, float *loss_per_epoch,
                       double *device_ms);
 int32_t ufe_gnn_evaluate(ufe_gnn *g, double *mean_loss);
-int32_t ufe_gnn_predict_velocity(ufe_gnn *g, ufe_ctx *mesh_ctx, int32_t use_prev_velocity, double *device_ms);
+int32_t ufe_gnn_predict_velocity(ufe_gnn *g, ufe_ctx *mesh_ctx, int32_t use_prev_velocity, int32_t smooth_passes,
+                                 double *device_ms);
 
 /* ---- allocation-free solve -------------------------------------------------------------------- */
 /* The CSR matrix-equation solve of ufe_solve_csr (same BiCGStab/Jacobi, same convergence test)

@@ -80,7 +80,7 @@ class DivaState(C.Structure):
 class SolveStats(C.Structure):
     _fields_ = [("n_visc_its", C.c_int32), ("n_Axb_its", C.c_int32), ("n_refinements", C.c_int32),
                 ("status", C.c_int32), ("L2_uv", C.c_double), ("visc_it_relax_applied", C.c_double),
-                ("device_ms", C.c_double), ("reserved", C.c_int32 * 6)]
+                ("device_ms", C.c_double), ("n_fp64_its", C.c_int32), ("reserved", C.c_int32 * 5)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}
@@ -310,7 +310,7 @@ EXPORTS = {
     "ufe_gnn_dataset_clear": (C.c_int32, [C.c_void_p]),
     "ufe_gnn_train": (C.c_int32, [C.c_void_p, C.c_int32, C.c_float, C.c_uint64, fptr, dptr]),
     "ufe_gnn_evaluate": (C.c_int32, [C.c_void_p, dptr]),
-    "ufe_gnn_predict_velocity": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_int32, dptr]),
+    "ufe_gnn_predict_velocity": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, dptr]),
 }
 
 _LIB = None

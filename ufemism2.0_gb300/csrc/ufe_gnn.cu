@@ -1164,9 +1164,10 @@ extern "C" int32_t ufe_gnn_evaluate(ufe_gnn *g, double *mean_loss) {
 
 // Warm start: predict the velocity of the mesh context's resident ice state and store it as the
 // resident velocity, so that ufe_solve_ssa_resident / ufe_solve_diva_resident with cold_start = 0
-// start the Picard loop from it.
+// start the Picard loop from it; `smooth_passes` averaging passes over each triangle and its
+// neighbours take the prediction's small-scale noise out first.
 extern "C" int32_t ufe_gnn_predict_velocity(ufe_gnn *g, ufe_ctx *mesh_ctx, int32_t use_prev_velocity,
-                                            double *device_ms) {
+                                            int32_t smooth_passes, double *device_ms) {
   if (!g || !mesh_ctx) return UFE_ERR_INVALID;
   return guarded(g->ctx, [&]() -> int32_t {
     UFE_REQUIRE(mesh_ctx->device == g->ctx->device, UFE_ERR_INVALID, "gnn and mesh contexts on different devices");
@@ -1181,6 +1182,7 @@ extern "C" int32_t ufe_gnn_predict_velocity(ufe_gnn *g, ufe_ctx *mesh_ctx, int32
     gnn_mesh_features(mesh_ctx, s, use_prev_velocity, g->gx, g->gmask);
     gnn_forward(g, s, Graph{n, g->gnbr}, g->gx, nullptr, nullptr);
     gnn_mesh_velocity(mesh_ctx, s, g->ybuf, true, g->gmask);
+    if (smooth_passes > 0) gnn_mesh_smooth(mesh_ctx, s, smooth_passes, g->gmask);
     UFE_CUDA(cudaEventRecord(mesh_ctx->ev1, s));
     gnn_check(g, s);
     if (device_ms) {

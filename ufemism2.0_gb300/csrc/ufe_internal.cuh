@@ -144,6 +144,7 @@ void free_thermo(ufe_ctx *ctx);
 void gnn_mesh_features(ufe_ctx *ctx, cudaStream_t s, int use_prev, float *x, float *mask);
 void gnn_mesh_graph(ufe_ctx *ctx, cudaStream_t s, int32_t *nbr);
 void gnn_mesh_velocity(ufe_ctx *ctx, cudaStream_t s, float *y, bool to_state, const float *mask);
+void gnn_mesh_smooth(ufe_ctx *ctx, cudaStream_t s, int passes, const float *mask);
 
 // ufe_layout.cu: internal (Z-order) numbering and the mappings at the ABI boundary
 void layout_upload_mesh(ufe_ctx *ctx, const ufe_mesh_desc *m);

@@ -77,6 +77,9 @@ __device__ __forceinline__ double v_add(double a, double b) { return a + b; }
 // ---- matrix access policies ---------------------------------------------------------------
 // 2x2-block rows (one triangle = its u and v rows); blocks stored in MatReal (FP64 or FP32),
 // vectors and accumulation in VecReal; L lanes per block row.
+// Sliced ELL (one lane per row): block rows in slices of 32 (one warp), the k-th entry of row
+// i at slot soff[i/32] + 32 k + i%32, so that a warp's loads of blocks and columns are
+// contiguous.  Short rows are padded with zero blocks whose column is the row itself.
 template <typename MatReal, typename VecReal, int L>
 struct BsrMat {
   using Vec = typename std::conditional<sizeof(VecReal) == 8, double2, float2>::type;
@@ -86,9 +89,44 @@ struct BsrMat {
   const int32_t *__restrict__ ptr;
   const int32_t *__restrict__ col;
   const Blk *__restrict__ blk;
+  const int32_t *__restrict__ soff = nullptr;   // sliced-ELL copy (L == 1), or null
+  const int32_t *__restrict__ scol = nullptr;
+  const Blk *__restrict__ sblk = nullptr;
   template <class G>
   __device__ __forceinline__ Vec row_partial(int i, int lane, G get) const {
     Vec y = v_zero<Vec>();
+    if (L == 1 && soff) {
+      const int sl = i >> 5;
+      const int s0 = __ldg(soff + sl), w = (__ldg(soff + sl + 1) - s0) >> 5;
+      const int base = s0 + (i & 31);
+      int k = 0;
+      for (; k + 4 <= w; k += 4) {   // four slots' loads in flight at once
+        int c[4];
+        Blk a[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const int slot = base + ((k + u) << 5);
+          c[u] = __ldg(scol + slot);
+          a[u] = sblk[slot];
+        }
+        Vec x[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) x[u] = get(c[u]);
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          y.x = fma(a[u].y, x[u].y, fma(a[u].x, x[u].x, y.x));
+          y.y = fma(a[u].w, x[u].y, fma(a[u].z, x[u].x, y.y));
+        }
+      }
+      for (; k < w; ++k) {
+        const int slot = base + (k << 5);
+        const Blk a = sblk[slot];
+        const Vec x = get(__ldg(scol + slot));
+        y.x = fma(a.y, x.y, fma(a.x, x.x, y.x));
+        y.y = fma(a.w, x.y, fma(a.z, x.x, y.y));
+      }
+      return y;
+    }
     int k2 = __ldg(ptr + i + 1);
     for (int k = __ldg(ptr + i) + lane; k < k2; k += L) {
       Blk a = blk[k];
@@ -114,6 +152,9 @@ struct BsrDiffMat {
   const int32_t *__restrict__ col;
   const float4 *__restrict__ blk;
   const float4 *__restrict__ rowsum;
+  const int32_t *__restrict__ soff = nullptr;   // sliced-ELL copy (L == 1), or null
+  const int32_t *__restrict__ scol = nullptr;
+  const float4 *__restrict__ sblk = nullptr;
   template <class G>
   __device__ __forceinline__ float2 row_partial(int i, int lane, G get) const {
     const float2 xi = get(i);
@@ -122,6 +163,40 @@ struct BsrDiffMat {
       const float4 s = rowsum[i];
       y.x = fmaf(s.y, xi.y, s.x * xi.x);
       y.y = fmaf(s.w, xi.y, s.z * xi.x);
+    }
+    if (L == 1 && soff) {
+      const int sl = i >> 5;
+      const int s0 = __ldg(soff + sl), w = (__ldg(soff + sl + 1) - s0) >> 5;
+      const int base = s0 + (i & 31);
+      int k = 0;
+      for (; k + 4 <= w; k += 4) {   // four slots' loads in flight at once
+        int c[4];
+        float4 a[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const int slot = base + ((k + u) << 5);
+          c[u] = __ldg(scol + slot);
+          a[u] = sblk[slot];
+        }
+        float2 xj[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) xj[u] = get(c[u]);
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const float dx = xj[u].x - xi.x, dy = xj[u].y - xi.y;
+          y.x = fmaf(a[u].y, dy, fmaf(a[u].x, dx, y.x));
+          y.y = fmaf(a[u].w, dy, fmaf(a[u].z, dx, y.y));
+        }
+      }
+      for (; k < w; ++k) {
+        const int slot = base + (k << 5);
+        const float4 a = sblk[slot];
+        const float2 xj = get(__ldg(scol + slot));
+        const float dx = xj.x - xi.x, dy = xj.y - xi.y;
+        y.x = fmaf(a.y, dy, fmaf(a.x, dx, y.x));
+        y.y = fmaf(a.w, dy, fmaf(a.z, dx, y.y));
+      }
+      return y;
     }
     int k2 = __ldg(ptr + i + 1);
     for (int k = __ldg(ptr + i) + lane; k < k2; k += L) {
@@ -400,11 +475,14 @@ inline unsigned krylov_grid(const M &mat, int threads, int max_blocks) {
 constexpr int kPersistMaxBlocks = 8 * 152;
 constexpr int kPersistSlots = 3;     // partial sums per block per phase
 
-struct GridSync {
+// arrival counter and generation on separate 128-byte lines: the waiters poll `gen` while the
+// arrivals update `count`
+struct __align__(128) GridSync {
   unsigned int count;
+  unsigned int pad0[31];
   unsigned int gen;
   int err;
-  int pad;
+  unsigned int pad1[30];
 };
 
 __device__ __forceinline__ unsigned int ld_acquire_u32(const unsigned int *p) {
@@ -428,11 +506,12 @@ __device__ __forceinline__ bool grid_barrier(GridSync *gs, unsigned int &gen) {
     } else {
       long long spins = 0;
       while (ld_acquire_u32(&gs->gen) == my) {
-        if (++spins > (1ll << 26) || *((volatile int *)&gs->err)) {
+        if (++spins > (1ll << 24) || *((volatile int *)&gs->err)) {
           ok = 0;
           atomicExch(&gs->err, 1);
           break;
         }
+        __nanosleep(32);
       }
     }
     __threadfence();
@@ -486,8 +565,10 @@ __device__ __forceinline__ void all_partials(const double *part, double *tot) {
 
 // Starts from the state k_krylov_init / k_inner_init left in *ks (and P[0], V[0]); runs until the
 // scalars stop the solve; leaves x, r, the counters and the status as the three-kernel loop does.
+constexpr int kPersistThreads = 1024;   // one block per SM
+
 template <class M>
-__global__ void __launch_bounds__(256) k_bicgstab_persist(M mat, KV<typename M::Vec> v, KrylovScalars *ks,
+__global__ void __launch_bounds__(kPersistThreads) k_bicgstab_persist(M mat, KV<typename M::Vec> v, KrylovScalars *ks,
                                                           double *part, GridSync *gs) {
   using Vec = typename M::Vec;
   using R = typename ScalarOf<Vec>::T;
@@ -582,6 +663,184 @@ __global__ void __launch_bounds__(256) k_bicgstab_persist(M mat, KV<typename M::
         const Vec pi = v.P[nxt][i], si = v.S[i], ti = v.T[i];
         v.X[i] = v_xupd(v.X[i], alpha, pi, omega, si);
         const Vec ri = v_sub_scaled(si, omega, ti);
+        v.R[i] = ri;
+        acc[0] += v_dot(ri, v.RP[i]);
+        acc[1] += v_dot(ri, ri);
+      }
+      block_partials<2>(acc, partX);
+      if (!(ok = grid_barrier(gs, gen))) break;
+      double tot[2];
+      all_partials<2>(partX, tot);
+      s.it += 1;
+      s.total_its += 1;
+      const double dp = sqrt(tot[1]);
+      s.dp = dp;
+      const double rho_new = tot[0];
+      s.rhoold = s.rho;
+      s.omegaold = s.omega;
+      s.rho = rho_new;
+      if (s.tbreak) { s.active = 0; s.status = UFE_OK; s.dp = 0.0; }
+      else if (isnan(dp)) { s.status = UFE_ERR_NAN; s.active = 0; }
+      else if (dp <= s.ttol) { s.active = 0; }
+      else if (dp >= 1e4 * s.rnorm0) { s.status = UFE_ERR_DIVERGED; s.active = 0; }
+      else if (s.it >= s.max_it) { s.status = UFE_WARN_KRYLOV_MAXIT; s.active = 0; }
+      else if (rho_new == 0.0) { s.status = UFE_ERR_DIVERGED; s.active = 0; }
+      else s.beta = (s.rho / s.rhoold) * (s.alpha / s.omegaold);
+    }
+  }
+  if (!ok) {
+    s.status = UFE_ERR_DEVICE;
+    s.active = 0;
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) *ks = s;
+}
+
+// ---- persistent FP32 BiCGStab with shared-memory neighbourhoods -------------------------------
+// Block b owns the contiguous block rows [b*rpb, (b+1)*rpb) (whole sliced-ELL slices; the rows are
+// in Z order, so they form a compact patch of the mesh).  Each SpMV phase first stages, into
+// shared memory, the vector its rows read: its own rows (coalesced) and the patch's halo rows
+// (listed once per mesh), computing the on-the-fly update (p, or s = r - alpha v) once per staged
+// entry; the rows then read neighbours from shared memory through per-slot local indices.
+struct HaloDiffMat {
+  int32_t items;
+  int32_t rpb;                          // rows per block (a multiple of 32)
+  const int32_t *__restrict__ soff;     // sliced-ELL slice offsets
+  const int32_t *__restrict__ lcol;     // local index (own rows, then halo) per slot
+  const float4 *__restrict__ sblk;      // FP32 blocks per slot
+  const float4 *__restrict__ rowsum;    // FP64 row sums rounded to FP32
+  const int32_t *__restrict__ halo_off; // gridDim.x + 1
+  const int32_t *__restrict__ halo_idx; // global rows of each block's halo
+};
+
+__device__ __forceinline__ float2 halo_row(const HaloDiffMat &m, int i, int il, const float2 *tab) {
+  const float2 xi = tab[il];
+  const float4 sr = m.rowsum[i];
+  float2 y = make_float2(fmaf(sr.y, xi.y, sr.x * xi.x), fmaf(sr.w, xi.y, sr.z * xi.x));
+  const int sl = i >> 5;
+  const int s0 = __ldg(m.soff + sl), w = (__ldg(m.soff + sl + 1) - s0) >> 5;
+  const int base = s0 + (i & 31);
+  int k = 0;
+  for (; k + 4 <= w; k += 4) {   // four slots' loads in flight at once
+    int c[4];
+    float4 a[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int slot = base + ((k + u) << 5);
+      c[u] = __ldg(m.lcol + slot);
+      a[u] = __ldg(m.sblk + slot);
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const float2 xj = tab[c[u]];
+      const float dx = xj.x - xi.x, dy = xj.y - xi.y;
+      y.x = fmaf(a[u].y, dy, fmaf(a[u].x, dx, y.x));
+      y.y = fmaf(a[u].w, dy, fmaf(a[u].z, dx, y.y));
+    }
+  }
+  for (; k < w; ++k) {
+    const int slot = base + (k << 5);
+    const float4 a = __ldg(m.sblk + slot);
+    const float2 xj = tab[__ldg(m.lcol + slot)];
+    const float dx = xj.x - xi.x, dy = xj.y - xi.y;
+    y.x = fmaf(a.y, dy, fmaf(a.x, dx, y.x));
+    y.y = fmaf(a.w, dy, fmaf(a.z, dx, y.y));
+  }
+  return y;
+}
+
+static __global__ void __launch_bounds__(kPersistThreads) k_bicgstab32_halo(HaloDiffMat m, KV<float2> v, KrylovScalars *ks,
+                                                                      double *part, GridSync *gs) {
+  extern __shared__ float2 tab[];
+  KrylovScalars s = *ks;
+  if (!s.active) return;
+  double *partP = part, *partS = part + kPersistMaxBlocks * kPersistSlots,
+         *partX = part + 2 * kPersistMaxBlocks * kPersistSlots;
+  unsigned int gen = ld_acquire_u32(&gs->gen);
+  const int r0 = blockIdx.x * m.rpb;
+  const int r1 = min(m.items, r0 + m.rpb);
+  const int own = max(r1 - r0, 0);
+  const int h0 = __ldg(m.halo_off + blockIdx.x);
+  const int nloc = own + (__ldg(m.halo_off + blockIdx.x + 1) - h0);
+  bool ok = true;
+  while (s.active) {
+    const int cur = s.it & 1, nxt = cur ^ 1;
+    // -- p <- r - beta omega v + beta p (staged);  v <- D^-1 A p;  (v, r^)
+    {
+      const float beta = (float)s.beta, bw = (float)(s.beta * s.omegaold);
+      const float2 *__restrict__ Po = v.P[cur];
+      const float2 *__restrict__ Vo = v.V[cur];
+      for (int e = threadIdx.x; e < nloc; e += blockDim.x) {
+        const int g = e < own ? r0 + e : __ldg(m.halo_idx + h0 + e - own);
+        const float2 pn = v_pupd(v.R[g], bw, Vo[g], beta, Po[g]);
+        tab[e] = pn;
+        if (e < own) v.P[nxt][g] = pn;
+      }
+      __syncthreads();
+      double acc[1] = {0.0};
+      for (int il = threadIdx.x; il < own; il += blockDim.x) {
+        const int i = r0 + il;
+        const float2 vn = v_mul(v.dinv[i], halo_row(m, i, il, tab));
+        v.V[nxt][i] = vn;
+        acc[0] += v_dot(vn, v.RP[i]);
+      }
+      block_partials<1>(acc, partP);
+      if (!(ok = grid_barrier(gs, gen))) break;
+      double tot[1];
+      all_partials<1>(partP, tot);
+      const double d1 = tot[0];
+      if (d1 == 0.0 || isnan(d1)) {
+        s.status = isnan(d1) ? UFE_ERR_NAN : UFE_ERR_DIVERGED;
+        s.active = 0;
+        break;
+      }
+      s.alpha = s.rho / d1;
+    }
+    // -- s <- r - alpha v (staged);  t <- D^-1 A s;  (s,t), (t,t), (s,s)
+    {
+      const float alpha = (float)s.alpha;
+      const float2 *__restrict__ Vn = v.V[nxt];
+      for (int e = threadIdx.x; e < nloc; e += blockDim.x) {
+        const int g = e < own ? r0 + e : __ldg(m.halo_idx + h0 + e - own);
+        const float2 sv = v_sub_scaled(v.R[g], alpha, Vn[g]);
+        tab[e] = sv;
+        if (e < own) v.S[g] = sv;
+      }
+      __syncthreads();
+      double acc[3] = {0.0, 0.0, 0.0};
+      for (int il = threadIdx.x; il < own; il += blockDim.x) {
+        const int i = r0 + il;
+        const float2 si = tab[il];
+        const float2 ti = v_mul(v.dinv[i], halo_row(m, i, il, tab));
+        v.T[i] = ti;
+        acc[0] += v_dot(si, ti);
+        acc[1] += v_dot(ti, ti);
+        acc[2] += v_dot(si, si);
+      }
+      block_partials<3>(acc, partS);
+      if (!(ok = grid_barrier(gs, gen))) break;
+      double tot[3];
+      all_partials<3>(partS, tot);
+      if (tot[1] == 0.0) {
+        if (tot[2] != 0.0) { s.status = UFE_ERR_DIVERGED; s.active = 0; break; }
+        s.omega = 0.0;
+        s.tbreak = 1;
+      } else if (isnan(tot[1])) {
+        s.status = UFE_ERR_NAN;
+        s.active = 0;
+        break;
+      } else {
+        s.omega = tot[0] / tot[1];
+      }
+    }
+    // -- x <- x + alpha p + omega s;  r <- s - omega t;  (r, r^), (r, r)
+    {
+      const float alpha = (float)s.alpha, omega = (float)s.omega;
+      double acc[2] = {0.0, 0.0};
+      for (int il = threadIdx.x; il < own; il += blockDim.x) {
+        const int i = r0 + il;
+        const float2 pi = v.P[nxt][i], si = v.S[i], ti = v.T[i];
+        v.X[i] = v_xupd(v.X[i], alpha, pi, omega, si);
+        const float2 ri = v_sub_scaled(si, omega, ti);
         v.R[i] = ri;
         acc[0] += v_dot(ri, v.RP[i]);
         acc[1] += v_dot(ri, ri);

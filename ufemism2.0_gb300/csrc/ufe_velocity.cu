@@ -810,6 +810,105 @@ static void check_operators(ufe_ctx *ctx) {
     UFE_REQUIRE(same(UFE_OP_M2_DDX_B_B, op), UFE_ERR_INVALID, "2nd-order b_b operators must share one pattern");
 }
 
+// The sliced-ELL layout of the stiffness pattern (the 2nd-order b_b operators' pattern).
+__global__ void k_sell_fill(int64_t nnzb, const int32_t *__restrict__ map, const double4 *__restrict__ blk,
+                            const float4 *__restrict__ blk32, double4 *__restrict__ sblk, float4 *__restrict__ sblk32) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nnzb) return;
+  const int32_t slot = map[k];
+  sblk[slot] = blk[k];
+  sblk32[slot] = blk32[k];
+}
+
+void build_sell(ufe_ctx *ctx, Work *w) {
+  const DevCSR &m2 = ctx->ops[UFE_OP_M2_DDX_B_B];
+  const int32_t n = w->nTri;
+  std::vector<int32_t> ptr(n + 1), ind(m2.nnz);
+  UFE_CUDA(cudaMemcpy(ptr.data(), m2.ptr, sizeof(int32_t) * (n + 1), cudaMemcpyDeviceToHost));
+  UFE_CUDA(cudaMemcpy(ind.data(), m2.ind, sizeof(int32_t) * m2.nnz, cudaMemcpyDeviceToHost));
+  const int32_t nsl = (n + 31) / 32;
+  std::vector<int32_t> off(nsl + 1, 0);
+  for (int32_t sl = 0; sl < nsl; ++sl) {
+    int32_t wmax = 0;
+    for (int32_t i = sl * 32; i < std::min(n, sl * 32 + 32); ++i) wmax = std::max(wmax, ptr[i + 1] - ptr[i]);
+    off[sl + 1] = off[sl] + 32 * wmax;
+  }
+  const int64_t nslots = off[nsl];
+  std::vector<int32_t> col(nslots), map(m2.nnz);
+  for (int32_t sl = 0; sl < nsl; ++sl) {
+    const int32_t wsl = (off[sl + 1] - off[sl]) / 32;
+    for (int32_t t = 0; t < 32; ++t) {
+      const int32_t i = sl * 32 + t;
+      for (int32_t k = 0; k < wsl; ++k) {
+        const int64_t slot = off[sl] + (int64_t)k * 32 + t;
+        const int32_t e = (i < n) ? ptr[i] + k : -1;
+        if (i < n && e < ptr[i + 1]) {
+          col[slot] = ind[e];
+          map[e] = (int32_t)slot;
+        } else {
+          col[slot] = i < n ? i : 0;   // padding: zero block on the row itself
+        }
+      }
+    }
+  }
+  w->nslots = nslots;
+  auto up = [&](const std::vector<int32_t> &h) {
+    int32_t *d = alloc_n<int32_t>(std::max<size_t>(h.size(), 1));
+    UFE_CUDA(cudaMemcpy(d, h.data(), sizeof(int32_t) * h.size(), cudaMemcpyHostToDevice));
+    return d;
+  };
+  w->sell_off = up(off);
+  w->sell_col = up(col);
+  w->sell_map = up(map);
+  // patches for the shared-memory persistent solve: one per SM
+  int dev = 0, sms = 0;
+  UFE_CUDA(cudaGetDevice(&dev));
+  UFE_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  const int32_t G = std::max(1, std::min<int32_t>(sms, nsl));
+  const int32_t rpb = ((n + G - 1) / G + 31) / 32 * 32;
+  std::vector<int32_t> hoff(G + 1, 0), hidx, lcol(nslots, 0);
+  int32_t maxlocal = 0;
+  std::vector<int32_t> halo;
+  for (int32_t b = 0; b < G; ++b) {
+    const int32_t r0 = std::min(n, b * rpb), r1 = std::min(n, r0 + rpb);
+    halo.clear();
+    // a block without rows owns no slice (r0 = n may sit inside the last, partial slice)
+    const int32_t sl0 = r0 / 32, sl1 = r1 > r0 ? (r1 + 31) / 32 : sl0;
+    for (int64_t slot = off[sl0]; slot < off[sl1]; ++slot)
+      if (col[slot] < r0 || col[slot] >= r1) halo.push_back(col[slot]);
+    std::sort(halo.begin(), halo.end());
+    halo.erase(std::unique(halo.begin(), halo.end()), halo.end());
+    const int32_t own = r1 - r0;
+    for (int64_t slot = off[sl0]; slot < off[sl1]; ++slot) {
+      const int32_t c = col[slot];
+      lcol[slot] = (c >= r0 && c < r1) ? c - r0
+                                       : own + (int32_t)(std::lower_bound(halo.begin(), halo.end(), c) - halo.begin());
+    }
+    hidx.insert(hidx.end(), halo.begin(), halo.end());
+    hoff[b + 1] = (int32_t)hidx.size();
+    maxlocal = std::max(maxlocal, own + (int32_t)halo.size());
+  }
+  w->halo_G = G;
+  w->halo_rpb = rpb;
+  w->halo_maxlocal = maxlocal;
+  w->halo_off = up(hoff);
+  w->halo_idx = up(hidx);
+  w->halo_lcol = up(lcol);
+  w->sell_blk = alloc_n<double4>(nslots);
+  w->sell_blk32 = alloc_n<float4>(nslots);
+  UFE_CUDA(cudaMemsetAsync(w->sell_blk, 0, sizeof(double4) * nslots, ctx->stream));
+  UFE_CUDA(cudaMemsetAsync(w->sell_blk32, 0, sizeof(float4) * nslots, ctx->stream));
+}
+
+bool use_sell() {
+  static int v = -1;
+  if (v < 0) {
+    const char *e = getenv("UFE_NO_SELL");
+    v = (e && *e && *e != '0') ? 0 : 1;
+  }
+  return v == 1;
+}
+
 Work *ensure_work(ufe_ctx *ctx) {
   check_operators(ctx);
   if (ctx->work) return ctx->work;
@@ -851,6 +950,7 @@ Work *ensure_work(ufe_ctx *ctx) {
   w->beta_eff_a = alloc_n<double>(nV);
   w->F2a1 = alloc_n<double>(nV);
   w->eta_3D_a = alloc_n<double>((size_t)nV * nz);
+  build_sell(ctx, w);
   w->ppart = alloc_n<double>((size_t)3 * kPersistMaxBlocks * kPersistSlots);
   w->gsync = alloc_n<GridSync>(1);
   w->F1_3D_a = alloc_n<double>((size_t)nV * nz);
@@ -888,7 +988,8 @@ void free_work(ufe_ctx *ctx) {
                   w->eta_3D_b, w->bfc_b, w->F2b1, w->beta_b, w->Hi, w->Hs, w->Avav, w->A_flow, w->beta_sq,
                   w->alpha_sq, w->effp, w->tys, w->mask_gr, w->N_a, w->beta_a, w->beta_eff_a, w->F2a1,
                   w->eta_3D_a, w->F1_3D_a, w->N_b_in, w->dNx_b_in, w->dNy_b_in, w->beta_b_in, w->ks,
-                  w->ps, w->err, w->ppart, w->gsync};
+                  w->ps, w->err, w->ppart, w->gsync, w->sell_off, w->sell_col, w->sell_map, w->sell_blk,
+                  w->sell_blk32, w->halo_off, w->halo_idx, w->halo_lcol};
   for (void *p : ptrs) dev_free(p);
   if (w->ks_host) cudaFreeHost(w->ks_host);
   if (w->ps_host) cudaFreeHost(w->ps_host);
@@ -922,16 +1023,16 @@ bool persistent_krylov() {
   return v == 1;
 }
 
-// Blocks of 256 threads for a persistent kernel: all co-resident, at most kPersistMaxBlocks,
+// Blocks of kPersistThreads for a persistent kernel: all co-resident, at most kPersistMaxBlocks,
 // no more than the rows need.
 unsigned persist_blocks(const void *kernel, int64_t lanes_total) {
   int dev = 0, sms = 0, per_sm = 0;
   UFE_CUDA(cudaGetDevice(&dev));
   UFE_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-  UFE_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, 256, 0));
+  UFE_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kPersistThreads, 0));
   int64_t nb = (int64_t)std::max(per_sm, 1) * sms;
   nb = std::min<int64_t>(nb, kPersistMaxBlocks);
-  nb = std::min<int64_t>(nb, (lanes_total + 255) / 256);
+  nb = std::min<int64_t>(nb, (lanes_total + kPersistThreads - 1) / kPersistThreads);
   return (unsigned)std::max<int64_t>(nb, 1);
 }
 
@@ -1005,6 +1106,11 @@ struct Solver {
     else if (mode == kFromSSA) k_assemble<kFromSSA><<<g, kThreads, 0, s>>>(a, q, c);
     else k_assemble<kFromDIVA><<<g, kThreads, 0, s>>>(a, q, c);
     UFE_CUDA(cudaGetLastError());
+    if (use_sell()) {
+      k_sell_fill<<<(unsigned)((w->nnzb + 255) / 256), 256, 0, s>>>(w->nnzb, w->sell_map, w->blk, w->blk32,
+                                                                      w->sell_blk, w->sell_blk32);
+      UFE_CUDA(cudaGetLastError());
+    }
   }
 
   template <class M>
@@ -1020,12 +1126,24 @@ struct Solver {
   template <int L>
   BsrMat<double, double, L> mat64() const {
     const DevCSR &m2 = ctx->ops[UFE_OP_M2_DDX_B_B];
-    return BsrMat<double, double, L>{w->nTri, m2.ptr, m2.ind, w->blk};
+    BsrMat<double, double, L> m{w->nTri, m2.ptr, m2.ind, w->blk};
+    if (L == 1 && use_sell()) {
+      m.soff = w->sell_off;
+      m.scol = w->sell_col;
+      m.sblk = w->sell_blk;
+    }
+    return m;
   }
   template <int L>
   BsrDiffMat<L> mat32() const {
     const DevCSR &m2 = ctx->ops[UFE_OP_M2_DDX_B_B];
-    return BsrDiffMat<L>{w->nTri, m2.ptr, m2.ind, w->blk32, w->rowsum32};
+    BsrDiffMat<L> m{w->nTri, m2.ptr, m2.ind, w->blk32, w->rowsum32};
+    if (L == 1 && use_sell()) {
+      m.soff = w->sell_off;
+      m.scol = w->sell_col;
+      m.sblk = w->sell_blk32;
+    }
+    return m;
   }
   KV<double2> kv64() const {
     KV<double2> v;
@@ -1064,24 +1182,58 @@ struct Solver {
     UFE_CUDA(cudaGetLastError());
   }
   // the FP32 inner BiCGStab as one persistent launch (replaces the while(in32) loop)
+  // shared-memory patches fit: one 1024-thread block per SM, the table in shared memory
+  bool halo_ok() const {
+    return use_sell() && lanes == 1 && w->halo_G > 0 &&
+           (size_t)w->halo_maxlocal * sizeof(float2) <= 160 * 1024 && !getenv("UFE_NO_HALO");
+  }
+  void inner_halo() {
+    const size_t smem = (size_t)w->halo_maxlocal * sizeof(float2);
+    static size_t attr = 0;
+    if (smem > attr) {
+      UFE_CUDA(cudaFuncSetAttribute(k_bicgstab32_halo, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      attr = smem;
+    }
+    HaloDiffMat m{w->nTri, w->halo_rpb, w->sell_off, w->halo_lcol, w->sell_blk32, w->rowsum32, w->halo_off,
+                  w->halo_idx};
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    UFE_CUDA(cudaStreamIsCapturing(s, &cap));
+    if (cap != cudaStreamCaptureStatusNone) {
+      k_bicgstab32_halo<<<w->halo_G, kPersistThreads, smem, s>>>(m, kv_inner(), w->ks + 1, w->ppart, w->gsync);
+      UFE_CUDA(cudaGetLastError());
+      return;
+    }
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(w->halo_G);
+    cfg.blockDim = dim3(kPersistThreads);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr1[1];
+    attr1[0].id = cudaLaunchAttributeCooperative;
+    attr1[0].val.cooperative = 1;
+    cfg.attrs = attr1;
+    cfg.numAttrs = 1;
+    UFE_CUDA(cudaLaunchKernelEx(&cfg, k_bicgstab32_halo, m, kv_inner(), w->ks + 1, w->ppart, w->gsync));
+  }
   template <int L>
   void inner_persist_l() {
     using MT = BsrDiffMat<L>;
     const MT m = mat32<L>();
     auto kern = k_bicgstab_persist<MT>;
     // grid: all blocks co-resident (computed before any capture begins, see Solver())
-    const unsigned nb = std::max(1u, std::min(persist_grid, (unsigned)(((int64_t)m.items * L + 255) / 256)));
+    const unsigned nb =
+        std::max(1u, std::min(persist_grid, (unsigned)(((int64_t)m.items * L + kPersistThreads - 1) / kPersistThreads)));
     cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
     UFE_CUDA(cudaStreamIsCapturing(s, &cap));
     if (cap != cudaStreamCaptureStatusNone) {
       // graph body: plain launch (the solve's kernels run one after another, so the grid is resident)
-      kern<<<nb, 256, 0, s>>>(m, kv_inner(), w->ks + 1, w->ppart, w->gsync);
+      kern<<<nb, kPersistThreads, 0, s>>>(m, kv_inner(), w->ks + 1, w->ppart, w->gsync);
       UFE_CUDA(cudaGetLastError());
       return;
     }
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(nb);
-    cfg.blockDim = dim3(256);
+    cfg.blockDim = dim3(kPersistThreads);
     cfg.stream = s;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeCooperative;
@@ -1091,6 +1243,10 @@ struct Solver {
     UFE_CUDA(cudaLaunchKernelEx(&cfg, kern, m, kv_inner(), w->ks + 1, w->ppart, w->gsync));
   }
   void enqueue_inner_persist() {
+    if (halo_ok()) {
+      inner_halo();
+      return;
+    }
     switch (lanes) {
       case 1: inner_persist_l<1>(); break;
       case 2: inner_persist_l<2>(); break;
@@ -1400,6 +1556,7 @@ int32_t run_picard(ufe_ctx *ctx, const ufe_solver_params &p, bool diva, ufe_solv
     stats->L2_uv = ps.L2;
     stats->visc_it_relax_applied = ps.relax;
     stats->device_ms = ms;
+    stats->n_fp64_its = ks.total_its;
   }
   return ps.status;
 }
@@ -1571,6 +1728,35 @@ __global__ void k_gnn_velocity(int nTri, double2 *uv, float *y, int to_state, co
     y[2 * t] = (float)(uv[t].x / 1e3);
     y[2 * t + 1] = (float)(uv[t].y / 1e3);
   }
+}
+
+// one averaging pass over each triangle and its TriC neighbours (ice triangles only)
+__global__ void k_smooth_uv(int nTri, const int32_t *TriC, const float *mask, const double2 *in, double2 *out) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nTri) return;
+  if (mask && !(mask[t] > 0.f)) {
+    out[t] = in[t];
+    return;
+  }
+  double2 sum = in[t];
+  int cnt = 1;
+  for (int q = 0; q < 3; ++q) {
+    const int32_t j = TriC[(int64_t)q * nTri + t] - 1;
+    if (j < 0 || (mask && !(mask[j] > 0.f))) continue;
+    sum.x += in[j].x;
+    sum.y += in[j].y;
+    ++cnt;
+  }
+  out[t] = make_double2(sum.x / cnt, sum.y / cnt);
+}
+
+void gnn_mesh_smooth(ufe_ctx *ctx, cudaStream_t s, int passes, const float *mask) {
+  Work *w = ctx->work;
+  for (int k = 0; k < passes; ++k) {   // ping-pong through the Krylov scratch vector S
+    k_smooth_uv<<<(ctx->nTri + 255) / 256, 256, 0, s>>>(ctx->nTri, ctx->TriC, mask, w->uv, w->kv.S);
+    k_smooth_uv<<<(ctx->nTri + 255) / 256, 256, 0, s>>>(ctx->nTri, ctx->TriC, mask, w->kv.S, w->uv);
+  }
+  UFE_CUDA(cudaGetLastError());
 }
 
 void gnn_mesh_features(ufe_ctx *ctx, cudaStream_t s, int use_prev, float *x, float *mask) {

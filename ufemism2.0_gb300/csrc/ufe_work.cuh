@@ -123,6 +123,18 @@ struct Work {
   KrylovScalars *ks_host = nullptr;   // pinned mirrors
   PicardScalars *ps_host = nullptr;
   int *err = nullptr;             // assembly error flags
+  // sliced-ELL copy of the stiffness matrix for the Krylov SpMVs (slices of 32 block rows)
+  int64_t nslots = 0;
+  int32_t *sell_off = nullptr;   // nslices + 1
+  int32_t *sell_col = nullptr;   // nslots; padding slots hold the row itself
+  int32_t *sell_map = nullptr;   // nnzb: slot of CSR block k
+  double4 *sell_blk = nullptr;   // nslots; padding slots stay zero
+  float4 *sell_blk32 = nullptr;
+  // patches of the persistent FP32 solve: block b owns rows [b*halo_rpb, (b+1)*halo_rpb)
+  int32_t halo_G = 0, halo_rpb = 0, halo_maxlocal = 0;
+  int32_t *halo_off = nullptr;   // halo_G + 1
+  int32_t *halo_idx = nullptr;   // halo rows of every block
+  int32_t *halo_lcol = nullptr;  // nslots: local index of each slot's column
   // persistent Krylov kernel: per-block partial sums of its three phases and its grid barrier
   double *ppart = nullptr;
   struct GridSync *gsync = nullptr;

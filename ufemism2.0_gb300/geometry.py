@@ -128,7 +128,7 @@ def channel_case(seed=0, nz=12, H=250.0, A=2e-17, res_scale=1.0, sliding="Schoof
     x, y = mesh.V[:, 0], mesh.V[:, 1]
     Hb = mismip_bed(x, y)
     SL = np.zeros(mesh.nV)
-    Hi = np.full(mesh.nV, H)
+    Hi = np.full(mesh.nV, float(H))
     Hs = surface_elevation(Hi, Hb, SL)
     taf = thickness_above_flotation(Hi, Hb, SL)
     effp = np.maximum(0.0, ICE_DENSITY * GRAV * Hi - SEAWATER_DENSITY * GRAV * np.maximum(0.0, SL - Hb))

@@ -125,9 +125,9 @@ class LearnedStart:
         self._check(self.lib.ufe_gnn_evaluate(self.h, C.byref(l)))
         return l.value
 
-    def predict(self, solver, use_prev_velocity: bool = False):
+    def predict(self, solver, use_prev_velocity: bool = False, smooth_passes: int = 0):
         """Store the predicted velocity as the solver's resident velocity; returns device ms."""
         ms = C.c_double()
         self._check(self.lib.ufe_gnn_predict_velocity(self.h, solver.ctx, 1 if use_prev_velocity else 0,
-                                                      C.byref(ms)))
+                                                      smooth_passes, C.byref(ms)))
         return ms.value
