@@ -591,6 +591,64 @@ def run_learned(args):
     print(json.dumps(line))
 
 
+ENSEMBLE_WORKLOAD = ("ensemble of SSA solves on meshes of uneven size (log-uniform vertex counts), each its own "
+                     "geometry of the learned-start ensemble family; autotuned rows per warp per mesh; members "
+                     "solved one after another vs side by side (ufe_ensemble_solve)")
+
+
+def run_ensemble(args):
+    import torch
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    pkg = __graft_entry__.load_package()
+    pkg.build()
+    rng = np.random.default_rng(7)
+    sizes = np.exp(rng.uniform(np.log(args.ens_min), np.log(args.ens_max), args.ens_members)).astype(int)
+    members = []
+    for k, nv in enumerate(sizes):
+        mesh = pkg.geometry.ensemble_mesh(nV=int(nv), seed=k)
+        ice, p = pkg.geometry.ensemble_member(mesh, 500 + k)
+        members.append((mesh, ice, p))
+        print(f"member {k}: {mesh.nV} vertices", file=sys.stderr, flush=True)
+    p = members[0][2]
+    solvers = [pkg.VelocitySolver(m, device=local) for m, _, _ in members]
+    tune = []
+    for sv, (m, ice, _) in zip(solvers, members):
+        sv.ice_upload(ice)
+        sv.solve_resident(p, diva=False, cold_start=True)   # warm-up: graphs, and the system to tune on
+        tune.append(sv.autotune(repeats=20)[0])
+    # one after another (device time of each solve)
+    seq_ms, its = 0.0, []
+    for sv in solvers:
+        st = sv.solve_resident(p, diva=False, cold_start=True)
+        seq_ms += st["device_ms"]
+        its.append((st["n_visc_its"], st["n_Axb_its"]))
+    pkg.ensemble_solve(solvers, p, diva=False, cold_start=True)   # warm-up of the concurrent launch
+    walls = []
+    with ClockSampler(local) as clocks:
+        for _ in range(args.steps):
+            stats, wall = pkg.ensemble_solve(solvers, p, diva=False, cold_start=True)
+            walls.append(wall)
+    for sv in solvers:
+        sv.close()
+    n = len(members)
+    value = n / (statistics.mean(walls) / 1000.0)
+    line = {"metric": "ensemble SSA velocity solves/s, members side by side, 1xGB300", "value": round(value, 4),
+            "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": 1,
+            "ms_per_step": round(statistics.mean(walls), 2), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic ensemble geometries from seeded random fields on generated meshes (no files)",
+            "config": {"workload": ENSEMBLE_WORKLOAD, "members": n, "vertices": [m.nV for m, _, _ in members],
+                       "total_vertices": int(sum(m.nV for m, _, _ in members)), "rows_per_warp": tune},
+            "one_after_another": {"value": round(n / (seq_ms / 1000.0), 4), "unit": UNIT,
+                                  "ms": round(seq_ms, 1)},
+            "speedup_side_by_side": round(seq_ms / statistics.mean(walls), 3),
+            "picard_its": [a for a, b in its], "krylov_its": [b for a, b in its],
+            "clocks": clocks.summary()}
+    print(json.dumps(line))
+
+
 def _with(pkg, p, **kw):
     q = pkg.abi.default_params(**{f: getattr(p, f) for f, _ in p._fields_ if f != "reserved"})
     for k, v in kw.items():
@@ -712,9 +770,12 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--mixed-steps", type=int, default=1,
                     help="solves of the FP32+refinement path measured beside the headline")
-    ap.add_argument("--workload", default="diva", choices=["diva", "thermo", "learned"],
+    ap.add_argument("--workload", default="diva", choices=["diva", "thermo", "learned", "ensemble"],
                     help="diva: the headline velocity solve; thermo: the batched column thermodynamics; "
                          "learned: the learned Picard start on the SSA ensemble")
+    ap.add_argument("--ens-members", type=int, default=12)
+    ap.add_argument("--ens-min", type=int, default=20000)
+    ap.add_argument("--ens-max", type=int, default=120000)
     ap.add_argument("--learned-variants", type=int, default=8,
                     help="channel variants the learned start trains on before the timed region (0: skip)")
     ap.add_argument("--learned-nv", type=int, default=30000)
@@ -730,6 +791,8 @@ def main():
         (run_thermo_reference if args.impl == "reference" else run_thermo)(args)
     elif args.workload == "learned":
         run_learned(args)
+    elif args.workload == "ensemble":
+        run_ensemble(args)
     elif args.impl == "reference":
         run_reference(args)
     else:

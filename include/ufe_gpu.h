@@ -381,6 +381,21 @@ int32_t ufe_zeta_operators(int32_t nz, const double *zeta, double *ddz_l, double
 int32_t ufe_tridiagonal_solve(ufe_ctx *ctx, int32_t n, int32_t nsys, const double *a, const double *b,
                               const double *c, const double *d, double *x);
 
+/* ---- ensembles ----------------------------------------------------------------------------------- */
+/* Solve n independent members, each a context on the same device with its mesh and resident ice
+ * state (ufe_ice_upload): every member's resident solve is queued on its own stream before any is
+ * waited for, so members of uneven size run side by side.  stats[i] (optional) per member;
+ * *wall_ms the time from the first launch to the last completion.  Returns the most severe
+ * member status.  No reference counterpart: the reference runs one solve at a time. */
+int32_t ufe_ensemble_solve(ufe_ctx *const *ctxs, int32_t n, const ufe_solver_params *p, int32_t diva,
+                           int32_t cold_start, ufe_solve_stats *stats, double *wall_ms);
+
+/* Autotuner: time the FP64 Krylov kernels of the system the last solve on ctx assembled with each
+ * rows-per-warp choice (1 -- with the sliced-ELL layout --, 2, 4, 8) and keep the fastest for the
+ * context's later solves.  *lanes receives the choice; us[0..3] (optional) the measured
+ * microseconds per iteration of each. */
+int32_t ufe_autotune(ufe_ctx *ctx, int32_t repeats, int32_t *lanes, double *us);
+
 /* ---- learned Picard start: tensor-core building block ----------------------------------------- */
 /* Y[M x N] = X[M x K] * W[N x K]^T with BF16 X and W (raw 16-bit patterns, row-major) and FP32 Y,
  * on the tcgen05 tensor cores (one 128-row tile per CTA, accumulator in tensor memory).  M a

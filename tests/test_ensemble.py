@@ -1,0 +1,49 @@
+"""Ensembles (members of uneven size solved side by side) and the per-mesh autotuner."""
+import numpy as np
+import pytest
+
+
+def _members(pkg, sizes=(1500, 3000, 6000)):
+    out = []
+    for k, nv in enumerate(sizes):
+        mesh = pkg.geometry.ensemble_mesh(nV=nv, seed=k)
+        ice, p = pkg.geometry.ensemble_member(mesh, 40 + k)
+        out.append((mesh, ice, p))
+    return out
+
+
+@pytest.mark.gpu
+def test_ensemble_matches_individual_solves(pkg, gpu_lib):
+    members = _members(pkg)
+    p = members[0][2]
+    solvers = [pkg.VelocitySolver(m) for m, _, _ in members]
+    try:
+        single = []
+        for sv, (m, ice, _) in zip(solvers, members):
+            sv.ice_upload(ice)
+            st = sv.solve_resident(p, diva=False, cold_start=True)
+            single.append((st, np.r_[sv.velocity_download()]))
+        stats, wall = pkg.ensemble_solve(solvers, p, diva=False, cold_start=True)
+        assert wall > 0
+        for (st1, u1), st2, sv in zip(single, stats, solvers):
+            assert st2["n_visc_its"] == st1["n_visc_its"] and st2["n_Axb_its"] == st1["n_Axb_its"]
+            assert np.array_equal(np.r_[sv.velocity_download()], u1)   # deterministic: bit for bit
+    finally:
+        for sv in solvers:
+            sv.close()
+
+
+@pytest.mark.gpu
+def test_autotune_choice_keeps_the_solution(pkg, gpu_lib):
+    mesh, ice, p = _members(pkg, sizes=(4000,))[0]
+    p.stress_balance_PETSc_rtol = 1e-12
+    p.stress_balance_PETSc_abstol = 0.0
+    with pkg.VelocitySolver(mesh) as sv:
+        sv.ice_upload(ice)
+        sv.solve_resident(p, diva=False, cold_start=True)
+        u0 = np.r_[sv.velocity_download()]
+        lanes, us = sv.autotune(repeats=10)
+        assert lanes in (1, 2, 4, 8) and (us > 0).all() and us[[1, 2, 4, 8].index(lanes)] == us.min()
+        sv.solve_resident(p, diva=False, cold_start=True)
+        u1 = np.r_[sv.velocity_download()]
+        assert np.linalg.norm(u1 - u0) / np.linalg.norm(u0) < 1e-8

@@ -7,7 +7,7 @@ which registers it as ``ufemism_gb300``.
 """
 from . import abi, mesh, geometry  # noqa: F401
 from .build import build  # noqa: F401
-from .solver import CSR, UfeError, VelocitySolver, new_diva_state, new_ssa_state  # noqa: F401
+from .solver import CSR, UfeError, VelocitySolver, ensemble_solve, new_diva_state, new_ssa_state  # noqa: F401
 from .thermo import ColumnSolver, zeta_operators  # noqa: F401
 from . import thermo  # noqa: F401
 from . import learned  # noqa: F401

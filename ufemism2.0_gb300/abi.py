@@ -298,6 +298,9 @@ EXPORTS = {
     "ufe_tridiagonal_solve": (C.c_int32, [C.c_void_p, C.c_int32, C.c_int32, dptr, dptr, dptr, dptr, dptr]),
     "ufe_umma_gemm_bf16": (C.c_int32, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p,
                                        C.c_void_p]),
+    "ufe_ensemble_solve": (C.c_int32, [C.POINTER(C.c_void_p), C.c_int32, C.POINTER(SolverParams), C.c_int32,
+                                       C.c_int32, C.POINTER(SolveStats), dptr]),
+    "ufe_autotune": (C.c_int32, [C.c_void_p, C.c_int32, iptr, dptr]),
     "ufe_gnn_param_count": (C.c_int32, []),
     "ufe_gnn_create": (C.c_int32, [C.c_void_p, C.c_uint64, C.POINTER(C.c_void_p)]),
     "ufe_gnn_destroy": (None, [C.c_void_p]),

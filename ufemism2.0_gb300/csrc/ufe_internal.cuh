@@ -105,6 +105,10 @@ struct ufe_ctx {
   struct Work *work = nullptr;
   // thermodynamics workspace and resident heat-equation state (ufe_thermo.cu)
   struct ThermoWork *thermo = nullptr;
+  // rows per warp of the block-row Krylov kernels for this mesh (0: the default; ufe_autotune)
+  int32_t lanes = 0;
+  // the persistent FP32 inner solve needs the whole GPU; ensembles switch it off for the member
+  bool allow_persistent = true;
 
   ReduceArea red;
 };

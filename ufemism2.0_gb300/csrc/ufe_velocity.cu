@@ -998,13 +998,13 @@ void free_work(ufe_ctx *ctx) {
 }
 
 int32_t bsr_lanes(ufe_ctx *ctx) {
+  if (ctx && ctx->lanes > 0) return ctx->lanes;   // chosen by ufe_autotune for this mesh
   static int lanes = -1;
   if (lanes < 0) {
     const char *e = getenv("UFE_BSR_LANES");
     int v = e ? atoi(e) : 1;
     lanes = (v == 1 || v == 2 || v == 4 || v == 8) ? v : 1;
   }
-  (void)ctx;
   return lanes;
 }
 
@@ -1388,7 +1388,7 @@ cudaGraphExec_t build_picard_graph(Solver &S, bool diva) {
     if (S.p.precision == UFE_PREC_FP32_REFINE) {
       // refinement loop: inner FP32 BiCGStab, then x += d and the FP64 residual test
       cudaGraphNode_t wi;
-      if (persistent_krylov()) {
+      if (persistent_krylov() && S.ctx->allow_persistent) {
         CondArg none{0, 0};
         auto ii = capture_into(S.s, kbody, {}, [&] {
           S.enqueue_inner_init(none);
@@ -1440,7 +1440,7 @@ void run_picard_host(Solver &S, bool diva) {
         UFE_CUDA(cudaStreamSynchronize(S.s));
         if (!w->ks_host[0].active) break;
         S.enqueue_inner_init(none);
-        if (persistent_krylov()) {
+        if (persistent_krylov() && S.ctx->allow_persistent) {
           S.enqueue_inner_persist();
         } else {
           for (;;) {
@@ -1515,17 +1515,18 @@ int32_t check_err_flag(Solver &S) {
   return UFE_OK;
 }
 
-// Run a resident Picard solve; fills stats; returns the status.
-int32_t run_picard(ufe_ctx *ctx, const ufe_solver_params &p, bool diva, ufe_solve_stats *stats) {
+// A resident Picard solve in two halves: picard_launch queues the whole solve on the context's
+// stream (graph or host loop) and the copies of its scalars; picard_collect waits for it and
+// reads the result.  Ensembles launch all members before collecting any.
+void picard_launch(ufe_ctx *ctx, const ufe_solver_params &p, bool diva) {
   Solver S(ctx, p);
   Work *w = S.w;
   UFE_REQUIRE(ctx->nz <= kMaxNz, UFE_ERR_CAPACITY, "nz exceeds 64 layers");
-  const int law = p.choice_sliding_law;
   cudaEventRecord(ctx->ev0, S.s);
   if (use_graphs()) {
     cudaGraphExec_t *gx = diva ? &w->graph_diva : &w->graph_ssa;
     uint64_t *key = diva ? &w->graph_diva_key : &w->graph_ssa_key;
-    uint64_t k = params_key(p, S.lanes, w->has_bc);
+    uint64_t k = params_key(p, S.lanes, w->has_bc) ^ (ctx->allow_persistent ? 0x5bd1e995ull : 0ull);
     if (!*gx || *key != k) {
       if (*gx) cudaGraphExecDestroy(*gx);
       *gx = nullptr;
@@ -1539,13 +1540,17 @@ int32_t run_picard(ufe_ctx *ctx, const ufe_solver_params &p, bool diva, ufe_solv
   cudaEventRecord(ctx->ev1, S.s);
   UFE_CUDA(cudaMemcpyAsync(w->ps_host, w->ps, sizeof(PicardScalars), cudaMemcpyDeviceToHost, S.s));
   UFE_CUDA(cudaMemcpyAsync(w->ks_host, w->ks, sizeof(KrylovScalars) * 2, cudaMemcpyDeviceToHost, S.s));
+}
+
+int32_t picard_collect(ufe_ctx *ctx, const ufe_solver_params &p, ufe_solve_stats *stats) {
+  Solver S(ctx, p);
+  Work *w = S.w;
   UFE_CUDA(cudaStreamSynchronize(S.s));
   check_err_flag(S);
   const PicardScalars ps = *w->ps_host;
   const KrylovScalars ks = w->ks_host[0];
   float ms = 0.f;
   cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
-  (void)law;
   int32_t total_its = w->ks_host[1].total_its + ks.total_its;
   if (stats) {
     memset(stats, 0, sizeof(*stats));
@@ -1559,6 +1564,12 @@ int32_t run_picard(ufe_ctx *ctx, const ufe_solver_params &p, bool diva, ufe_solv
     stats->n_fp64_its = ks.total_its;
   }
   return ps.status;
+}
+
+// Run a resident Picard solve; fills stats; returns the status.
+int32_t run_picard(ufe_ctx *ctx, const ufe_solver_params &p, bool diva, ufe_solve_stats *stats) {
+  picard_launch(ctx, p, diva);
+  return picard_collect(ctx, p, stats);
 }
 
 }  // namespace
@@ -1638,6 +1649,32 @@ static void check_sliding_inputs(const ufe_solver_params *p, const ufe_ice_state
       break;
     default: break;
   }
+}
+
+// Queue a resident solve; false when there is nothing to solve (no grounded ice), in which
+// case the zero velocity is already set and the stats are zero.
+static bool resident_launch(ufe_ctx *ctx, const ufe_solver_params *p, int32_t cold_start, bool diva) {
+  validate_params(p);
+  UFE_CUDA(cudaSetDevice(ctx->device));
+  Work *w = ensure_work(ctx);
+  cudaStream_t s = ctx->stream;
+  const int nTri = ctx->nTri;
+  if (cold_start) {
+    UFE_CUDA(cudaMemsetAsync(w->uv, 0, sizeof(double2) * nTri, s));
+    if (diva) {
+      UFE_CUDA(cudaMemsetAsync(w->uv_base, 0, sizeof(double2) * nTri, s));
+      UFE_CUDA(cudaMemsetAsync(w->tau_b, 0, sizeof(double2) * nTri, s));
+      UFE_CUDA(cudaMemsetAsync(w->eta_3D_b, 0, sizeof(double) * (size_t)nTri * ctx->nz, s));
+    }
+  }
+  bool skip = !w->any_grounded || (!diva && p->choice_sliding_law == UFE_SLIDING_NO_SLIDING);
+  if (skip) {
+    UFE_CUDA(cudaMemsetAsync(w->uv, 0, sizeof(double2) * nTri, s));
+    if (diva) UFE_CUDA(cudaMemsetAsync(w->uv_base, 0, sizeof(double2) * nTri, s));
+    return false;
+  }
+  picard_launch(ctx, *p, diva);
+  return true;
 }
 
 static int32_t resident_solve(ufe_ctx *ctx, const ufe_solver_params *p, int32_t cold_start, bool diva,
@@ -1796,6 +1833,96 @@ extern "C" int32_t ufe_solve_ssa_resident(ufe_ctx *ctx, const ufe_solver_params 
 extern "C" int32_t ufe_solve_diva_resident(ufe_ctx *ctx, const ufe_solver_params *p, int32_t cold_start,
                                            ufe_solve_stats *stats) {
   return guarded(ctx, [&]() -> int32_t { return resident_solve(ctx, p, cold_start, true, stats); });
+}
+
+// Many independent members, each a context with its mesh and resident ice state (on one device):
+// every member's solve is queued on its own stream before any is waited for, so the members of
+// uneven size run side by side.  The persistent FP32 kernel (which needs the whole GPU) is not
+// used inside an ensemble.
+extern "C" int32_t ufe_ensemble_solve(ufe_ctx *const *ctxs, int32_t n, const ufe_solver_params *p, int32_t diva,
+                                      int32_t cold_start, ufe_solve_stats *stats, double *wall_ms) {
+  if (!ctxs || n < 1 || !p) return UFE_ERR_INVALID;
+  for (int32_t i = 0; i < n; ++i)
+    if (!ctxs[i] || ctxs[i]->device != ctxs[0]->device) return UFE_ERR_INVALID;
+  std::vector<char> launched(n, 0);
+  std::vector<int32_t> rc(n, UFE_OK);
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  if (cudaSetDevice(ctxs[0]->device) != cudaSuccess || cudaEventCreate(&e0) != cudaSuccess ||
+      cudaEventCreate(&e1) != cudaSuccess)
+    return UFE_ERR_DEVICE;
+  cudaEventRecord(e0, ctxs[0]->stream);
+  for (int32_t i = 0; i < n; ++i) {
+    ufe_ctx *c = ctxs[i];
+    if (i > 0) cudaStreamWaitEvent(c->stream, e0, 0);
+    rc[i] = guarded(c, [&]() -> int32_t {
+      c->allow_persistent = false;
+      launched[i] = resident_launch(c, p, cold_start, diva != 0) ? 1 : 0;
+      return UFE_OK;
+    });
+  }
+  for (int32_t i = 0; i < n; ++i) {
+    ufe_ctx *c = ctxs[i];
+    if (rc[i] < 0) continue;
+    rc[i] = guarded(c, [&]() -> int32_t {
+      if (!launched[i]) {
+        UFE_CUDA(cudaStreamSynchronize(c->stream));
+        if (stats) memset(&stats[i], 0, sizeof(ufe_solve_stats));
+        return UFE_OK;
+      }
+      return picard_collect(c, *p, stats ? &stats[i] : nullptr);
+    });
+    if (i > 0) {
+      cudaEvent_t done;
+      if (cudaEventCreateWithFlags(&done, cudaEventDisableTiming) == cudaSuccess) {
+        cudaEventRecord(done, c->stream);
+        cudaStreamWaitEvent(ctxs[0]->stream, done, 0);
+        cudaEventDestroy(done);
+      }
+    }
+  }
+  for (int32_t i = 0; i < n; ++i) ctxs[i]->allow_persistent = true;
+  cudaEventRecord(e1, ctxs[0]->stream);
+  cudaEventSynchronize(e1);
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, e0, e1);
+  if (wall_ms) *wall_ms = ms;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  int32_t worst = UFE_OK;
+  for (int32_t i = 0; i < n; ++i) {
+    if (rc[i] < 0 && (worst >= 0 || rc[i] < worst)) worst = rc[i];
+    else if (worst >= 0 && rc[i] > worst) worst = rc[i];
+  }
+  return worst;
+}
+
+// The autotuner: for this mesh, time the three FP64 Krylov kernels with each rows-per-warp
+// choice (1 with the sliced-ELL layout, 2, 4, 8) on the system the last solve assembled, and keep
+// the fastest for this context's later solves.  us (optional, 4 entries): the measured
+// per-iteration microseconds of each choice.
+extern "C" int32_t ufe_autotune(ufe_ctx *ctx, int32_t repeats, int32_t *lanes_out, double *us) {
+  return guarded(ctx, [&]() -> int32_t {
+    UFE_REQUIRE(ctx->work, UFE_ERR_INVALID, "autotune: run a solve on this context first");
+    const int choices[4] = {1, 2, 4, 8};
+    double best = 1e300;
+    int best_l = 1;
+    for (int c = 0; c < 4; ++c) {
+      ctx->lanes = choices[c];
+      double t[3] = {0, 0, 0};
+      int64_t geo[2];
+      const int32_t rc = ufe_profile_krylov_kernels(ctx, UFE_PREC_FP64, repeats > 0 ? repeats : 20, t, geo);
+      UFE_REQUIRE(rc == UFE_OK, rc, "autotune: kernel timing failed");
+      const double it = t[0] + t[1] + t[2];
+      if (us) us[c] = it;
+      if (it < best) {
+        best = it;
+        best_l = choices[c];
+      }
+    }
+    ctx->lanes = best_l;
+    if (lanes_out) *lanes_out = best_l;
+    return UFE_OK;
+  });
 }
 
 static void download_pair(ufe_ctx *ctx, const double2 *src, double *a, double *b) {
@@ -2005,7 +2132,7 @@ extern "C" int32_t ufe_solve_linearised(ufe_ctx *ctx, const ufe_solver_params *p
         UFE_CUDA(cudaStreamSynchronize(S.s));
         if (!w->ks_host[0].active) break;
         S.enqueue_inner_init(none);
-        if (persistent_krylov()) {
+        if (persistent_krylov() && S.ctx->allow_persistent) {
           S.enqueue_inner_persist();
         } else {
           for (;;) {

@@ -261,6 +261,14 @@ class VelocitySolver:
         self._check(self.lib.ufe_profile_krylov_kernels(self.ctx, precision, repeats, abi.as_d(us), geo))
         return us, (geo[0], geo[1])
 
+    def autotune(self, repeats: int = 20):
+        """Pick the rows per warp of the Krylov kernels for this mesh (after a solve); returns
+        (choice, microseconds per iteration for 1, 2, 4, 8)."""
+        lanes = C.c_int32()
+        us = np.zeros(4)
+        self._check(self.lib.ufe_autotune(self.ctx, repeats, C.byref(lanes), abi.as_d(us)))
+        return lanes.value, us
+
     def velocity_download(self):
         u, v = np.zeros(self.mesh.nTri), np.zeros(self.mesh.nTri)
         self._check(self.lib.ufe_velocity_download(self.ctx, abi.as_d(u), abi.as_d(v)))
@@ -312,3 +320,19 @@ def new_diva_state(nTri, nz, with_3d=True):
         d["u_3D_b"] = np.zeros((nTri, nz), order="F")
         d["v_3D_b"] = np.zeros((nTri, nz), order="F")
     return d
+
+
+def ensemble_solve(solvers, params, diva: bool, cold_start: bool = True):
+    """ufe_ensemble_solve over VelocitySolvers with their ice states uploaded; returns
+    (list of stats dicts, wall milliseconds).  A negative status raises UfeError."""
+    lib = abi.load_library()
+    n = len(solvers)
+    arr = (C.c_void_p * n)(*[sv.ctx.value for sv in solvers])
+    stats = (abi.SolveStats * n)()
+    wall = C.c_double()
+    rc = lib.ufe_ensemble_solve(arr, n, C.byref(params), 1 if diva else 0, 1 if cold_start else 0, stats,
+                                C.byref(wall))
+    if rc < 0:
+        msgs = [(lib.ufe_ctx_last_error(sv.ctx) or b"").decode() for sv in solvers]
+        raise UfeError(rc, "; ".join(m for m in msgs if m))
+    return [st.as_dict() for st in stats], wall.value
