@@ -25,9 +25,18 @@ def test_ensemble_matches_individual_solves(pkg, gpu_lib):
             single.append((st, np.r_[sv.velocity_download()]))
         stats, wall = pkg.ensemble_solve(solvers, p, diva=False, cold_start=True)
         assert wall > 0
+        # a lone solve may run its Krylov loop as one persistent launch (the whole GPU); ensemble
+        # members share the GPU and use the three-kernel loop: same iteration, other reduction order
         for (st1, u1), st2, sv in zip(single, stats, solvers):
-            assert st2["n_visc_its"] == st1["n_visc_its"] and st2["n_Axb_its"] == st1["n_Axb_its"]
-            assert np.array_equal(np.r_[sv.velocity_download()], u1)   # deterministic: bit for bit
+            assert st2["n_visc_its"] == st1["n_visc_its"]
+            assert abs(st2["n_Axb_its"] - st1["n_Axb_its"]) <= 0.05 * st1["n_Axb_its"]
+            u2 = np.r_[sv.velocity_download()]
+            assert np.linalg.norm(u2 - u1) / np.linalg.norm(u1) < 2e-5   # Krylov abstol 1e-5
+        # the ensemble itself is deterministic: a second run repeats it bit for bit
+        first = [np.r_[sv.velocity_download()] for sv in solvers]
+        pkg.ensemble_solve(solvers, p, diva=False, cold_start=True)
+        for u, sv in zip(first, solvers):
+            assert np.array_equal(np.r_[sv.velocity_download()], u)
     finally:
         for sv in solvers:
             sv.close()

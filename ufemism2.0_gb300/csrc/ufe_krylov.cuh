@@ -695,24 +695,27 @@ __global__ void __launch_bounds__(kPersistThreads) k_bicgstab_persist(M mat, KV<
   if (blockIdx.x == 0 && threadIdx.x == 0) *ks = s;
 }
 
-// ---- persistent FP32 BiCGStab with shared-memory neighbourhoods -------------------------------
+// ---- persistent BiCGStab with shared-memory neighbourhoods (FP32 inner and FP64 solves) --------
 // Block b owns the contiguous block rows [b*rpb, (b+1)*rpb) (whole sliced-ELL slices; the rows are
 // in Z order, so they form a compact patch of the mesh).  Each SpMV phase first stages, into
 // shared memory, the vector its rows read: its own rows (coalesced) and the patch's halo rows
 // (listed once per mesh), computing the on-the-fly update (p, or s = r - alpha v) once per staged
 // entry; the rows then read neighbours from shared memory through per-slot local indices.
-struct HaloDiffMat {
+template <class Blk>
+struct HaloMat {
   int32_t items;
   int32_t rpb;                          // rows per block (a multiple of 32)
   const int32_t *__restrict__ soff;     // sliced-ELL slice offsets
   const int32_t *__restrict__ lcol;     // local index (own rows, then halo) per slot
-  const float4 *__restrict__ sblk;      // FP32 blocks per slot
-  const float4 *__restrict__ rowsum;    // FP64 row sums rounded to FP32
+  const Blk *__restrict__ sblk;         // blocks per slot
+  const float4 *__restrict__ rowsum;    // FP32 difference form: FP64 row sums rounded to FP32
   const int32_t *__restrict__ halo_off; // gridDim.x + 1
   const int32_t *__restrict__ halo_idx; // global rows of each block's halo
 };
+using HaloDiffMat = HaloMat<float4>;
 
-__device__ __forceinline__ float2 halo_row(const HaloDiffMat &m, int i, int il, const float2 *tab) {
+// FP32 difference form: y_i = S_i x_i + sum_j A_ij (x_j - x_i)
+__device__ __forceinline__ float2 halo_row(const HaloMat<float4> &m, int i, int il, const float2 *tab) {
   const float2 xi = tab[il];
   const float4 sr = m.rowsum[i];
   float2 y = make_float2(fmaf(sr.y, xi.y, sr.x * xi.x), fmaf(sr.w, xi.y, sr.z * xi.x));
@@ -748,9 +751,45 @@ __device__ __forceinline__ float2 halo_row(const HaloDiffMat &m, int i, int il, 
   return y;
 }
 
-static __global__ void __launch_bounds__(kPersistThreads) k_bicgstab32_halo(HaloDiffMat m, KV<float2> v, KrylovScalars *ks,
-                                                                      double *part, GridSync *gs) {
-  extern __shared__ float2 tab[];
+// FP64 plain form, summed in the row's storage order
+__device__ __forceinline__ double2 halo_row(const HaloMat<double4> &m, int i, int il, const double2 *tab) {
+  double2 y = make_double2(0.0, 0.0);
+  const int sl = i >> 5;
+  const int s0 = __ldg(m.soff + sl), w = (__ldg(m.soff + sl + 1) - s0) >> 5;
+  const int base = s0 + (i & 31);
+  int k = 0;
+  for (; k + 4 <= w; k += 4) {
+    int c[4];
+    double4 a[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int slot = base + ((k + u) << 5);
+      c[u] = __ldg(m.lcol + slot);
+      a[u] = m.sblk[slot];
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const double2 x = tab[c[u]];
+      y.x = fma(a[u].y, x.y, fma(a[u].x, x.x, y.x));
+      y.y = fma(a[u].w, x.y, fma(a[u].z, x.x, y.y));
+    }
+  }
+  for (; k < w; ++k) {
+    const int slot = base + (k << 5);
+    const double4 a = m.sblk[slot];
+    const double2 x = tab[__ldg(m.lcol + slot)];
+    y.x = fma(a.y, x.y, fma(a.x, x.x, y.x));
+    y.y = fma(a.w, x.y, fma(a.z, x.x, y.y));
+  }
+  return y;
+}
+
+template <class Vec, class Blk>
+__global__ void __launch_bounds__(kPersistThreads) k_bicgstab_halo(HaloMat<Blk> m, KV<Vec> v, KrylovScalars *ks,
+                                                                   double *part, GridSync *gs) {
+  using R = typename ScalarOf<Vec>::T;
+  extern __shared__ __align__(16) unsigned char tab_raw[];
+  Vec *tab = reinterpret_cast<Vec *>(tab_raw);
   KrylovScalars s = *ks;
   if (!s.active) return;
   double *partP = part, *partS = part + kPersistMaxBlocks * kPersistSlots,
@@ -766,12 +805,12 @@ static __global__ void __launch_bounds__(kPersistThreads) k_bicgstab32_halo(Halo
     const int cur = s.it & 1, nxt = cur ^ 1;
     // -- p <- r - beta omega v + beta p (staged);  v <- D^-1 A p;  (v, r^)
     {
-      const float beta = (float)s.beta, bw = (float)(s.beta * s.omegaold);
-      const float2 *__restrict__ Po = v.P[cur];
-      const float2 *__restrict__ Vo = v.V[cur];
+      const R beta = (R)s.beta, bw = (R)(s.beta * s.omegaold);
+      const Vec *__restrict__ Po = v.P[cur];
+      const Vec *__restrict__ Vo = v.V[cur];
       for (int e = threadIdx.x; e < nloc; e += blockDim.x) {
         const int g = e < own ? r0 + e : __ldg(m.halo_idx + h0 + e - own);
-        const float2 pn = v_pupd(v.R[g], bw, Vo[g], beta, Po[g]);
+        const Vec pn = v_pupd(v.R[g], bw, Vo[g], beta, Po[g]);
         tab[e] = pn;
         if (e < own) v.P[nxt][g] = pn;
       }
@@ -779,7 +818,7 @@ static __global__ void __launch_bounds__(kPersistThreads) k_bicgstab32_halo(Halo
       double acc[1] = {0.0};
       for (int il = threadIdx.x; il < own; il += blockDim.x) {
         const int i = r0 + il;
-        const float2 vn = v_mul(v.dinv[i], halo_row(m, i, il, tab));
+        const Vec vn = v_mul(v.dinv[i], halo_row(m, i, il, tab));
         v.V[nxt][i] = vn;
         acc[0] += v_dot(vn, v.RP[i]);
       }
@@ -797,11 +836,11 @@ static __global__ void __launch_bounds__(kPersistThreads) k_bicgstab32_halo(Halo
     }
     // -- s <- r - alpha v (staged);  t <- D^-1 A s;  (s,t), (t,t), (s,s)
     {
-      const float alpha = (float)s.alpha;
-      const float2 *__restrict__ Vn = v.V[nxt];
+      const R alpha = (R)s.alpha;
+      const Vec *__restrict__ Vn = v.V[nxt];
       for (int e = threadIdx.x; e < nloc; e += blockDim.x) {
         const int g = e < own ? r0 + e : __ldg(m.halo_idx + h0 + e - own);
-        const float2 sv = v_sub_scaled(v.R[g], alpha, Vn[g]);
+        const Vec sv = v_sub_scaled(v.R[g], alpha, Vn[g]);
         tab[e] = sv;
         if (e < own) v.S[g] = sv;
       }
@@ -809,8 +848,8 @@ static __global__ void __launch_bounds__(kPersistThreads) k_bicgstab32_halo(Halo
       double acc[3] = {0.0, 0.0, 0.0};
       for (int il = threadIdx.x; il < own; il += blockDim.x) {
         const int i = r0 + il;
-        const float2 si = tab[il];
-        const float2 ti = v_mul(v.dinv[i], halo_row(m, i, il, tab));
+        const Vec si = tab[il];
+        const Vec ti = v_mul(v.dinv[i], halo_row(m, i, il, tab));
         v.T[i] = ti;
         acc[0] += v_dot(si, ti);
         acc[1] += v_dot(ti, ti);
@@ -834,13 +873,13 @@ static __global__ void __launch_bounds__(kPersistThreads) k_bicgstab32_halo(Halo
     }
     // -- x <- x + alpha p + omega s;  r <- s - omega t;  (r, r^), (r, r)
     {
-      const float alpha = (float)s.alpha, omega = (float)s.omega;
+      const R alpha = (R)s.alpha, omega = (R)s.omega;
       double acc[2] = {0.0, 0.0};
       for (int il = threadIdx.x; il < own; il += blockDim.x) {
         const int i = r0 + il;
-        const float2 pi = v.P[nxt][i], si = v.S[i], ti = v.T[i];
+        const Vec pi = v.P[nxt][i], si = v.S[i], ti = v.T[i];
         v.X[i] = v_xupd(v.X[i], alpha, pi, omega, si);
-        const float2 ri = v_sub_scaled(si, omega, ti);
+        const Vec ri = v_sub_scaled(si, omega, ti);
         v.R[i] = ri;
         acc[0] += v_dot(ri, v.RP[i]);
         acc[1] += v_dot(ri, ri);

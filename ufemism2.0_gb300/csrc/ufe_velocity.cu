@@ -1013,6 +1013,12 @@ int32_t bsr_lanes(ufe_ctx *ctx) {
 
 namespace {
 
+__global__ void k_reset_gsync(GridSync *g) {
+  g->count = 0u;
+  g->gen = 0u;
+  g->err = 0;
+}
+
 // The FP32 inner BiCGStab runs as one persistent launch unless UFE_NO_PERSIST=1.
 bool persistent_krylov() {
   static int v = -1;
@@ -1191,7 +1197,8 @@ struct Solver {
     const size_t smem = (size_t)w->halo_maxlocal * sizeof(float2);
     static size_t attr = 0;
     if (smem > attr) {
-      UFE_CUDA(cudaFuncSetAttribute(k_bicgstab32_halo, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      UFE_CUDA(cudaFuncSetAttribute(k_bicgstab_halo<float2, float4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)smem));
       attr = smem;
     }
     HaloDiffMat m{w->nTri, w->halo_rpb, w->sell_off, w->halo_lcol, w->sell_blk32, w->rowsum32, w->halo_off,
@@ -1199,7 +1206,8 @@ struct Solver {
     cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
     UFE_CUDA(cudaStreamIsCapturing(s, &cap));
     if (cap != cudaStreamCaptureStatusNone) {
-      k_bicgstab32_halo<<<w->halo_G, kPersistThreads, smem, s>>>(m, kv_inner(), w->ks + 1, w->ppart, w->gsync);
+      k_bicgstab_halo<float2, float4><<<w->halo_G, kPersistThreads, smem, s>>>(m, kv_inner(), w->ks + 1, w->ppart,
+                                                                              w->gsync);
       UFE_CUDA(cudaGetLastError());
       return;
     }
@@ -1213,7 +1221,44 @@ struct Solver {
     attr1[0].val.cooperative = 1;
     cfg.attrs = attr1;
     cfg.numAttrs = 1;
-    UFE_CUDA(cudaLaunchKernelEx(&cfg, k_bicgstab32_halo, m, kv_inner(), w->ks + 1, w->ppart, w->gsync));
+    UFE_CUDA(cudaLaunchKernelEx(&cfg, k_bicgstab_halo<float2, float4>, m, kv_inner(), w->ks + 1, w->ppart, w->gsync));
+  }
+  // the FP64 solve as one persistent launch with shared-memory patches (the plain FP64 path)
+  bool halo64_ok() const {
+    return persistent_krylov() && ctx->allow_persistent && use_sell() && lanes == 1 && w->halo_G > 0 &&
+           (size_t)w->halo_maxlocal * sizeof(double2) <= 160 * 1024 && !getenv("UFE_NO_HALO");
+  }
+  void enqueue_outer_halo64() {
+    const size_t smem = (size_t)w->halo_maxlocal * sizeof(double2);
+    static size_t attr = 0;
+    if (smem > attr) {
+      UFE_CUDA(cudaFuncSetAttribute(k_bicgstab_halo<double2, double4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)smem));
+      attr = smem;
+    }
+    HaloMat<double4> m{w->nTri, w->halo_rpb, w->sell_off, w->halo_lcol, w->sell_blk, nullptr, w->halo_off,
+                       w->halo_idx};
+    k_reset_gsync<<<1, 1, 0, s>>>(w->gsync);
+    UFE_CUDA(cudaGetLastError());
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    UFE_CUDA(cudaStreamIsCapturing(s, &cap));
+    if (cap != cudaStreamCaptureStatusNone) {
+      k_bicgstab_halo<double2, double4><<<w->halo_G, kPersistThreads, smem, s>>>(m, kv64(), w->ks, w->ppart,
+                                                                                 w->gsync);
+      UFE_CUDA(cudaGetLastError());
+      return;
+    }
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(w->halo_G);
+    cfg.blockDim = dim3(kPersistThreads);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeCooperative;
+    at[0].val.cooperative = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    UFE_CUDA(cudaLaunchKernelEx(&cfg, k_bicgstab_halo<double2, double4>, m, kv64(), w->ks, w->ppart, w->gsync));
   }
   template <int L>
   void inner_persist_l() {
@@ -1379,6 +1424,17 @@ cudaGraphExec_t build_picard_graph(Solver &S, bool diva) {
     cudaGraph_t body;
     add_while(g, sinks, h_outer, &body);
     CondArg outer{h_outer, 1};
+    if (S.p.precision != UFE_PREC_FP32_REFINE && S.halo64_ok()) {
+      // FP64: the whole Krylov solve of a Picard iteration is one persistent launch
+      CondArg none{0, 0};
+      auto pre = capture_into(S.s, body, {}, [&] { S.enqueue_picard_pre(diva, none); });
+      auto ks = capture_into(S.s, body, pre, [&] { S.enqueue_outer_halo64(); });
+      capture_into(S.s, body, ks, [&] { S.enqueue_picard_post(diva, outer); });
+      cudaGraphExec_t exec;
+      UFE_CUDA(cudaGraphInstantiate(&exec, g, 0));
+      cudaGraphDestroy(g);
+      return exec;
+    }
     cudaGraphConditionalHandle h_inner;
     UFE_CUDA(cudaGraphConditionalHandleCreate(&h_inner, body, 0, 0));
     CondArg inner{h_inner, 1};
@@ -1451,6 +1507,9 @@ void run_picard_host(Solver &S, bool diva) {
           }
         }
         S.enqueue_refine_update(none);
+      } else if (S.halo64_ok()) {
+        S.enqueue_outer_halo64();
+        break;
       } else {
         for (int c = 0; c < 8; ++c) S.krylov_iter64(none);
         UFE_CUDA(cudaMemcpyAsync(w->ks_host, w->ks, sizeof(KrylovScalars), cudaMemcpyDeviceToHost, S.s));
