@@ -171,7 +171,10 @@ typedef struct {
   double  device_ms;        /* device time of the solve                                   */
   int32_t n_fp64_its;       /* of n_Axb_its: FP64 BiCGStab iterations (all of them with    */
                             /* UFE_PREC_FP64; the fallback solves with UFE_PREC_FP32_REFINE) */
-  int32_t reserved[5];
+  int32_t n_kernels;        /* kernels the solve launched, counted from the kernel nodes of  */
+                            /* its graph (-1 where loops inside a Picard iteration make the  */
+                            /* count data dependent, or without graphs)                      */
+  int32_t reserved[4];
 } ufe_solve_stats;
 
 /* ---- context ------------------------------------------------------------------------------- */
@@ -266,6 +269,11 @@ int32_t ufe_solve_ssa_resident(ufe_ctx *ctx, const ufe_solver_params *p, int32_t
 int32_t ufe_solve_diva_resident(ufe_ctx *ctx, const ufe_solver_params *p, int32_t cold_start,
                                 ufe_solve_stats *stats);
 int32_t ufe_velocity_download(ufe_ctx *ctx, double *u_b, double *v_b);
+
+/* Mean microseconds per iteration of the persistent Krylov kernel (the whole solve in one launch
+ * with shared-memory patches: the FP64 solve, or the FP32 inner solve) on the system the last solve
+ * on ctx assembled, running `iterations` iterations.  Measurement only. */
+int32_t ufe_profile_krylov_persistent(ufe_ctx *ctx, int32_t precision, int32_t iterations, double *us_per_iteration);
 
 /* ---- thermodynamics: implicit column temperature solve ---------------------------------------- */
 enum ufe_heat_capacity { UFE_CP_UNIFORM = 0, UFE_CP_POUNDER1965 = 1 };   /* choice_ice_heat_capacity        */
@@ -426,6 +434,9 @@ int32_t ufe_gnn_set_params(ufe_gnn *g, const float *params);          /* also re
 int32_t ufe_gnn_forward(ufe_gnn *g, int64_t n, const int32_t *nbr, const float *x, float *y);
 int32_t ufe_gnn_loss_grad(ufe_gnn *g, int64_t n, const int32_t *nbr, const float *x, const float *target,
                           const float *w, double *loss, float *grad);
+
+/* Kernels one ufe_gnn_predict_velocity call launches with this many smoothing passes. */
+int32_t ufe_gnn_predict_kernels(int32_t smooth_passes);
 
 /* The mesh path.  ufe_gnn_features: the 16 features of a mesh context's resident ice state (after
  * ufe_ice_upload), nTri x 16 in the caller's triangle order; use_prev_velocity = 0 zeroes the

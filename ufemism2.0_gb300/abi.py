@@ -80,7 +80,8 @@ class DivaState(C.Structure):
 class SolveStats(C.Structure):
     _fields_ = [("n_visc_its", C.c_int32), ("n_Axb_its", C.c_int32), ("n_refinements", C.c_int32),
                 ("status", C.c_int32), ("L2_uv", C.c_double), ("visc_it_relax_applied", C.c_double),
-                ("device_ms", C.c_double), ("n_fp64_its", C.c_int32), ("reserved", C.c_int32 * 5)]
+                ("device_ms", C.c_double), ("n_fp64_its", C.c_int32), ("n_kernels", C.c_int32),
+                ("reserved", C.c_int32 * 4)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}
@@ -285,6 +286,8 @@ EXPORTS = {
                                           C.c_void_p]),
     "ufe_solve_history": (C.c_int32, [C.c_void_p, dptr, C.c_int32, iptr]),
     "ufe_profile_krylov_kernels": (C.c_int32, [C.c_void_p, C.c_int32, C.c_int32, dptr, C.POINTER(C.c_int64)]),
+    "ufe_gnn_predict_kernels": (C.c_int32, [C.c_int32]),
+    "ufe_profile_krylov_persistent": (C.c_int32, [C.c_void_p, C.c_int32, C.c_int32, dptr]),
     "ufe_default_thermo_params": (None, [C.POINTER(ThermoParams)]),
     "ufe_thermo_step": (C.c_int32, [C.c_void_p, C.POINTER(ThermoParams), C.c_int32, C.c_int32, dptr,
                                     C.POINTER(ThermoColumns), dptr, iptr]),

@@ -1166,6 +1166,12 @@ extern "C" int32_t ufe_gnn_evaluate(ufe_gnn *g, double *mean_loss) {
 // resident velocity, so that ufe_solve_ssa_resident / ufe_solve_diva_resident with cold_start = 0
 // start the Picard loop from it; `smooth_passes` averaging passes over each triangle and its
 // neighbours take the prediction's small-scale noise out first.
+// Kernels one ufe_gnn_predict_velocity launches: graph, features, encoder, the layers, decoder,
+// velocity store, and two per smoothing pass.
+extern "C" int32_t ufe_gnn_predict_kernels(int32_t smooth_passes) {
+  return 1 + 1 + (2 + kLayers) + 1 + 2 * (smooth_passes > 0 ? smooth_passes : 0);
+}
+
 extern "C" int32_t ufe_gnn_predict_velocity(ufe_gnn *g, ufe_ctx *mesh_ctx, int32_t use_prev_velocity,
                                             int32_t smooth_passes, double *device_ms) {
   if (!g || !mesh_ctx) return UFE_ERR_INVALID;

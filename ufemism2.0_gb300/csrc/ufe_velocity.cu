@@ -1413,6 +1413,21 @@ uint64_t params_key(const ufe_solver_params &p, int lanes, int has_bc) {
   return h;
 }
 
+// Kernel nodes of a graph (not those inside its conditional bodies).
+int32_t count_kernel_nodes(cudaGraph_t g) {
+  size_t n = 0;
+  UFE_CUDA(cudaGraphGetNodes(g, nullptr, &n));
+  std::vector<cudaGraphNode_t> nodes(n);
+  if (n) UFE_CUDA(cudaGraphGetNodes(g, nodes.data(), &n));
+  int32_t k = 0;
+  for (size_t i = 0; i < n; ++i) {
+    cudaGraphNodeType t;
+    UFE_CUDA(cudaGraphNodeGetType(nodes[i], &t));
+    if (t == cudaGraphNodeTypeKernel) ++k;
+  }
+  return k;
+}
+
 // The whole Picard solve as one graph: prologue -> while(picard){ pre -> while(krylov){...} -> post }
 cudaGraphExec_t build_picard_graph(Solver &S, bool diva) {
   cudaGraph_t g;
@@ -1421,6 +1436,8 @@ cudaGraphExec_t build_picard_graph(Solver &S, bool diva) {
     cudaGraphConditionalHandle h_outer;
     UFE_CUDA(cudaGraphConditionalHandleCreate(&h_outer, g, 1, cudaGraphCondAssignDefault));
     auto sinks = capture_into(S.s, g, {}, [&] { S.enqueue_prologue(diva); });
+    S.w->graph_kernels_pro[diva] = count_kernel_nodes(g);
+    S.w->graph_kernels_it[diva] = -1;
     cudaGraph_t body;
     add_while(g, sinks, h_outer, &body);
     CondArg outer{h_outer, 1};
@@ -1430,6 +1447,7 @@ cudaGraphExec_t build_picard_graph(Solver &S, bool diva) {
       auto pre = capture_into(S.s, body, {}, [&] { S.enqueue_picard_pre(diva, none); });
       auto ks = capture_into(S.s, body, pre, [&] { S.enqueue_outer_halo64(); });
       capture_into(S.s, body, ks, [&] { S.enqueue_picard_post(diva, outer); });
+      S.w->graph_kernels_it[diva] = count_kernel_nodes(body);
       cudaGraphExec_t exec;
       UFE_CUDA(cudaGraphInstantiate(&exec, g, 0));
       cudaGraphDestroy(g);
@@ -1593,8 +1611,11 @@ void picard_launch(ufe_ctx *ctx, const ufe_solver_params &p, bool diva) {
       *key = k;
     }
     UFE_CUDA(cudaGraphLaunch(*gx, S.s));
+    w->last_kernels_pro = w->graph_kernels_pro[diva];
+    w->last_kernels_it = w->graph_kernels_it[diva];
   } else {
     run_picard_host(S, diva);
+    w->last_kernels_pro = w->last_kernels_it = -1;
   }
   cudaEventRecord(ctx->ev1, S.s);
   UFE_CUDA(cudaMemcpyAsync(w->ps_host, w->ps, sizeof(PicardScalars), cudaMemcpyDeviceToHost, S.s));
@@ -1621,6 +1642,7 @@ int32_t picard_collect(ufe_ctx *ctx, const ufe_solver_params &p, ufe_solve_stats
     stats->visc_it_relax_applied = ps.relax;
     stats->device_ms = ms;
     stats->n_fp64_its = ks.total_its;
+    stats->n_kernels = w->last_kernels_it >= 0 ? w->last_kernels_pro + ps.it * w->last_kernels_it : -1;
   }
   return ps.status;
 }
@@ -2226,6 +2248,55 @@ extern "C" int32_t ufe_solve_linearised(ufe_ctx *ctx, const ufe_solver_params *p
       *n_Axb_its = (p->precision == UFE_PREC_FP32_REFINE) ? w->ks_host[1].total_its + w->ks_host[0].total_its
                                                           : w->ks_host[0].it;
     return w->ks_host[0].status;
+  });
+}
+
+// Mean microseconds per iteration of the persistent Krylov kernel (FP64 solve, or FP32 inner
+// solve) on the system the last solve assembled.  The solve restarts from its usual
+// initialisation (x = 0 for the FP64 solve; the current FP64 residual for the inner solve) with
+// a zero tolerance, so the kernel runs `iterations` iterations unless the recurrence breaks down.
+extern "C" int32_t ufe_profile_krylov_persistent(ufe_ctx *ctx, int32_t precision, int32_t iterations,
+                                                 double *us_per_iteration) {
+  return guarded(ctx, [&]() -> int32_t {
+    UFE_REQUIRE(us_per_iteration && iterations >= 1, UFE_ERR_INVALID, "bad profile arguments");
+    UFE_CUDA(cudaSetDevice(ctx->device));
+    Work *w = ensure_work(ctx);
+    UFE_REQUIRE(w->nnzb > 0, UFE_ERR_INVALID, "no assembled system: run a solve first");
+    ufe_solver_params p;
+    ufe_default_params(&p);
+    p.precision = precision;
+    p.krylov_max_it = iterations;
+    p.krylov_inner_rtol = 1e-300;
+    Solver S(ctx, p);
+    const bool fp32 = precision == UFE_PREC_FP32_REFINE;
+    UFE_REQUIRE(fp32 ? S.halo_ok() : S.halo64_ok(), UFE_ERR_INVALID, "persistent Krylov kernel not in use");
+    cudaStream_t s = S.s;
+    CondArg none{0, 0};
+    if (fp32) {
+      S.enqueue_inner_init(none);
+    } else {
+      BsrMat<double, double, 1> m = S.mat64<1>();
+      k_krylov_init<BsrMat<double, double, 1>><<<krylov_grid(m, kThreads, S.grid), kThreads, 0, s>>>(
+          m, S.kv64(), w->ks, 0.0, 0.0, iterations, 1, ctx->red.partials, ctx->red.tickets, none, 0);
+      UFE_CUDA(cudaGetLastError());
+    }
+    KrylovScalars *dks = w->ks + (fp32 ? 1 : 0);
+    UFE_CUDA(cudaEventRecord(ctx->ev0, s));
+    if (fp32) {
+      k_reset_gsync<<<1, 1, 0, s>>>(w->gsync);
+      S.inner_halo();
+    } else {
+      S.enqueue_outer_halo64();
+    }
+    UFE_CUDA(cudaEventRecord(ctx->ev1, s));
+    UFE_CUDA(cudaEventSynchronize(ctx->ev1));
+    float ms = 0.f;
+    UFE_CUDA(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+    KrylovScalars out;
+    UFE_CUDA(cudaMemcpy(&out, dks, sizeof(out), cudaMemcpyDeviceToHost));
+    UFE_REQUIRE(out.it >= 1, UFE_ERR_DEVICE, "persistent Krylov kernel did not iterate");
+    *us_per_iteration = 1000.0 * ms / out.it;
+    return UFE_OK;
   });
 }
 

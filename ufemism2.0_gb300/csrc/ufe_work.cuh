@@ -138,9 +138,12 @@ struct Work {
   // persistent Krylov kernel: per-block partial sums of its three phases and its grid barrier
   double *ppart = nullptr;
   struct GridSync *gsync = nullptr;
-  // graphs
+  // graphs, and their kernel nodes: in the prologue and in one Picard iteration ([0] SSA, [1] DIVA;
+  // -1 where a Picard iteration holds a data-dependent loop)
   cudaGraphExec_t graph_ssa = nullptr, graph_diva = nullptr;
   uint64_t graph_ssa_key = 0, graph_diva_key = 0;
+  int32_t graph_kernels_pro[2] = {-1, -1}, graph_kernels_it[2] = {-1, -1};
+  int32_t last_kernels_pro = -1, last_kernels_it = -1;   // of the solve last launched
 };
 
 Work *ensure_work(ufe_ctx *ctx);

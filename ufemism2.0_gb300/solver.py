@@ -261,6 +261,12 @@ class VelocitySolver:
         self._check(self.lib.ufe_profile_krylov_kernels(self.ctx, precision, repeats, abi.as_d(us), geo))
         return us, (geo[0], geo[1])
 
+    def profile_krylov_persistent(self, precision: int, iterations: int = 200):
+        """Microseconds per iteration of the persistent Krylov kernel on the last assembled system."""
+        us = C.c_double()
+        self._check(self.lib.ufe_profile_krylov_persistent(self.ctx, precision, iterations, C.byref(us)))
+        return us.value
+
     def autotune(self, repeats: int = 20):
         """Pick the rows per warp of the Krylov kernels for this mesh (after a solve); returns
         (choice, microseconds per iteration for 1, 2, 4, 8)."""
