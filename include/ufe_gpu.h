@@ -91,8 +91,16 @@ enum ufe_bc {               /* BC_{u,v}_{west,east,south,north} (solve_linearise
 };
 enum ufe_precision {
   UFE_PREC_FP64       = 0,  /* FP64 everywhere                                              */
-  UFE_PREC_FP32_REFINE = 1  /* FP32 Krylov (matrix, vectors, preconditioner), FP64 residual
+  UFE_PREC_FP32_REFINE = 1, /* FP32 Krylov (matrix, vectors, preconditioner), FP64 residual
                                recomputation and iterative refinement to the same tolerance   */
+  UFE_PREC_FP32_PAIR  = 2   /* the Krylov solve in double-word arithmetic: every matrix entry,
+                               vector element and recurrence scalar is a pair of FP32 numbers
+                               (about 48 significant bits) computed on the FP32 pipe; the
+                               Picard loop, assembly and stopping tests stay FP64.  A system
+                               with values outside the FP32 exponent range is solved in FP64.
+                               Where the persistent Krylov kernel is not used (UFE_NO_PERSIST,
+                               UFE_NO_SELL, no room for its shared-memory patches) this mode
+                               runs as UFE_PREC_FP64                                          */
 };
 enum ufe_initial_guess {
   UFE_X0_ZERO    = 0,       /* every Krylov solve starts from x = 0, as PETSc does by default  */
@@ -174,7 +182,8 @@ typedef struct {
   int32_t n_kernels;        /* kernels the solve launched, counted from the kernel nodes of  */
                             /* its graph (-1 where loops inside a Picard iteration make the  */
                             /* count data dependent, or without graphs)                      */
-  int32_t reserved[4];
+  int32_t n_pair_its;       /* of n_Axb_its: double-word iterations (UFE_PREC_FP32_PAIR)    */
+  int32_t reserved[3];
 } ufe_solve_stats;
 
 /* ---- context ------------------------------------------------------------------------------- */
@@ -271,8 +280,9 @@ int32_t ufe_solve_diva_resident(ufe_ctx *ctx, const ufe_solver_params *p, int32_
 int32_t ufe_velocity_download(ufe_ctx *ctx, double *u_b, double *v_b);
 
 /* Mean microseconds per iteration of the persistent Krylov kernel (the whole solve in one launch
- * with shared-memory patches: the FP64 solve, or the FP32 inner solve) on the system the last solve
- * on ctx assembled, running `iterations` iterations.  Measurement only. */
+ * with shared-memory patches: the FP64 solve, the double-word solve with its conversions in and
+ * out, or the FP32 inner solve) on the system the last solve on ctx assembled, running
+ * `iterations` iterations.  Measurement only. */
 int32_t ufe_profile_krylov_persistent(ufe_ctx *ctx, int32_t precision, int32_t iterations, double *us_per_iteration);
 
 /* ---- thermodynamics: implicit column temperature solve ---------------------------------------- */

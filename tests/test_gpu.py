@@ -137,7 +137,7 @@ def test_assembly_bc_variants_bitexact(pkg, oracle_mod, dome, gpu_golden_ops):
     assert np.array_equal(Ag.val, Ao.val) and np.array_equal(bg, bo)
 
 
-@pytest.mark.parametrize("precision,tol", [(0, 1e-9), (1, 1e-6)])
+@pytest.mark.parametrize("precision,tol", [(0, 1e-9), (1, 1e-6), (2, 1e-8)])
 def test_linearised_solve_matches_direct(pkg, oracle_mod, dome, gpu_golden_ops, precision, tol):
     import scipy.sparse.linalg as spla
     mesh = dome[0]
@@ -223,6 +223,34 @@ def test_mixed_precision_matches_fp64(pkg, dome, gpu_golden_ops):
     n32 = gpu_golden_ops.solve_SSA(ice, b, p32)
     assert n32[2]["status"] == 0 and n32[2]["n_refinements"] >= 1
     assert rel_l2(np.r_[b["u_b"], b["v_b"]], np.r_[a["u_b"], a["v_b"]]) < 1e-6
+
+
+@pytest.mark.parametrize("diva", [False, True])
+def test_pair_precision_matches_fp64(pkg, diva):
+    """UFE_PREC_FP32_PAIR (double-word Krylov on the FP32 pipe) against the FP64 path: the same
+    Picard history within one iteration, the velocities within the Krylov tolerance, and every
+    Krylov iteration done by the double-word kernel."""
+    mesh, ice, params = pkg.geometry.small_channel(sliding="Schoof2005")
+    p64 = pkg.abi.default_params(**{f: getattr(params, f) for f, _ in params._fields_ if f != "reserved"})
+    p64.stress_balance_PETSc_rtol = 1e-10
+    p64.stress_balance_PETSc_abstol = 0.0
+    pp = pkg.abi.default_params(**{f: getattr(p64, f) for f, _ in p64._fields_ if f != "reserved"})
+    pp.precision = pkg.abi.PREC_FP32_PAIR
+    with pkg.VelocitySolver(mesh) as s:
+        s.ice_upload(ice)
+        a = s.solve_resident(p64, diva=diva, cold_start=True)
+        ua = np.r_[s.velocity_download()]
+        b = s.solve_resident(pp, diva=diva, cold_start=True)
+        ub = np.r_[s.velocity_download()]
+        c = s.solve_resident(pp, diva=diva, cold_start=True)
+        uc = np.r_[s.velocity_download()]
+    assert a["status"] == b["status"] == 0
+    assert abs(a["n_visc_its"] - b["n_visc_its"]) <= 1
+    assert b["n_pair_its"] == b["n_Axb_its"] > 0 and b["n_fp64_its"] == 0
+    assert a["n_pair_its"] == 0 and a["n_fp64_its"] == a["n_Axb_its"]
+    assert abs(a["n_Axb_its"] - b["n_Axb_its"]) <= 0.05 * a["n_Axb_its"]
+    assert rel_l2(ub, ua) < 1e-7, rel_l2(ub, ua)
+    assert np.array_equal(ub, uc)          # deterministic
 
 
 # ---- failure behaviour ---------------------------------------------------------------------------

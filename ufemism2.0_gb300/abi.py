@@ -31,7 +31,7 @@ OP = {name: i for i, name in enumerate(OPERATORS)}
 
 SLIDING = {"no_sliding": 0, "Weertman": 1, "Coulomb": 2, "Budd": 3, "Tsai2015": 4, "Schoof2005": 5}
 BC = {"infinite": 0, "zero": 1}
-PREC_FP64, PREC_FP32_REFINE = 0, 1
+PREC_FP64, PREC_FP32_REFINE, PREC_FP32_PAIR = 0, 1, 2
 X0_ZERO, X0_CURRENT = 0, 1
 
 dptr = C.POINTER(C.c_double)
@@ -81,7 +81,7 @@ class SolveStats(C.Structure):
     _fields_ = [("n_visc_its", C.c_int32), ("n_Axb_its", C.c_int32), ("n_refinements", C.c_int32),
                 ("status", C.c_int32), ("L2_uv", C.c_double), ("visc_it_relax_applied", C.c_double),
                 ("device_ms", C.c_double), ("n_fp64_its", C.c_int32), ("n_kernels", C.c_int32),
-                ("reserved", C.c_int32 * 4)]
+                ("n_pair_its", C.c_int32), ("reserved", C.c_int32 * 3)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}

@@ -53,7 +53,9 @@ struct KrylovScalars {
   int32_t tbreak;      // t = 0 in the last iteration: x + alpha p is the final update
   int32_t pad;         // failed inner solves of the current refinement loop
   int32_t fallback;    // the FP32 refinement loop gave up: finish in FP64
-  int32_t pad2;
+  int32_t owner;       // [2]: 1 while the double-word solve owns the current linear solve
+  int32_t pair_its;    // of total_its: double-word (UFE_PREC_FP32_PAIR) iterations
+  int32_t pad3;
 };
 
 constexpr int kHistMax = 128;   // Picard iterations recorded per solve

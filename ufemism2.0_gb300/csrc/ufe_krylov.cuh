@@ -16,11 +16,13 @@
 
 #include <type_traits>
 
+#include "ufe_dword.cuh"
 #include "ufe_work.cuh"
 
 template <class V> struct ScalarOf { using T = double; };
 template <> struct ScalarOf<float2> { using T = float; };
 template <> struct ScalarOf<double2> { using T = double; };
+template <> struct ScalarOf<dw2> { using T = dw; };
 
 // ---- vector element helpers ---------------------------------------------------------------
 // The Krylov arithmetic uses explicit fused multiply-adds: FP64 instructions are the scarce
@@ -475,12 +477,16 @@ inline unsigned krylov_grid(const M &mat, int threads, int max_blocks) {
 constexpr int kPersistMaxBlocks = 8 * 152;
 constexpr int kPersistSlots = 3;     // partial sums per block per phase
 
-// arrival counter and generation on separate 128-byte lines: the waiters poll `gen` while the
-// arrivals update `count`
+// The barrier counts arrivals monotonically within one launch: barrier k of a launch with G
+// blocks is passed once the counter reaches k*G.  Each block's thread 0 adds its arrival with a
+// release reduction (no round trip) and polls the counter with acquire loads, so the last
+// arrival releases everyone after one L2 write and one read.  The counter must be zero when a
+// persistent kernel starts: every launch site resets it (k_reset_gsync / k_inner_init) on the
+// same stream just before.  `err` ends every later wait of the launch once one wait gave up.
 struct __align__(128) GridSync {
   unsigned int count;
   unsigned int pad0[31];
-  unsigned int gen;
+  unsigned int gen;     // unused by the barrier; kept zero
   int err;
   unsigned int pad1[30];
 };
@@ -491,31 +497,29 @@ __device__ __forceinline__ unsigned int ld_acquire_u32(const unsigned int *p) {
   return v;
 }
 
-// false (block-uniform) when the wait gave up
-__device__ __forceinline__ bool grid_barrier(GridSync *gs, unsigned int &gen) {
+__device__ __forceinline__ void red_release_add_u32(unsigned int *p, unsigned int v) {
+  asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// false (block-uniform) when the wait gave up.  `target` is thread 0's running arrival target
+// (zero at kernel start).
+__device__ __forceinline__ bool grid_barrier(GridSync *gs, unsigned int &target) {
   __shared__ int ok_s;
   __syncthreads();
   if (threadIdx.x == 0) {
     int ok = 1;
-    const unsigned int my = gen;
+    target += gridDim.x;
     __threadfence();
-    if (atomicAdd(&gs->count, 1u) == gridDim.x - 1) {
-      atomicExch(&gs->count, 0u);
-      __threadfence();
-      atomicAdd(&gs->gen, 1u);
-    } else {
-      long long spins = 0;
-      while (ld_acquire_u32(&gs->gen) == my) {
-        if (++spins > (1ll << 24) || *((volatile int *)&gs->err)) {
-          ok = 0;
-          atomicExch(&gs->err, 1);
-          break;
-        }
-        __nanosleep(32);
+    red_release_add_u32(&gs->count, 1u);
+    for (long long spins = 0; ld_acquire_u32(&gs->count) < target; ++spins) {
+      if (spins > (1ll << 24) || *((volatile int *)&gs->err)) {
+        ok = 0;
+        atomicExch(&gs->err, 1);
+        break;
       }
+      if (spins > 4096) __nanosleep(64);
     }
     __threadfence();
-    gen = my + 1;
     ok_s = ok;
   }
   __syncthreads();
@@ -576,7 +580,7 @@ __global__ void __launch_bounds__(kPersistThreads) k_bicgstab_persist(M mat, KV<
   if (!s.active) return;
   double *partP = part, *partS = part + kPersistMaxBlocks * kPersistSlots,
          *partX = part + 2 * kPersistMaxBlocks * kPersistSlots;
-  unsigned int gen = ld_acquire_u32(&gs->gen);
+  unsigned int gen = 0;   // barrier arrival target (thread 0)
   const int lane0 = threadIdx.x % M::kLanes;
   const int64_t gstride = ((int64_t)gridDim.x * blockDim.x) / M::kLanes;
   const int64_t nrows_pad = ((mat.items + gstride - 1) / gstride) * gstride;
@@ -784,28 +788,166 @@ __device__ __forceinline__ double2 halo_row(const HaloMat<double4> &m, int i, in
   return y;
 }
 
+// Double-word form (UFE_PREC_FP32_PAIR), summed in the row's storage order with Dot2
+// accumulators: the FP64 plain form's arithmetic on the FP32 pipe.
+__device__ __forceinline__ dw2 halo_row(const HaloMat<dwblk> &m, int i, int il, const dw2 *tab) {
+  dw_acc yu, yv;
+  const int sl = i >> 5;
+  const int s0 = __ldg(m.soff + sl), w = (__ldg(m.soff + sl + 1) - s0) >> 5;
+  const int base = s0 + (i & 31);
+  int k = 0;
+  for (; k + 2 <= w; k += 2) {   // two slots' loads in flight at once (register budget of 64)
+    int c[2];
+    dwblk a[2];
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+      const int slot = base + ((k + u) << 5);
+      c[u] = __ldg(m.lcol + slot);
+      a[u] = m.sblk[slot];
+    }
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+      const float4 x = tab[c[u]].q;
+      yu.mac(a[u].hi.x, a[u].lo.x, x.x, x.z);
+      yu.mac(a[u].hi.y, a[u].lo.y, x.y, x.w);
+      yv.mac(a[u].hi.z, a[u].lo.z, x.x, x.z);
+      yv.mac(a[u].hi.w, a[u].lo.w, x.y, x.w);
+    }
+  }
+  for (; k < w; ++k) {
+    const int slot = base + (k << 5);
+    const dwblk a = m.sblk[slot];
+    const float4 x = tab[__ldg(m.lcol + slot)].q;
+    yu.mac(a.hi.x, a.lo.x, x.x, x.z);
+    yu.mac(a.hi.y, a.lo.y, x.y, x.w);
+    yv.mac(a.hi.z, a.lo.z, x.x, x.z);
+    yv.mac(a.hi.w, a.lo.w, x.y, x.w);
+  }
+  return make_dw2(yu.result(), yv.result());
+}
+
+// Per-thread dot-product accumulators of the persistent solve: FP64 for the FP64 and FP32 forms;
+// Dot2 pairs for the double-word form, summed across the block in double-word arithmetic (FP32
+// pipe) and rounded to FP64 once per block for the grid sums.
+template <class Vec>
+struct DotAcc {
+  using Part = double;
+  double v = 0.0;
+  __device__ __forceinline__ void add(Vec a, Vec b) { v += v_dot(a, b); }
+  __device__ __forceinline__ Part part() const { return v; }
+  static __device__ __forceinline__ Part zero() { return 0.0; }
+  static __device__ __forceinline__ Part warp_sum(Part x) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+    return x;
+  }
+  static __device__ __forceinline__ double finish(Part x) { return x; }
+};
+template <>
+struct DotAcc<dw2> {
+  using Part = float2;   // (hi, lo)
+  dw_acc a;
+  __device__ __forceinline__ void add(dw2 x, dw2 y) {
+    a.mac(x.q.x, x.q.z, y.q.x, y.q.z);
+    a.mac(x.q.y, x.q.w, y.q.y, y.q.w);
+  }
+  __device__ __forceinline__ Part part() const {
+    const dw t = a.result();
+    return make_float2(t.hi, t.lo);
+  }
+  static __device__ __forceinline__ Part zero() { return make_float2(0.f, 0.f); }
+  static __device__ __forceinline__ Part warp_sum(Part x) {
+    dw t(x.x, x.y);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+      t = dw_add(t, dw(__shfl_xor_sync(0xffffffffu, t.hi, o), __shfl_xor_sync(0xffffffffu, t.lo, o)));
+    return make_float2(t.hi, t.lo);
+  }
+  static __device__ __forceinline__ double finish(Part x) { return dw(x.x, x.y).to_double(); }
+};
+
+// block sum of NP accumulators (fixed tree), written by thread 0 to part[blockIdx.x * NP + k]
+template <int NP, class Acc>
+__device__ __forceinline__ void block_partials_acc(const Acc (&acc)[NP], double *part) {
+  using P = typename Acc::Part;
+  __shared__ P red[NP][32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+  for (int k = 0; k < NP; ++k) {
+    const P v = Acc::warp_sum(acc[k].part());
+    if (lane == 0) red[k][warp] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < 32) {
+#pragma unroll
+    for (int k = 0; k < NP; ++k) {
+      const P v = Acc::warp_sum(lane < nw ? red[k][lane] : Acc::zero());
+      if (lane == 0) part[(int64_t)blockIdx.x * NP + k] = Acc::finish(v);
+    }
+  }
+}
+
+// After a phase's barrier: the block loads all blocks' partials at once (one L2 round trip,
+// one value per thread; the grid holds at most kHaloMaxBlocks blocks), warp k sums value k in
+// block order, and thread 0 runs update(tot) on the block's shared scalars.  Every thread sees
+// the result after the closing barrier.
+constexpr int kHaloMaxBlocks = kPersistThreads / kPersistSlots;
+template <int NP, class F>
+__device__ __forceinline__ void phase_update(const double *part, F &&update) {
+  __shared__ double sp[kPersistThreads];
+  __shared__ double tot[kPersistSlots];
+  const int n = (int)gridDim.x * NP;
+  if ((int)threadIdx.x < n) sp[threadIdx.x] = __ldcg(part + threadIdx.x);
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (warp < NP) {
+    double v = 0.0;
+    for (int b = lane; b < (int)gridDim.x; b += 32) v += sp[b * NP + warp];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (lane == 0) tot[warp] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) update(tot);
+  __syncthreads();
+}
+
+// The whole BiCGStab solve in one launch (one 1024-thread block per SM): each block owns the
+// contiguous rows [blockIdx.x * rpb, ...) and stages its patch (own rows, then halo rows) in
+// shared memory for the two SpMVs.  The scalar recurrence (divisions, square root, stopping
+// tests) runs once per block, in thread 0, on the block's shared copy of the scalars; the other
+// threads read the coefficients of the next phase from shared memory, already in the solve's
+// arithmetic (FP64, FP32 or double-word).
 template <class Vec, class Blk>
 __global__ void __launch_bounds__(kPersistThreads) k_bicgstab_halo(HaloMat<Blk> m, KV<Vec> v, KrylovScalars *ks,
                                                                    double *part, GridSync *gs) {
   using R = typename ScalarOf<Vec>::T;
   extern __shared__ __align__(16) unsigned char tab_raw[];
   Vec *tab = reinterpret_cast<Vec *>(tab_raw);
-  KrylovScalars s = *ks;
+  __shared__ KrylovScalars s;
+  __shared__ __align__(16) unsigned char rs_raw[2 * sizeof(R)];
+  R *rs = reinterpret_cast<R *>(rs_raw);
+  if (threadIdx.x == 0) {
+    s = *ks;
+    rs[0] = (R)s.beta;
+    rs[1] = (R)(s.beta * s.omegaold);
+  }
+  __syncthreads();
   if (!s.active) return;
   double *partP = part, *partS = part + kPersistMaxBlocks * kPersistSlots,
          *partX = part + 2 * kPersistMaxBlocks * kPersistSlots;
-  unsigned int gen = ld_acquire_u32(&gs->gen);
+  unsigned int gen = 0;   // barrier arrival target (thread 0)
   const int r0 = blockIdx.x * m.rpb;
   const int r1 = min(m.items, r0 + m.rpb);
   const int own = max(r1 - r0, 0);
   const int h0 = __ldg(m.halo_off + blockIdx.x);
   const int nloc = own + (__ldg(m.halo_off + blockIdx.x + 1) - h0);
   bool ok = true;
-  while (s.active) {
+  for (;;) {
     const int cur = s.it & 1, nxt = cur ^ 1;
     // -- p <- r - beta omega v + beta p (staged);  v <- D^-1 A p;  (v, r^)
     {
-      const R beta = (R)s.beta, bw = (R)(s.beta * s.omegaold);
+      const R beta = rs[0], bw = rs[1];
       const Vec *__restrict__ Po = v.P[cur];
       const Vec *__restrict__ Vo = v.V[cur];
       for (int e = threadIdx.x; e < nloc; e += blockDim.x) {
@@ -815,28 +957,30 @@ __global__ void __launch_bounds__(kPersistThreads) k_bicgstab_halo(HaloMat<Blk> 
         if (e < own) v.P[nxt][g] = pn;
       }
       __syncthreads();
-      double acc[1] = {0.0};
+      DotAcc<Vec> acc[1];
       for (int il = threadIdx.x; il < own; il += blockDim.x) {
         const int i = r0 + il;
         const Vec vn = v_mul(v.dinv[i], halo_row(m, i, il, tab));
         v.V[nxt][i] = vn;
-        acc[0] += v_dot(vn, v.RP[i]);
+        acc[0].add(vn, v.RP[i]);
       }
-      block_partials<1>(acc, partP);
+      block_partials_acc<1>(acc, partP);
       if (!(ok = grid_barrier(gs, gen))) break;
-      double tot[1];
-      all_partials<1>(partP, tot);
-      const double d1 = tot[0];
-      if (d1 == 0.0 || isnan(d1)) {
-        s.status = isnan(d1) ? UFE_ERR_NAN : UFE_ERR_DIVERGED;
-        s.active = 0;
-        break;
-      }
-      s.alpha = s.rho / d1;
+      phase_update<1>(partP, [&](const double *tot) {
+        const double d1 = tot[0];
+        if (d1 == 0.0 || isnan(d1)) {
+          s.status = isnan(d1) ? UFE_ERR_NAN : UFE_ERR_DIVERGED;
+          s.active = 0;
+        } else {
+          s.alpha = s.rho / d1;
+          rs[0] = (R)s.alpha;
+        }
+      });
+      if (!s.active) break;
     }
     // -- s <- r - alpha v (staged);  t <- D^-1 A s;  (s,t), (t,t), (s,s)
     {
-      const R alpha = (R)s.alpha;
+      const R alpha = rs[0];
       const Vec *__restrict__ Vn = v.V[nxt];
       for (int e = threadIdx.x; e < nloc; e += blockDim.x) {
         const int g = e < own ? r0 + e : __ldg(m.halo_idx + h0 + e - own);
@@ -845,69 +989,79 @@ __global__ void __launch_bounds__(kPersistThreads) k_bicgstab_halo(HaloMat<Blk> 
         if (e < own) v.S[g] = sv;
       }
       __syncthreads();
-      double acc[3] = {0.0, 0.0, 0.0};
+      DotAcc<Vec> acc[3];
       for (int il = threadIdx.x; il < own; il += blockDim.x) {
         const int i = r0 + il;
         const Vec si = tab[il];
         const Vec ti = v_mul(v.dinv[i], halo_row(m, i, il, tab));
         v.T[i] = ti;
-        acc[0] += v_dot(si, ti);
-        acc[1] += v_dot(ti, ti);
-        acc[2] += v_dot(si, si);
+        acc[0].add(si, ti);
+        acc[1].add(ti, ti);
+        acc[2].add(si, si);
       }
-      block_partials<3>(acc, partS);
+      block_partials_acc<3>(acc, partS);
       if (!(ok = grid_barrier(gs, gen))) break;
-      double tot[3];
-      all_partials<3>(partS, tot);
-      if (tot[1] == 0.0) {
-        if (tot[2] != 0.0) { s.status = UFE_ERR_DIVERGED; s.active = 0; break; }
-        s.omega = 0.0;
-        s.tbreak = 1;
-      } else if (isnan(tot[1])) {
-        s.status = UFE_ERR_NAN;
-        s.active = 0;
-        break;
-      } else {
-        s.omega = tot[0] / tot[1];
-      }
+      phase_update<3>(partS, [&](const double *tot) {
+        if (tot[1] == 0.0) {
+          if (tot[2] != 0.0) {
+            s.status = UFE_ERR_DIVERGED;
+            s.active = 0;
+          } else {
+            s.omega = 0.0;
+            s.tbreak = 1;
+          }
+        } else if (isnan(tot[1])) {
+          s.status = UFE_ERR_NAN;
+          s.active = 0;
+        } else {
+          s.omega = tot[0] / tot[1];
+        }
+        rs[1] = (R)s.omega;
+      });
+      if (!s.active) break;
     }
     // -- x <- x + alpha p + omega s;  r <- s - omega t;  (r, r^), (r, r)
     {
-      const R alpha = (R)s.alpha, omega = (R)s.omega;
-      double acc[2] = {0.0, 0.0};
+      const R alpha = rs[0], omega = rs[1];
+      DotAcc<Vec> acc[2];
       for (int il = threadIdx.x; il < own; il += blockDim.x) {
         const int i = r0 + il;
         const Vec pi = v.P[nxt][i], si = v.S[i], ti = v.T[i];
         v.X[i] = v_xupd(v.X[i], alpha, pi, omega, si);
         const Vec ri = v_sub_scaled(si, omega, ti);
         v.R[i] = ri;
-        acc[0] += v_dot(ri, v.RP[i]);
-        acc[1] += v_dot(ri, ri);
+        acc[0].add(ri, v.RP[i]);
+        acc[1].add(ri, ri);
       }
-      block_partials<2>(acc, partX);
+      block_partials_acc<2>(acc, partX);
       if (!(ok = grid_barrier(gs, gen))) break;
-      double tot[2];
-      all_partials<2>(partX, tot);
-      s.it += 1;
-      s.total_its += 1;
-      const double dp = sqrt(tot[1]);
-      s.dp = dp;
-      const double rho_new = tot[0];
-      s.rhoold = s.rho;
-      s.omegaold = s.omega;
-      s.rho = rho_new;
-      if (s.tbreak) { s.active = 0; s.status = UFE_OK; s.dp = 0.0; }
-      else if (isnan(dp)) { s.status = UFE_ERR_NAN; s.active = 0; }
-      else if (dp <= s.ttol) { s.active = 0; }
-      else if (dp >= 1e4 * s.rnorm0) { s.status = UFE_ERR_DIVERGED; s.active = 0; }
-      else if (s.it >= s.max_it) { s.status = UFE_WARN_KRYLOV_MAXIT; s.active = 0; }
-      else if (rho_new == 0.0) { s.status = UFE_ERR_DIVERGED; s.active = 0; }
-      else s.beta = (s.rho / s.rhoold) * (s.alpha / s.omegaold);
+      phase_update<2>(partX, [&](const double *tot) {
+        s.it += 1;
+        s.total_its += 1;
+        const double dp = sqrt(tot[1]);
+        s.dp = dp;
+        const double rho_new = tot[0];
+        s.rhoold = s.rho;
+        s.omegaold = s.omega;
+        s.rho = rho_new;
+        if (s.tbreak) { s.active = 0; s.status = UFE_OK; s.dp = 0.0; }
+        else if (isnan(dp)) { s.status = UFE_ERR_NAN; s.active = 0; }
+        else if (dp <= s.ttol) { s.active = 0; }
+        else if (dp >= 1e4 * s.rnorm0) { s.status = UFE_ERR_DIVERGED; s.active = 0; }
+        else if (s.it >= s.max_it) { s.status = UFE_WARN_KRYLOV_MAXIT; s.active = 0; }
+        else if (rho_new == 0.0) { s.status = UFE_ERR_DIVERGED; s.active = 0; }
+        else s.beta = (s.rho / s.rhoold) * (s.alpha / s.omegaold);
+        rs[0] = (R)s.beta;
+        rs[1] = (R)(s.beta * s.omegaold);
+      });
+      if (!s.active) break;
     }
   }
-  if (!ok) {
-    s.status = UFE_ERR_DEVICE;
-    s.active = 0;
+  if (threadIdx.x == 0) {
+    if (!ok) {
+      s.status = UFE_ERR_DEVICE;
+      s.active = 0;
+    }
+    if (blockIdx.x == 0) *ks = s;
   }
-  if (blockIdx.x == 0 && threadIdx.x == 0) *ks = s;
 }

@@ -811,13 +811,76 @@ static void check_operators(ufe_ctx *ctx) {
 }
 
 // The sliced-ELL layout of the stiffness pattern (the 2nd-order b_b operators' pattern).
+// Entries a double-word copy cannot carry: beyond the FP32 range, not finite, or so small
+// (below 1e-30) that the low word would leave the normal FP32 range.
+__device__ __forceinline__ bool pair_unsafe(double a, bool tiny_matters) {
+  const double m = fabs(a);
+  return !(m <= 1e36) || (tiny_matters && m != 0.0 && m < 1e-30);
+}
+
 __global__ void k_sell_fill(int64_t nnzb, const int32_t *__restrict__ map, const double4 *__restrict__ blk,
-                            const float4 *__restrict__ blk32, double4 *__restrict__ sblk, float4 *__restrict__ sblk32) {
+                            const float4 *__restrict__ blk32, double4 *__restrict__ sblk, float4 *__restrict__ sblk32,
+                            dwblk *__restrict__ sblkp, int *pair_bad) {
   const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= nnzb) return;
   const int32_t slot = map[k];
-  sblk[slot] = blk[k];
+  const double4 b = blk[k];
+  sblk[slot] = b;
   sblk32[slot] = blk32[k];
+  if (sblkp) {
+    sblkp[slot] = to_dwblk(b);
+    if (pair_unsafe(b.x, true) || pair_unsafe(b.y, true) || pair_unsafe(b.z, true) || pair_unsafe(b.w, true))
+      atomicOr(pair_bad, 1);
+  }
+}
+
+// UFE_PREC_FP32_PAIR, around the persistent double-word BiCGStab:
+//   k_pair_enter  the FP64 start k_krylov_init left (x, r, r^, D^-1; p = v = 0) in double-word form
+//   k_pair_decide the double-word solve takes the linear solve ([0] -> [2], [0] inactive) unless a
+//                 matrix or vector value is outside what a pair of FP32 numbers carries; then the
+//                 FP64 solve keeps it
+//   k_pair_exit   x back to FP64, the scalars back to [0] (iterations counted in pair_its)
+__global__ void k_pair_enter(int n, const double2 *__restrict__ X, const double2 *__restrict__ R,
+                             const double2 *__restrict__ RP, const double2 *__restrict__ dinv, dw2 *pX, dw2 *pR,
+                             dw2 *pRP, dw2 *pdinv, dw2 *pP0, dw2 *pV0, const KrylovScalars *ks, int *pair_bad) {
+  if (!ks->active) return;
+  bool bad = false;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const double2 x = X[i], r = R[i], rp = RP[i], d = dinv[i];
+    bad |= pair_unsafe(x.x, false) || pair_unsafe(x.y, false) || pair_unsafe(r.x, false) ||
+           pair_unsafe(r.y, false) || pair_unsafe(d.x, false) || pair_unsafe(d.y, false);
+    pX[i] = to_dw2(x);
+    pR[i] = to_dw2(r);
+    pRP[i] = to_dw2(rp);
+    pdinv[i] = to_dw2(d);
+    pP0[i] = dw2{make_float4(0.f, 0.f, 0.f, 0.f)};
+    pV0[i] = dw2{make_float4(0.f, 0.f, 0.f, 0.f)};
+  }
+  if (bad) atomicOr(pair_bad, 1);
+}
+
+__global__ void k_pair_decide(KrylovScalars *ks, int *pair_bad) {
+  KrylovScalars s = ks[0];
+  if (*pair_bad == 0 && s.active) {
+    s.owner = 1;
+    ks[0].active = 0;
+  } else {
+    s.owner = 0;
+    s.active = 0;
+  }
+  ks[2] = s;
+  *pair_bad = 0;
+}
+
+__global__ void k_pair_exit(int n, const dw2 *__restrict__ pX, double2 *X, KrylovScalars *ks) {
+  if (!ks[2].owner) return;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) X[i] = to_double2(pX[i]);
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    KrylovScalars s = ks[2];
+    s.pair_its = ks[0].pair_its + s.it;
+    s.owner = 0;
+    ks[0] = s;
+  }
 }
 
 void build_sell(ufe_ctx *ctx, Work *w) {
@@ -864,7 +927,7 @@ void build_sell(ufe_ctx *ctx, Work *w) {
   int dev = 0, sms = 0;
   UFE_CUDA(cudaGetDevice(&dev));
   UFE_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-  const int32_t G = std::max(1, std::min<int32_t>(sms, nsl));
+  const int32_t G = std::max(1, std::min<int32_t>(std::min<int32_t>(sms, nsl), kHaloMaxBlocks));
   const int32_t rpb = ((n + G - 1) / G + 31) / 32 * 32;
   std::vector<int32_t> hoff(G + 1, 0), hidx, lcol(nslots, 0);
   int32_t maxlocal = 0;
@@ -958,17 +1021,17 @@ Work *ensure_work(ufe_ctx *ctx) {
   w->dNx_b_in = alloc_n<double>(nTri);
   w->dNy_b_in = alloc_n<double>(nTri);
   w->beta_b_in = alloc_n<double>(nTri);
-  w->ks = alloc_n<KrylovScalars>(2);   // [0] outer/FP64, [1] FP32 inner
+  w->ks = alloc_n<KrylovScalars>(3);   // [0] outer/FP64, [1] FP32 inner, [2] double-word solve
   w->ps = alloc_n<PicardScalars>(1);
   w->err = alloc_n<int>(1);
-  UFE_CUDA(cudaMallocHost(&w->ks_host, sizeof(KrylovScalars) * 2));
+  UFE_CUDA(cudaMallocHost(&w->ks_host, sizeof(KrylovScalars) * 3));
   UFE_CUDA(cudaMallocHost(&w->ps_host, sizeof(PicardScalars)));
   cudaStream_t s = ctx->stream;
   UFE_CUDA(cudaMemsetAsync(w->uv, 0, sizeof(double2) * nTri, s));
   UFE_CUDA(cudaMemsetAsync(w->uv_base, 0, sizeof(double2) * nTri, s));
   UFE_CUDA(cudaMemsetAsync(w->tau_b, 0, sizeof(double2) * nTri, s));
   UFE_CUDA(cudaMemsetAsync(w->eta_3D_b, 0, sizeof(double) * (size_t)nTri * nz, s));
-  UFE_CUDA(cudaMemsetAsync(w->ks, 0, sizeof(KrylovScalars) * 2, s));
+  UFE_CUDA(cudaMemsetAsync(w->ks, 0, sizeof(KrylovScalars) * 3, s));
   UFE_CUDA(cudaMemsetAsync(w->err, 0, sizeof(int), s));
   UFE_CUDA(cudaStreamSynchronize(s));
   return w;
@@ -989,7 +1052,8 @@ void free_work(ufe_ctx *ctx) {
                   w->alpha_sq, w->effp, w->tys, w->mask_gr, w->N_a, w->beta_a, w->beta_eff_a, w->F2a1,
                   w->eta_3D_a, w->F1_3D_a, w->N_b_in, w->dNx_b_in, w->dNy_b_in, w->beta_b_in, w->ks,
                   w->ps, w->err, w->ppart, w->gsync, w->sell_off, w->sell_col, w->sell_map, w->sell_blk,
-                  w->sell_blk32, w->halo_off, w->halo_idx, w->halo_lcol};
+                  w->sell_blk32, w->halo_off, w->halo_idx, w->halo_lcol, w->pX, w->pR, w->pRP, w->pS, w->pT,
+                  w->pdinv, w->pP[0], w->pP[1], w->pV[0], w->pV[1], w->sell_blkp, w->pair_bad};
   for (void *p : ptrs) dev_free(p);
   if (w->ks_host) cudaFreeHost(w->ks_host);
   if (w->ps_host) cudaFreeHost(w->ps_host);
@@ -1068,6 +1132,7 @@ struct Solver {
     ab = OpRow{mab.ptr, mab.ind, mab.val, ctx->ops[UFE_OP_DDX_A_B].val, ctx->ops[UFE_OP_DDY_A_B].val};
     const DevCSR &mba = ctx->ops[UFE_OP_MAP_B_A];
     ba = OpRow{mba.ptr, mba.ind, mba.val, ctx->ops[UFE_OP_DDX_B_A].val, ctx->ops[UFE_OP_DDY_B_A].val};
+    if (pair_ok()) ensure_pair();
   }
 
   int eblocks(int64_t n) const { return pick_blocks(n, kThreads, grid); }
@@ -1113,8 +1178,9 @@ struct Solver {
     else k_assemble<kFromDIVA><<<g, kThreads, 0, s>>>(a, q, c);
     UFE_CUDA(cudaGetLastError());
     if (use_sell()) {
-      k_sell_fill<<<(unsigned)((w->nnzb + 255) / 256), 256, 0, s>>>(w->nnzb, w->sell_map, w->blk, w->blk32,
-                                                                      w->sell_blk, w->sell_blk32);
+      k_sell_fill<<<(unsigned)((w->nnzb + 255) / 256), 256, 0, s>>>(
+          w->nnzb, w->sell_map, w->blk, w->blk32, w->sell_blk, w->sell_blk32, pair_ok() ? w->sell_blkp : nullptr,
+          w->pair_bad);
       UFE_CUDA(cudaGetLastError());
     }
   }
@@ -1259,6 +1325,66 @@ struct Solver {
     cfg.attrs = at;
     cfg.numAttrs = 1;
     UFE_CUDA(cudaLaunchKernelEx(&cfg, k_bicgstab_halo<double2, double4>, m, kv64(), w->ks, w->ppart, w->gsync));
+  }
+  // UFE_PREC_FP32_PAIR: the linear solve in double-word arithmetic, one persistent launch with the
+  // FP64 solve's shared-memory patches; the FP64 persistent solve runs after it and does the work
+  // only when the double-word solve declined (k_pair_decide)
+  bool pair_ok() const { return p.precision == UFE_PREC_FP32_PAIR && halo64_ok(); }
+  void ensure_pair() {
+    if (w->sell_blkp) return;
+    const int n = w->nTri;
+    dw2 **v[] = {&w->pX, &w->pR, &w->pRP, &w->pS, &w->pT, &w->pdinv, &w->pP[0], &w->pP[1], &w->pV[0], &w->pV[1]};
+    for (auto q : v) *q = static_cast<dw2 *>(dev_alloc(sizeof(dw2) * (size_t)(n ? n : 1)));
+    w->sell_blkp = static_cast<dwblk *>(dev_alloc(sizeof(dwblk) * (size_t)(w->nslots ? w->nslots : 1)));
+    w->pair_bad = static_cast<int *>(dev_alloc(sizeof(int)));
+    UFE_CUDA(cudaMemsetAsync(w->sell_blkp, 0, sizeof(dwblk) * (size_t)(w->nslots ? w->nslots : 1), s));
+    UFE_CUDA(cudaMemsetAsync(w->pair_bad, 0, sizeof(int), s));
+  }
+  KV<dw2> kvpair() const {
+    KV<dw2> v;
+    v.X = w->pX; v.R = w->pR; v.RP = w->pRP; v.S = w->pS; v.T = w->pT; v.B = nullptr;
+    v.dinv = w->pdinv;
+    v.P[0] = w->pP[0]; v.P[1] = w->pP[1]; v.V[0] = w->pV[0]; v.V[1] = w->pV[1];
+    return v;
+  }
+  void enqueue_outer_pair() {
+    const int g = eblocks(w->nTri);
+    k_pair_enter<<<g, kThreads, 0, s>>>(w->nTri, w->kv.X, w->kv.R, w->kv.RP, w->kv.dinv, w->pX, w->pR, w->pRP,
+                                        w->pdinv, w->pP[0], w->pV[0], w->ks, w->pair_bad);
+    k_pair_decide<<<1, 1, 0, s>>>(w->ks, w->pair_bad);
+    UFE_CUDA(cudaGetLastError());
+    const size_t smem = (size_t)w->halo_maxlocal * sizeof(dw2);
+    static size_t attr = 0;
+    if (smem > attr) {
+      UFE_CUDA(cudaFuncSetAttribute(k_bicgstab_halo<dw2, dwblk>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)smem));
+      attr = smem;
+    }
+    HaloMat<dwblk> m{w->nTri, w->halo_rpb, w->sell_off, w->halo_lcol, w->sell_blkp, nullptr, w->halo_off,
+                     w->halo_idx};
+    k_reset_gsync<<<1, 1, 0, s>>>(w->gsync);
+    UFE_CUDA(cudaGetLastError());
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    UFE_CUDA(cudaStreamIsCapturing(s, &cap));
+    if (cap != cudaStreamCaptureStatusNone) {
+      k_bicgstab_halo<dw2, dwblk><<<w->halo_G, kPersistThreads, smem, s>>>(m, kvpair(), w->ks + 2, w->ppart, w->gsync);
+      UFE_CUDA(cudaGetLastError());
+    } else {
+      cudaLaunchConfig_t cfg = {};
+      cfg.gridDim = dim3(w->halo_G);
+      cfg.blockDim = dim3(kPersistThreads);
+      cfg.dynamicSmemBytes = smem;
+      cfg.stream = s;
+      cudaLaunchAttribute at[1];
+      at[0].id = cudaLaunchAttributeCooperative;
+      at[0].val.cooperative = 1;
+      cfg.attrs = at;
+      cfg.numAttrs = 1;
+      UFE_CUDA(cudaLaunchKernelEx(&cfg, k_bicgstab_halo<dw2, dwblk>, m, kvpair(), w->ks + 2, w->ppart, w->gsync));
+    }
+    k_pair_exit<<<g, kThreads, 0, s>>>(w->nTri, w->pX, w->kv.X, w->ks);
+    UFE_CUDA(cudaGetLastError());
+    enqueue_outer_halo64();
   }
   template <int L>
   void inner_persist_l() {
@@ -1442,10 +1568,13 @@ cudaGraphExec_t build_picard_graph(Solver &S, bool diva) {
     add_while(g, sinks, h_outer, &body);
     CondArg outer{h_outer, 1};
     if (S.p.precision != UFE_PREC_FP32_REFINE && S.halo64_ok()) {
-      // FP64: the whole Krylov solve of a Picard iteration is one persistent launch
+      // FP64 or double-word: the whole Krylov solve of a Picard iteration is one persistent launch
       CondArg none{0, 0};
       auto pre = capture_into(S.s, body, {}, [&] { S.enqueue_picard_pre(diva, none); });
-      auto ks = capture_into(S.s, body, pre, [&] { S.enqueue_outer_halo64(); });
+      auto ks = capture_into(S.s, body, pre, [&] {
+        if (S.pair_ok()) S.enqueue_outer_pair();
+        else S.enqueue_outer_halo64();
+      });
       capture_into(S.s, body, ks, [&] { S.enqueue_picard_post(diva, outer); });
       S.w->graph_kernels_it[diva] = count_kernel_nodes(body);
       cudaGraphExec_t exec;
@@ -1526,7 +1655,8 @@ void run_picard_host(Solver &S, bool diva) {
         }
         S.enqueue_refine_update(none);
       } else if (S.halo64_ok()) {
-        S.enqueue_outer_halo64();
+        if (S.pair_ok()) S.enqueue_outer_pair();
+        else S.enqueue_outer_halo64();
         break;
       } else {
         for (int c = 0; c < 8; ++c) S.krylov_iter64(none);
@@ -1565,8 +1695,9 @@ void validate_params(const ufe_solver_params *p) {
   UFE_REQUIRE(p->choice_sliding_law >= 0 && p->choice_sliding_law <= UFE_SLIDING_SCHOOF2005, UFE_ERR_INVALID,
               "unknown sliding law");
   UFE_REQUIRE(p->visc_it_nit >= 0 && p->krylov_max_it >= 1, UFE_ERR_INVALID, "iteration limits out of range");
-  UFE_REQUIRE(p->precision == UFE_PREC_FP64 || p->precision == UFE_PREC_FP32_REFINE, UFE_ERR_INVALID,
-              "unknown precision mode");
+  UFE_REQUIRE(p->precision == UFE_PREC_FP64 || p->precision == UFE_PREC_FP32_REFINE ||
+                  p->precision == UFE_PREC_FP32_PAIR,
+              UFE_ERR_INVALID, "unknown precision mode");
   UFE_REQUIRE(p->krylov_initial_guess == UFE_X0_ZERO || p->krylov_initial_guess == UFE_X0_CURRENT, UFE_ERR_INVALID,
               "unknown initial guess mode");
   const int32_t bcs[8] = {p->BC_u_west, p->BC_u_east, p->BC_u_south, p->BC_u_north,
@@ -1641,7 +1772,8 @@ int32_t picard_collect(ufe_ctx *ctx, const ufe_solver_params &p, ufe_solve_stats
     stats->L2_uv = ps.L2;
     stats->visc_it_relax_applied = ps.relax;
     stats->device_ms = ms;
-    stats->n_fp64_its = ks.total_its;
+    stats->n_fp64_its = ks.total_its - ks.pair_its;
+    stats->n_pair_its = ks.pair_its;
     stats->n_kernels = w->last_kernels_it >= 0 ? w->last_kernels_pro + ps.it * w->last_kernels_it : -1;
   }
   return ps.status;
@@ -2205,7 +2337,7 @@ extern "C" int32_t ufe_solve_linearised(ufe_ctx *ctx, const ufe_solver_params *p
     upload_pair(ctx, w->uv, u_b, v_b);
     Solver S(ctx, *p);
     CondArg none{0, 0};
-    UFE_CUDA(cudaMemsetAsync(w->ks, 0, sizeof(KrylovScalars) * 2, S.s));
+    UFE_CUDA(cudaMemsetAsync(w->ks, 0, sizeof(KrylovScalars) * 3, S.s));
     S.enqueue_assemble(kFromTriangles, p->krylov_initial_guess == UFE_X0_CURRENT, none);
     for (;;) {
       if (p->precision == UFE_PREC_FP32_REFINE) {
@@ -2224,6 +2356,9 @@ extern "C" int32_t ufe_solve_linearised(ufe_ctx *ctx, const ufe_solver_params *p
           }
         }
         S.enqueue_refine_update(none);
+      } else if (S.pair_ok()) {
+        S.enqueue_outer_pair();
+        break;
       } else {
         for (int c = 0; c < 8; ++c) S.krylov_iter64(none);
         UFE_CUDA(cudaMemcpyAsync(w->ks_host, w->ks, sizeof(KrylovScalars), cudaMemcpyDeviceToHost, S.s));
@@ -2251,8 +2386,8 @@ extern "C" int32_t ufe_solve_linearised(ufe_ctx *ctx, const ufe_solver_params *p
   });
 }
 
-// Mean microseconds per iteration of the persistent Krylov kernel (FP64 solve, or FP32 inner
-// solve) on the system the last solve assembled.  The solve restarts from its usual
+// Mean microseconds per iteration of the persistent Krylov kernel (FP64 solve, double-word
+// solve, or FP32 inner solve) on the system the last solve assembled.  The solve restarts from its usual
 // initialisation (x = 0 for the FP64 solve; the current FP64 residual for the inner solve) with
 // a zero tolerance, so the kernel runs `iterations` iterations unless the recurrence breaks down.
 extern "C" int32_t ufe_profile_krylov_persistent(ufe_ctx *ctx, int32_t precision, int32_t iterations,
@@ -2269,7 +2404,9 @@ extern "C" int32_t ufe_profile_krylov_persistent(ufe_ctx *ctx, int32_t precision
     p.krylov_inner_rtol = 1e-300;
     Solver S(ctx, p);
     const bool fp32 = precision == UFE_PREC_FP32_REFINE;
-    UFE_REQUIRE(fp32 ? S.halo_ok() : S.halo64_ok(), UFE_ERR_INVALID, "persistent Krylov kernel not in use");
+    const bool pair = precision == UFE_PREC_FP32_PAIR;
+    UFE_REQUIRE(fp32 ? S.halo_ok() : pair ? S.pair_ok() : S.halo64_ok(), UFE_ERR_INVALID,
+                "persistent Krylov kernel not in use");
     cudaStream_t s = S.s;
     CondArg none{0, 0};
     if (fp32) {
@@ -2285,6 +2422,8 @@ extern "C" int32_t ufe_profile_krylov_persistent(ufe_ctx *ctx, int32_t precision
     if (fp32) {
       k_reset_gsync<<<1, 1, 0, s>>>(w->gsync);
       S.inner_halo();
+    } else if (pair) {
+      S.enqueue_outer_pair();   // conversions in and out included
     } else {
       S.enqueue_outer_halo64();
     }

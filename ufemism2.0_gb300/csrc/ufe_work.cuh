@@ -2,6 +2,7 @@
 #pragma once
 
 #include "ufe_internal.cuh"
+#include "ufe_dword.cuh"
 
 // ------------------------------------------------------------------------------------------
 // Deterministic grid reductions without waiting: each block writes its partial sums, and the
@@ -135,6 +136,12 @@ struct Work {
   int32_t *halo_off = nullptr;   // halo_G + 1
   int32_t *halo_idx = nullptr;   // halo rows of every block
   int32_t *halo_lcol = nullptr;  // nslots: local index of each slot's column
+  // double-word Krylov solve (UFE_PREC_FP32_PAIR), allocated on first use: its vectors, the
+  // sliced-ELL blocks in double-word form, and the flag of values outside the FP32 range
+  dw2 *pX = nullptr, *pR = nullptr, *pRP = nullptr, *pS = nullptr, *pT = nullptr, *pdinv = nullptr;
+  dw2 *pP[2] = {nullptr, nullptr}, *pV[2] = {nullptr, nullptr};
+  dwblk *sell_blkp = nullptr;
+  int *pair_bad = nullptr;
   // persistent Krylov kernel: per-block partial sums of its three phases and its grid barrier
   double *ppart = nullptr;
   struct GridSync *gsync = nullptr;
