@@ -329,20 +329,34 @@ def run_ours(args):
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline(pkg, mesh, ice, params, plain_runs["fp64"][0][0]["n_Axb_its"], seconds=args.cpu_seconds)
+    # the headline is the fastest measured path (zero or learned start, any Krylov precision); the
+    # rates are already the slowest rank's, so every rank picks the same path
+    cands = [(f"plain_{k}", plain_runs[k], k) for k in ("fp64", "fp32_pair", "fp32_refined")]
+    if learned:
+        cands += [(f"learned_{k}", learned_runs[k], k) for k in ("fp64", "fp32_pair", "fp32_refined")]
+    head_name, (head_sts, head_value, head_clk, head_wall), head_prec = max(cands, key=lambda c: c[1][1] or 0.0)
+    if head_name.startswith("learned"):
+        launches = kernels(head_sts, predict_kernels)
+    else:
+        launches = kernels(head_sts)
+    if learned and head_name == f"learned_{best}":
+        head_e2e = learned["e2e"]
+    else:
+        # end to end through the public C ABI with pinned host buffers: ice upload, the solve
+        # from the zero start (or the learned start), velocity download -- every step
+        solver.ice_upload(ice_h)
+        solve(prec[head_prec])
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            solver.ice_upload(ice_h)
+            solve(prec[head_prec])
+            solver.velocity_download()
+        torch.cuda.synchronize()
+        head_e2e = {"value": round(world * args.steps / slowest(time.perf_counter() - t0), 4), "unit": UNIT,
+                    "path": head_name, "h2d_bytes_per_step": int(sum(v.nbytes for v in ice_h.values())),
+                    "d2h_bytes_per_step": int(2 * 8 * mesh.nTri)}
     if rank == 0:
-        if learned:
-            head_name = f"learned_{best}"
-            head_sts, head_value, head_clk, head_wall = learned_runs[best]
-            launches = kernels(head_sts, predict_kernels)
-            head_e2e = learned["e2e"]
-            head_prec = best
-        else:
-            head_prec = max(("fp64", "fp32_pair"), key=lambda k: plain_runs[k][1])
-            head_name = f"plain_{head_prec}"
-            head_sts, head_value, head_clk, head_wall = plain_runs[head_prec]
-            launches = kernels(head_sts)
-            head_e2e = {"value": round(e2e_plain, 4), "unit": UNIT, "path": "plain_fp64",
-                        "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)}
         kname = {"fp64": "k_bicgstab_halo<double2,double4> (persistent FP64 BiCGStab)",
                  "fp32_pair": "k_bicgstab_halo<dw2,dwblk> (persistent double-word BiCGStab)"}
         rk = head_prec if head_prec in us_it and us_it.get(head_prec) else "fp64"
@@ -372,7 +386,8 @@ def run_ours(args):
                        "stiffness_blocks_2x2": int(nnzb), "l2": "flushed (256 MB write) before every solve",
                        "parallelism": f"replicas x{world}",
                        "path": head_name + (" (learned Picard start, inference inside the timed solves)"
-                                            if learned else "") + ", graph-resident solve"},
+                                            if head_name.startswith("learned") else " (zero start)")
+                               + ", graph-resident solve"},
             "speedup_vs_plain_fp64": round(head_value / value64, 3),
             "plain": plain,
             "learned_start": learned,

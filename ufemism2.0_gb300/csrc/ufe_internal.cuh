@@ -55,6 +55,9 @@ struct KrylovScalars {
   int32_t fallback;    // the FP32 refinement loop gave up: finish in FP64
   int32_t owner;       // [2]: 1 while the double-word solve owns the current linear solve
   int32_t pair_its;    // of total_its: double-word (UFE_PREC_FP32_PAIR) iterations
+  int32_t pair_rounds; // double-word solves of the current linear solve (restarts from the FP64 residual)
+  int32_t pair_stop;   // the double-word path declined or failed: finish in FP64
+  int32_t pair_rounds_total;
   int32_t pad3;
 };
 

@@ -866,23 +866,53 @@ struct DotAcc<dw2> {
   static __device__ __forceinline__ double finish(Part x) { return dw(x.x, x.y).to_double(); }
 };
 
-// block sum of NP accumulators (fixed tree), written by thread 0 to part[blockIdx.x * NP + k]
+// Scratch of the FP64 block sums (one instance per kernel that uses it).
+__device__ __forceinline__ double *fp64_reduce_scratch() {
+  __shared__ double buf[kPersistSlots * kPersistThreads];
+  return buf;
+}
+
+// block sum of NP accumulators (fixed tree), written by thread 0 to part[blockIdx.x * NP + k].
+// FP64 sums run as a shared-memory tree down to one warp: a butterfly of shuffles would issue
+// 5 FP64 adds per warp per value, and FP64 issue is scarce on GB300.  Double-word sums stay in
+// shuffles (FP32 pipe).
 template <int NP, class Acc>
 __device__ __forceinline__ void block_partials_acc(const Acc (&acc)[NP], double *part) {
   using P = typename Acc::Part;
-  __shared__ P red[NP][32];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  if constexpr (std::is_same<P, double>::value) {
+    double *t = fp64_reduce_scratch();
+    const int n = blockDim.x;   // a power of two
 #pragma unroll
-  for (int k = 0; k < NP; ++k) {
-    const P v = Acc::warp_sum(acc[k].part());
-    if (lane == 0) red[k][warp] = v;
-  }
-  __syncthreads();
-  if (threadIdx.x < 32) {
+    for (int k = 0; k < NP; ++k) t[k * n + threadIdx.x] = acc[k].part();
+    __syncthreads();
+    for (int st = n >> 1; st >= 32; st >>= 1) {
+      if ((int)threadIdx.x < st)
+#pragma unroll
+        for (int k = 0; k < NP; ++k) t[k * n + threadIdx.x] += t[k * n + threadIdx.x + st];
+      __syncthreads();
+    }
+    if (warp == 0) {
+#pragma unroll
+      for (int k = 0; k < NP; ++k) {
+        const double v = Acc::warp_sum(t[k * n + lane]);
+        if (lane == 0) part[(int64_t)blockIdx.x * NP + k] = v;
+      }
+    }
+  } else {
+    __shared__ P red[NP][32];
 #pragma unroll
     for (int k = 0; k < NP; ++k) {
-      const P v = Acc::warp_sum(lane < nw ? red[k][lane] : Acc::zero());
-      if (lane == 0) part[(int64_t)blockIdx.x * NP + k] = Acc::finish(v);
+      const P v = Acc::warp_sum(acc[k].part());
+      if (lane == 0) red[k][warp] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < 32) {
+#pragma unroll
+      for (int k = 0; k < NP; ++k) {
+        const P v = Acc::warp_sum(lane < nw ? red[k][lane] : Acc::zero());
+        if (lane == 0) part[(int64_t)blockIdx.x * NP + k] = Acc::finish(v);
+      }
     }
   }
 }
@@ -892,10 +922,14 @@ __device__ __forceinline__ void block_partials_acc(const Acc (&acc)[NP], double 
 // block order, and thread 0 runs update(tot) on the block's shared scalars.  Every thread sees
 // the result after the closing barrier.
 constexpr int kHaloMaxBlocks = kPersistThreads / kPersistSlots;
+__device__ __forceinline__ double *phase_scratch() {
+  __shared__ double buf[kPersistThreads + kPersistSlots];
+  return buf;
+}
 template <int NP, class F>
 __device__ __forceinline__ void phase_update(const double *part, F &&update) {
-  __shared__ double sp[kPersistThreads];
-  __shared__ double tot[kPersistSlots];
+  double *sp = phase_scratch();
+  double *tot = sp + kPersistThreads;
   const int n = (int)gridDim.x * NP;
   if ((int)threadIdx.x < n) sp[threadIdx.x] = __ldcg(part + threadIdx.x);
   __syncthreads();

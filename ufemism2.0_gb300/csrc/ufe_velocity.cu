@@ -460,6 +460,8 @@ __global__ void k_assemble(AssembleArgs a, PhysParams q, CondArg cond) {
     s.refinements = 0;
     s.pad = 0;
     s.fallback = 0;
+    s.pair_rounds = 0;
+    s.pair_stop = 0;
     s.active = 1;
     if (isnan(dp)) { s.status = UFE_ERR_NAN; s.active = 0; }
     else if (dp <= s.ttol) s.active = 0;
@@ -834,12 +836,17 @@ __global__ void k_sell_fill(int64_t nnzb, const int32_t *__restrict__ map, const
   }
 }
 
-// UFE_PREC_FP32_PAIR, around the persistent double-word BiCGStab:
-//   k_pair_enter  the FP64 start k_krylov_init left (x, r, r^, D^-1; p = v = 0) in double-word form
+// UFE_PREC_FP32_PAIR, around the persistent double-word BiCGStab.  One round:
+//   k_pair_enter  the FP64 start (x, r, r^, D^-1; p = v = 0) in double-word form
 //   k_pair_decide the double-word solve takes the linear solve ([0] -> [2], [0] inactive) unless a
 //                 matrix or vector value is outside what a pair of FP32 numbers carries; then the
-//                 FP64 solve keeps it
-//   k_pair_exit   x back to FP64, the scalars back to [0] (iterations counted in pair_its)
+//                 FP64 solve keeps it (pair_stop)
+//   k_pair_exit   x back to FP64, the scalars back to [0] (iterations counted in pair_its); a
+//                 failed double-word solve leaves x alone and sets pair_stop
+//   then the FP64 residual of the new x (k_krylov_init from x): converged means done; otherwise
+//   k_pair_gate starts another round from that residual (the double-word recurrence residual
+//   drifts from the true one about 2^-46 per operation), up to kPairRounds, after which the FP64
+//   solve finishes from the current x.
 __global__ void k_pair_enter(int n, const double2 *__restrict__ X, const double2 *__restrict__ R,
                              const double2 *__restrict__ RP, const double2 *__restrict__ dinv, dw2 *pX, dw2 *pR,
                              dw2 *pRP, dw2 *pdinv, dw2 *pP0, dw2 *pV0, const KrylovScalars *ks, int *pair_bad) {
@@ -859,12 +866,15 @@ __global__ void k_pair_enter(int n, const double2 *__restrict__ X, const double2
   if (bad) atomicOr(pair_bad, 1);
 }
 
+constexpr int kPairRounds = 4;
+
 __global__ void k_pair_decide(KrylovScalars *ks, int *pair_bad) {
   KrylovScalars s = ks[0];
-  if (*pair_bad == 0 && s.active) {
+  if (*pair_bad == 0 && s.active && !s.pair_stop) {
     s.owner = 1;
     ks[0].active = 0;
   } else {
+    if (s.active) ks[0].pair_stop = 1;
     s.owner = 0;
     s.active = 0;
   }
@@ -874,13 +884,24 @@ __global__ void k_pair_decide(KrylovScalars *ks, int *pair_bad) {
 
 __global__ void k_pair_exit(int n, const dw2 *__restrict__ pX, double2 *X, KrylovScalars *ks) {
   if (!ks[2].owner) return;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) X[i] = to_double2(pX[i]);
+  const bool failed = ks[2].status < 0;
+  if (!failed)
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) X[i] = to_double2(pX[i]);
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     KrylovScalars s = ks[2];
     s.pair_its = ks[0].pair_its + s.it;
+    s.pair_rounds = ks[0].pair_rounds + 1;
+    s.pair_rounds_total = ks[0].pair_rounds_total + 1;
     s.owner = 0;
+    if (failed) s.pair_stop = 1;
     ks[0] = s;
   }
+}
+
+// after the FP64 residual of a round: another round while not converged, allowed and useful
+__global__ void k_pair_gate(KrylovScalars *ks, CondArg cond) {
+  const KrylovScalars s = ks[0];
+  set_cond(cond, s.active && !s.pair_stop && s.pair_rounds < kPairRounds);
 }
 
 void build_sell(ufe_ctx *ctx, Work *w) {
@@ -1347,7 +1368,8 @@ struct Solver {
     v.P[0] = w->pP[0]; v.P[1] = w->pP[1]; v.V[0] = w->pV[0]; v.V[1] = w->pV[1];
     return v;
   }
-  void enqueue_outer_pair() {
+  // one double-word solve from the FP64 state in ks[0] (conversions in and out)
+  void pair_solve_once() {
     const int g = eblocks(w->nTri);
     k_pair_enter<<<g, kThreads, 0, s>>>(w->nTri, w->kv.X, w->kv.R, w->kv.RP, w->kv.dinv, w->pX, w->pR, w->pRP,
                                         w->pdinv, w->pP[0], w->pV[0], w->ks, w->pair_bad);
@@ -1384,6 +1406,28 @@ struct Solver {
     }
     k_pair_exit<<<g, kThreads, 0, s>>>(w->nTri, w->pX, w->kv.X, w->ks);
     UFE_CUDA(cudaGetLastError());
+  }
+  // a round: the double-word solve, the FP64 residual of its x, and the decision on another round
+  void pair_round(CondArg c) {
+    pair_solve_once();
+    BsrMat<double, double, 1> m = mat64<1>();
+    CondArg none{0, 0};
+    k_krylov_init<BsrMat<double, double, 1>><<<krylov_grid(m, kThreads, grid), kThreads, 0, s>>>(
+        m, kv64(), w->ks, p.stress_balance_PETSc_rtol, p.stress_balance_PETSc_abstol, p.krylov_max_it, 0,
+        ctx->red.partials, ctx->red.tickets, none, 0);
+    k_pair_gate<<<1, 1, 0, s>>>(w->ks, c);
+    UFE_CUDA(cudaGetLastError());
+  }
+  // the linear solve of UFE_PREC_FP32_PAIR with host-side loop control (graphs off, the
+  // linearised-solve entry point): rounds while the FP64 residual asks for them, then the FP64
+  // solve, which does the work only when the rounds ended unconverged
+  void run_pair_host() {
+    for (int r = 0; r < kPairRounds; ++r) {
+      UFE_CUDA(cudaMemcpyAsync(w->ks_host, w->ks, sizeof(KrylovScalars), cudaMemcpyDeviceToHost, s));
+      UFE_CUDA(cudaStreamSynchronize(s));
+      if (!w->ks_host[0].active || w->ks_host[0].pair_stop) break;
+      pair_round(CondArg{0, 0});
+    }
     enqueue_outer_halo64();
   }
   template <int L>
@@ -1564,19 +1608,37 @@ cudaGraphExec_t build_picard_graph(Solver &S, bool diva) {
     auto sinks = capture_into(S.s, g, {}, [&] { S.enqueue_prologue(diva); });
     S.w->graph_kernels_pro[diva] = count_kernel_nodes(g);
     S.w->graph_kernels_it[diva] = -1;
+    S.w->graph_kernels_round[diva] = -1;
     cudaGraph_t body;
     add_while(g, sinks, h_outer, &body);
     CondArg outer{h_outer, 1};
+    if (S.pair_ok()) {
+      // double-word: while(rounds){ persistent double-word solve, FP64 residual, gate }, then the
+      // persistent FP64 solve (idle unless the rounds ended unconverged)
+      cudaGraphConditionalHandle h_pair;
+      UFE_CUDA(cudaGraphConditionalHandleCreate(&h_pair, body, 0, 0));
+      CondArg pc{h_pair, 1};
+      auto pre = capture_into(S.s, body, {}, [&] { S.enqueue_picard_pre(diva, pc); });
+      cudaGraph_t rbody;
+      cudaGraphNode_t wr = add_while(body, pre, h_pair, &rbody);
+      capture_into(S.s, rbody, {}, [&] { S.pair_round(pc); });
+      auto fb = capture_into(S.s, body, {wr}, [&] { S.enqueue_outer_halo64(); });
+      capture_into(S.s, body, fb, [&] { S.enqueue_picard_post(diva, outer); });
+      S.w->graph_kernels_it[diva] = count_kernel_nodes(body);
+      S.w->graph_kernels_round[diva] = count_kernel_nodes(rbody);
+      cudaGraphExec_t exec;
+      UFE_CUDA(cudaGraphInstantiate(&exec, g, 0));
+      cudaGraphDestroy(g);
+      return exec;
+    }
     if (S.p.precision != UFE_PREC_FP32_REFINE && S.halo64_ok()) {
-      // FP64 or double-word: the whole Krylov solve of a Picard iteration is one persistent launch
+      // FP64: the whole Krylov solve of a Picard iteration is one persistent launch
       CondArg none{0, 0};
       auto pre = capture_into(S.s, body, {}, [&] { S.enqueue_picard_pre(diva, none); });
-      auto ks = capture_into(S.s, body, pre, [&] {
-        if (S.pair_ok()) S.enqueue_outer_pair();
-        else S.enqueue_outer_halo64();
-      });
+      auto ks = capture_into(S.s, body, pre, [&] { S.enqueue_outer_halo64(); });
       capture_into(S.s, body, ks, [&] { S.enqueue_picard_post(diva, outer); });
       S.w->graph_kernels_it[diva] = count_kernel_nodes(body);
+      S.w->graph_kernels_round[diva] = 0;
       cudaGraphExec_t exec;
       UFE_CUDA(cudaGraphInstantiate(&exec, g, 0));
       cudaGraphDestroy(g);
@@ -1655,7 +1717,7 @@ void run_picard_host(Solver &S, bool diva) {
         }
         S.enqueue_refine_update(none);
       } else if (S.halo64_ok()) {
-        if (S.pair_ok()) S.enqueue_outer_pair();
+        if (S.pair_ok()) S.run_pair_host();
         else S.enqueue_outer_halo64();
         break;
       } else {
@@ -1744,9 +1806,10 @@ void picard_launch(ufe_ctx *ctx, const ufe_solver_params &p, bool diva) {
     UFE_CUDA(cudaGraphLaunch(*gx, S.s));
     w->last_kernels_pro = w->graph_kernels_pro[diva];
     w->last_kernels_it = w->graph_kernels_it[diva];
+    w->last_kernels_round = w->graph_kernels_round[diva];
   } else {
     run_picard_host(S, diva);
-    w->last_kernels_pro = w->last_kernels_it = -1;
+    w->last_kernels_pro = w->last_kernels_it = w->last_kernels_round = -1;
   }
   cudaEventRecord(ctx->ev1, S.s);
   UFE_CUDA(cudaMemcpyAsync(w->ps_host, w->ps, sizeof(PicardScalars), cudaMemcpyDeviceToHost, S.s));
@@ -1774,7 +1837,9 @@ int32_t picard_collect(ufe_ctx *ctx, const ufe_solver_params &p, ufe_solve_stats
     stats->device_ms = ms;
     stats->n_fp64_its = ks.total_its - ks.pair_its;
     stats->n_pair_its = ks.pair_its;
-    stats->n_kernels = w->last_kernels_it >= 0 ? w->last_kernels_pro + ps.it * w->last_kernels_it : -1;
+    stats->n_kernels = (w->last_kernels_it >= 0 && w->last_kernels_round >= 0)
+                           ? w->last_kernels_pro + ps.it * w->last_kernels_it + ks.pair_rounds_total * w->last_kernels_round
+                           : -1;
   }
   return ps.status;
 }
@@ -2357,7 +2422,7 @@ extern "C" int32_t ufe_solve_linearised(ufe_ctx *ctx, const ufe_solver_params *p
         }
         S.enqueue_refine_update(none);
       } else if (S.pair_ok()) {
-        S.enqueue_outer_pair();
+        S.run_pair_host();
         break;
       } else {
         for (int c = 0; c < 8; ++c) S.krylov_iter64(none);
@@ -2381,7 +2446,7 @@ extern "C" int32_t ufe_solve_linearised(ufe_ctx *ctx, const ufe_solver_params *p
     download_pair(ctx, w->kv.X, u_b, v_b);
     if (n_Axb_its)
       *n_Axb_its = (p->precision == UFE_PREC_FP32_REFINE) ? w->ks_host[1].total_its + w->ks_host[0].total_its
-                                                          : w->ks_host[0].it;
+                                                          : w->ks_host[0].total_its;
     return w->ks_host[0].status;
   });
 }
@@ -2423,7 +2488,7 @@ extern "C" int32_t ufe_profile_krylov_persistent(ufe_ctx *ctx, int32_t precision
       k_reset_gsync<<<1, 1, 0, s>>>(w->gsync);
       S.inner_halo();
     } else if (pair) {
-      S.enqueue_outer_pair();   // conversions in and out included
+      S.pair_solve_once();   // conversions in and out included
     } else {
       S.enqueue_outer_halo64();
     }

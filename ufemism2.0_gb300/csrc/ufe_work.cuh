@@ -149,8 +149,9 @@ struct Work {
   // -1 where a Picard iteration holds a data-dependent loop)
   cudaGraphExec_t graph_ssa = nullptr, graph_diva = nullptr;
   uint64_t graph_ssa_key = 0, graph_diva_key = 0;
-  int32_t graph_kernels_pro[2] = {-1, -1}, graph_kernels_it[2] = {-1, -1};
-  int32_t last_kernels_pro = -1, last_kernels_it = -1;   // of the solve last launched
+  // and in one double-word round (UFE_PREC_FP32_PAIR; 0 for the other persistent path)
+  int32_t graph_kernels_pro[2] = {-1, -1}, graph_kernels_it[2] = {-1, -1}, graph_kernels_round[2] = {-1, -1};
+  int32_t last_kernels_pro = -1, last_kernels_it = -1, last_kernels_round = -1;   // of the solve last launched
 };
 
 Work *ensure_work(ufe_ctx *ctx);
