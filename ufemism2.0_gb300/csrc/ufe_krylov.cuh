@@ -475,7 +475,7 @@ inline unsigned krylov_grid(const M &mat, int threads, int max_blocks) {
 // take identical decisions without another round trip.  The barrier's spin is bounded: a block
 // that waits too long records the failure and every block leaves the loop.
 constexpr int kPersistMaxBlocks = 8 * 152;
-constexpr int kPersistSlots = 3;     // partial sums per block per phase
+constexpr int kPersistSlots = 5;     // partial sums per block per phase
 
 // The barrier counts arrivals monotonically within one launch: barrier k of a launch with G
 // blocks is passed once the counter reaches k*G.  Each block's thread 0 adds its arrival with a
@@ -952,6 +952,14 @@ __device__ __forceinline__ void phase_update(const double *part, F &&update) {
 // tests) runs once per block, in thread 0, on the block's shared copy of the scalars; the other
 // threads read the coefficients of the next phase from shared memory, already in the solve's
 // arithmetic (FP64, FP32 or double-word).
+//
+// Two grid-wide reductions per iteration instead of three.  The s-phase also forms (s, r^) and
+// (t, r^), so the scalars of r_{k+1} = s - omega t follow without reducing over r:
+//   (r_{k+1}, r^) = (s, r^) - omega (t, r^),   |r_{k+1}|^2 = (s, s) - omega (2 (s, t) - omega (t, t)),
+// and the x/r update of iteration k runs inside the p staging of iteration k+1 (r of a halo row
+// is formed on the fly from its s and t; each row's owner writes x and r).  The iterates are
+// those of PETSc's KSPBCGS; only the rounding of rho and of the residual norm differs.  The
+// x/r update of the last iteration runs after the loop.
 template <class Vec, class Blk>
 __global__ void __launch_bounds__(kPersistThreads) k_bicgstab_halo(HaloMat<Blk> m, KV<Vec> v, KrylovScalars *ks,
                                                                    double *part, GridSync *gs) {
@@ -959,34 +967,49 @@ __global__ void __launch_bounds__(kPersistThreads) k_bicgstab_halo(HaloMat<Blk> 
   extern __shared__ __align__(16) unsigned char tab_raw[];
   Vec *tab = reinterpret_cast<Vec *>(tab_raw);
   __shared__ KrylovScalars s;
-  __shared__ __align__(16) unsigned char rs_raw[2 * sizeof(R)];
+  __shared__ int finish;   // 1 when the last iteration's x/r update is still to be applied
+  // coefficients in the solve's arithmetic: [0] beta, [1] beta * omega_old, [2] alpha, [3] omega
+  __shared__ __align__(16) unsigned char rs_raw[4 * sizeof(R)];
   R *rs = reinterpret_cast<R *>(rs_raw);
   if (threadIdx.x == 0) {
     s = *ks;
     rs[0] = (R)s.beta;
     rs[1] = (R)(s.beta * s.omegaold);
+    finish = 0;
   }
   __syncthreads();
   if (!s.active) return;
-  double *partP = part, *partS = part + kPersistMaxBlocks * kPersistSlots,
-         *partX = part + 2 * kPersistMaxBlocks * kPersistSlots;
+  double *partP = part, *partS = part + kPersistMaxBlocks * kPersistSlots;
   unsigned int gen = 0;   // barrier arrival target (thread 0)
   const int r0 = blockIdx.x * m.rpb;
   const int r1 = min(m.items, r0 + m.rpb);
   const int own = max(r1 - r0, 0);
   const int h0 = __ldg(m.halo_off + blockIdx.x);
   const int nloc = own + (__ldg(m.halo_off + blockIdx.x + 1) - h0);
-  bool ok = true;
+  bool ok = true, pending = false;   // pending: iteration k-1's x/r update not yet applied
   for (;;) {
     const int cur = s.it & 1, nxt = cur ^ 1;
-    // -- p <- r - beta omega v + beta p (staged);  v <- D^-1 A p;  (v, r^)
+    // -- [x <- x + alpha p + omega s; r <- s - omega t]  p <- r - beta omega v + beta p (staged);
+    //    v <- D^-1 A p;  (v, r^)
     {
-      const R beta = rs[0], bw = rs[1];
+      const R beta = rs[0], bw = rs[1], ap = rs[2], wp = rs[3];
       const Vec *__restrict__ Po = v.P[cur];
       const Vec *__restrict__ Vo = v.V[cur];
       for (int e = threadIdx.x; e < nloc; e += blockDim.x) {
         const int g = e < own ? r0 + e : __ldg(m.halo_idx + h0 + e - own);
-        const Vec pn = v_pupd(v.R[g], bw, Vo[g], beta, Po[g]);
+        const Vec po = Po[g];
+        Vec r;
+        if (pending) {
+          const Vec sg = v.S[g];
+          r = v_sub_scaled(sg, wp, v.T[g]);
+          if (e < own) {
+            v.X[g] = v_xupd(v.X[g], ap, po, wp, sg);
+            v.R[g] = r;
+          }
+        } else {
+          r = v.R[g];
+        }
+        const Vec pn = v_pupd(r, bw, Vo[g], beta, po);
         tab[e] = pn;
         if (e < own) v.P[nxt][g] = pn;
       }
@@ -1001,20 +1024,21 @@ __global__ void __launch_bounds__(kPersistThreads) k_bicgstab_halo(HaloMat<Blk> 
       block_partials_acc<1>(acc, partP);
       if (!(ok = grid_barrier(gs, gen))) break;
       phase_update<1>(partP, [&](const double *tot) {
+        finish = 0;   // the staging above applied the previous iteration's x/r update
         const double d1 = tot[0];
         if (d1 == 0.0 || isnan(d1)) {
           s.status = isnan(d1) ? UFE_ERR_NAN : UFE_ERR_DIVERGED;
           s.active = 0;
         } else {
           s.alpha = s.rho / d1;
-          rs[0] = (R)s.alpha;
+          rs[2] = (R)s.alpha;
         }
       });
       if (!s.active) break;
     }
-    // -- s <- r - alpha v (staged);  t <- D^-1 A s;  (s,t), (t,t), (s,s)
+    // -- s <- r - alpha v (staged);  t <- D^-1 A s;  (s,t), (t,t), (s,s), (s,r^), (t,r^)
     {
-      const R alpha = rs[0];
+      const R alpha = rs[2];
       const Vec *__restrict__ Vn = v.V[nxt];
       for (int e = threadIdx.x; e < nloc; e += blockDim.x) {
         const int g = e < own ? r0 + e : __ldg(m.halo_idx + h0 + e - own);
@@ -1023,60 +1047,46 @@ __global__ void __launch_bounds__(kPersistThreads) k_bicgstab_halo(HaloMat<Blk> 
         if (e < own) v.S[g] = sv;
       }
       __syncthreads();
-      DotAcc<Vec> acc[3];
+      DotAcc<Vec> acc[5];
       for (int il = threadIdx.x; il < own; il += blockDim.x) {
         const int i = r0 + il;
         const Vec si = tab[il];
         const Vec ti = v_mul(v.dinv[i], halo_row(m, i, il, tab));
         v.T[i] = ti;
+        const Vec rp = v.RP[i];
         acc[0].add(si, ti);
         acc[1].add(ti, ti);
         acc[2].add(si, si);
+        acc[3].add(si, rp);
+        acc[4].add(ti, rp);
       }
-      block_partials_acc<3>(acc, partS);
+      block_partials_acc<5>(acc, partS);
       if (!(ok = grid_barrier(gs, gen))) break;
-      phase_update<3>(partS, [&](const double *tot) {
+      phase_update<5>(partS, [&](const double *tot) {
         if (tot[1] == 0.0) {
           if (tot[2] != 0.0) {
             s.status = UFE_ERR_DIVERGED;
             s.active = 0;
-          } else {
-            s.omega = 0.0;
-            s.tbreak = 1;
+            return;
           }
+          s.omega = 0.0;
+          s.tbreak = 1;
         } else if (isnan(tot[1])) {
           s.status = UFE_ERR_NAN;
           s.active = 0;
+          return;
         } else {
           s.omega = tot[0] / tot[1];
         }
-        rs[1] = (R)s.omega;
-      });
-      if (!s.active) break;
-    }
-    // -- x <- x + alpha p + omega s;  r <- s - omega t;  (r, r^), (r, r)
-    {
-      const R alpha = rs[0], omega = rs[1];
-      DotAcc<Vec> acc[2];
-      for (int il = threadIdx.x; il < own; il += blockDim.x) {
-        const int i = r0 + il;
-        const Vec pi = v.P[nxt][i], si = v.S[i], ti = v.T[i];
-        v.X[i] = v_xupd(v.X[i], alpha, pi, omega, si);
-        const Vec ri = v_sub_scaled(si, omega, ti);
-        v.R[i] = ri;
-        acc[0].add(ri, v.RP[i]);
-        acc[1].add(ri, ri);
-      }
-      block_partials_acc<2>(acc, partX);
-      if (!(ok = grid_barrier(gs, gen))) break;
-      phase_update<2>(partX, [&](const double *tot) {
+        const double w = s.omega;
+        finish = 1;   // this iteration's x/r update is due from here on
         s.it += 1;
         s.total_its += 1;
-        const double dp = sqrt(tot[1]);
+        const double rho_new = tot[3] - w * tot[4];
+        const double dp = sqrt(fmax(tot[2] - w * (2.0 * tot[0] - w * tot[1]), 0.0));
         s.dp = dp;
-        const double rho_new = tot[0];
         s.rhoold = s.rho;
-        s.omegaold = s.omega;
+        s.omegaold = w;
         s.rho = rho_new;
         if (s.tbreak) { s.active = 0; s.status = UFE_OK; s.dp = 0.0; }
         else if (isnan(dp)) { s.status = UFE_ERR_NAN; s.active = 0; }
@@ -1086,9 +1096,22 @@ __global__ void __launch_bounds__(kPersistThreads) k_bicgstab_halo(HaloMat<Blk> 
         else if (rho_new == 0.0) { s.status = UFE_ERR_DIVERGED; s.active = 0; }
         else s.beta = (s.rho / s.rhoold) * (s.alpha / s.omegaold);
         rs[0] = (R)s.beta;
-        rs[1] = (R)(s.beta * s.omegaold);
+        rs[1] = (R)(s.beta * w);
+        rs[3] = (R)w;
       });
       if (!s.active) break;
+      pending = true;
+    }
+  }
+  // the x/r update of the last iteration
+  if (ok && finish) {
+    const R alpha = rs[2], omega = rs[3];
+    const int nxt = ((s.it - 1) & 1) ^ 1;   // the parity p was written with in that iteration
+    for (int il = threadIdx.x; il < own; il += blockDim.x) {
+      const int i = r0 + il;
+      const Vec si = v.S[i];
+      v.X[i] = v_xupd(v.X[i], alpha, v.P[nxt][i], omega, si);
+      v.R[i] = v_sub_scaled(si, omega, v.T[i]);
     }
   }
   if (threadIdx.x == 0) {
