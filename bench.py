@@ -557,6 +557,7 @@ def run_learned(args):
     train_ids = range(args.learned_train)
     test_ids = range(100000, 100000 + args.learned_test)
     p32_of = lambda p: _with(pkg, p, precision=pkg.abi.PREC_FP32_REFINE)
+    pair_of = lambda p: _with(pkg, p, precision=pkg.abi.PREC_FP32_PAIR)
     out = {}
     with pkg.VelocitySolver(mesh, device=local) as s:
         net = pkg.LearnedStart(s, seed=1)
@@ -576,8 +577,9 @@ def run_learned(args):
         gen_wall = time.perf_counter() - t0
         losses, train_ms = net.train(epochs=args.learned_epochs, lr=args.learned_lr)
         net.dataset_clear()
-        rows = {"cold_fp64": [], "learned_fp64": [], "learned_fp32": []}
-        errs = {"cold_fp64": [], "learned_fp64": [], "learned_fp32": []}
+        keys = ("cold_fp64", "cold_fp32_pair", "learned_fp64", "learned_fp32_pair", "learned_fp32")
+        rows = {k: [] for k in keys}
+        errs = {k: [] for k in keys}
         pred_ms = []
         with ClockSampler(local) as clocks:
             for m in test_ids:
@@ -599,24 +601,27 @@ def run_learned(args):
                         s.solve_resident(_with(pkg, p, visc_it_norm_dUV_tol=1e-6, visc_it_nit=400), diva=False)
                     ut = np.r_[s.velocity_download()]
                     errs["cold_fp64"].append(np.linalg.norm((uc - ut)[sel]) / np.linalg.norm(ut[sel]))
-                for key, pp in (("learned_fp64", p), ("learned_fp32", p32_of(p))):
+                st = s.solve_resident(pair_of(p), diva=False, cold_start=True)
+                rows["cold_fp32_pair"].append(st)
+                if ut is not None:
+                    u = np.r_[s.velocity_download()]
+                    errs["cold_fp32_pair"].append(np.linalg.norm((u - ut)[sel]) / np.linalg.norm(ut[sel]))
+                for key, pp in (("learned_fp64", p), ("learned_fp32_pair", pair_of(p)), ("learned_fp32", p32_of(p))):
                     pred_ms.append(net.predict(s))
                     st = s.solve_resident(pp, diva=False, cold_start=False)
                     rows[key].append(st)
                     if ut is not None:
                         u = np.r_[s.velocity_download()]
                         errs[key].append(np.linalg.norm((u - ut)[sel]) / np.linalg.norm(ut[sel]))
-                print(f"held-out {m}: cold {rows['cold_fp64'][-1]['n_visc_its']} learned "
-                      f"{rows['learned_fp64'][-1]['n_visc_its']} / {rows['learned_fp32'][-1]['n_visc_its']}",
-                      file=sys.stderr, flush=True)
+                print(f"held-out {m}: Picard iterations " +
+                      " ".join(f"{k} {rows[k][-1]['n_visc_its']}" for k in keys), file=sys.stderr, flush=True)
         net.close()
     n = len(test_ids)
     mean_pred = float(np.mean(pred_ms))
     def rate(key, extra_ms=0.0):
         return n / ((sum(r["device_ms"] for r in rows[key]) + n * extra_ms) / 1000.0)
-    vals = {"cold_fp64": rate("cold_fp64"), "learned_fp64": rate("learned_fp64", mean_pred),
-            "learned_fp32": rate("learned_fp32", mean_pred)}
-    best = max(("learned_fp64", "learned_fp32"), key=lambda k: vals[k])
+    vals = {k: rate(k, mean_pred if k.startswith("learned") else 0.0) for k in rows}
+    best = max(vals, key=lambda k: vals[k])   # the fastest path, zero or learned start
     peaks, peak_kind = measured_peaks()
     line = {
         "metric": METRIC, "value": round(vals[best], 4), "unit": UNIT, "n_gpus": world, "steps": n, "warmup": 0,

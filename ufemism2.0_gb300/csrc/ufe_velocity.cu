@@ -83,10 +83,12 @@ PhysParams make_phys(const ufe_solver_params &p, int has_bc) {
 }
 
 // calc_effective_viscosity_Glen_2D / _3D_uv_only (constitutive_equation.f90:25-80)
-__device__ __forceinline__ double glen(double eps0, double ux, double uy, double vx, double vy,
-                                       double uz, double vz, double A, double n) {
+// Glen's flow law, 3-D (constitutive_equation.f90:25-80), with A^(-1/n) evaluated beforehand:
+// 0.5 A^(-1/n) (eps^2 + eps0^2)^((1-n)/(2n))
+__device__ __forceinline__ double glen_apow(double eps0, double ux, double uy, double vx, double vy,
+                                            double uz, double vz, double A_pow, double n) {
   double e = ux * ux + vy * vy + ux * vy + 0.25 * ((uy + vx) * (uy + vx)) + 0.25 * (uz * uz + vz * vz) + eps0;
-  return 0.5 * pow(A, -1.0 / n) * pow(e, (1.0 - n) / (2.0 * n));
+  return 0.5 * A_pow * pow(e, (1.0 - n) / (2.0 * n));
 }
 __device__ __forceinline__ double glen2d(double eps0, double ux, double uy, double vx, double vy,
                                          double A, double n) {
@@ -132,7 +134,8 @@ struct OpRow {  // a CSR family with shared pattern
 // vertically averaged flow factor (calc_vertically_averaged_flow_parameter, SSA_main.f90:312-337)
 __global__ void k_prologue(int nV, int nTri, int nz, OpRow ab, const double *Hi, const double *Hs,
                            const double *A_flow, const double *zeta, double2 *tau_d, double *Avav,
-                           PicardScalars *ps, KrylovScalars *ks, double relax0, double eps0, double n_glen) {
+                           double *A_pow, PicardScalars *ps, KrylovScalars *ks, double relax0, double eps0,
+                           double n_glen) {
   int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < nTri; t += stride) {
     double Hib = 0.0, dx = 0.0, dy = 0.0;
@@ -151,6 +154,10 @@ __global__ void k_prologue(int nV, int nTri, int nz, OpRow ab, const double *Hi,
         a = a + 0.5 * (A_flow[(int64_t)k * nV + v] + A_flow[(int64_t)(k - 1) * nV + v]) * (zeta[k] - zeta[k - 1]);
       Avav[v] = a;
     }
+  // DIVA: A^(-1/n) per vertex and layer, constant over the Picard iterations of a solve
+  if (A_pow)
+    for (int64_t ix = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; ix < (int64_t)nV * nz; ix += stride)
+      A_pow[ix] = pow(A_flow[ix], -1.0 / n_glen);
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     PicardScalars &p = *ps;
     p.L2 = 1e9;
@@ -202,7 +209,7 @@ __global__ void k_vertex_ssa(int nV, OpRow ba, const double2 *uv, const double *
 // calc_effective_viscosity (:412-479), the surface value of calc_F_integrals' F2 (:481-520) and
 // the vertex part of calc_effective_basal_friction_coefficient (:522-574).
 __global__ void k_vertex_diva(int nV, int nTri, int nz, OpRow ba, const double2 *uv, const double2 *uv_base,
-                              const double2 *tau_b, const double *eta_3D_b, const double *A_flow,
+                              const double2 *tau_b, const double *eta_3D_b, const double *A_pow,
                               const double *Hi, const double *zeta_g, SlidingIn sl, PhysParams q,
                               const PicardScalars *ps, double *eta_3D_a, double *N_a, double *F2a1,
                               double *beta_a, double *beta_eff_a) {
@@ -238,7 +245,7 @@ __global__ void k_vertex_diva(int nV, int nTri, int nz, OpRow ba, const double2 
         dvz = dvz + m * (tb.y * zeta[l] / e);
       }
       int64_t ix = (int64_t)l * nV + vi;
-      double e = glen(eps0, ux, uy, vx, vy, duz, dvz, A_flow[ix], q.n_glen);
+      double e = glen_apow(eps0, ux, uy, vx, vy, duz, dvz, A_pow[ix], q.n_glen);
       e = fmin(fmax(e, q.visc_eff_min), eta_max);
       eta_k[l] = e;
       eta_3D_a[ix] = e;
@@ -1024,6 +1031,7 @@ Work *ensure_work(ufe_ctx *ctx) {
   w->Hs = alloc_n<double>(nV);
   w->Avav = alloc_n<double>(nV);
   w->A_flow = alloc_n<double>((size_t)nV * nz);
+  w->A_pow = alloc_n<double>((size_t)nV * nz);
   w->beta_sq = alloc_n<double>(nV);
   w->alpha_sq = alloc_n<double>(nV);
   w->effp = alloc_n<double>(nV);
@@ -1069,7 +1077,7 @@ void free_work(ufe_ctx *ctx) {
                   w->kv.P[0], w->kv.P[1], w->kv.V[0], w->kv.V[1], w->kv.x32, w->kv.R32, w->kv.RP32,
                   w->kv.S32, w->kv.T32, w->kv.dinv32, w->kv.P32[0], w->kv.P32[1], w->kv.V32[0],
                   w->kv.V32[1], w->uv, w->tau_d, w->fgr_b, w->bc_mask, w->bc_uv, w->uv_base, w->tau_b,
-                  w->eta_3D_b, w->bfc_b, w->F2b1, w->beta_b, w->Hi, w->Hs, w->Avav, w->A_flow, w->beta_sq,
+                  w->eta_3D_b, w->bfc_b, w->F2b1, w->beta_b, w->Hi, w->Hs, w->Avav, w->A_flow, w->beta_sq, w->A_pow,
                   w->alpha_sq, w->effp, w->tys, w->mask_gr, w->N_a, w->beta_a, w->beta_eff_a, w->F2a1,
                   w->eta_3D_a, w->F1_3D_a, w->N_b_in, w->dNx_b_in, w->dNy_b_in, w->beta_b_in, w->ks,
                   w->ps, w->err, w->ppart, w->gsync, w->sell_off, w->sell_col, w->sell_map, w->sell_blk,
@@ -1506,7 +1514,8 @@ struct Solver {
   void enqueue_prologue(bool diva) {
     k_prologue<<<eblocks(std::max(w->nV, w->nTri)), kThreads, 0, s>>>(
         w->nV, w->nTri, w->nz, ab, w->Hi, w->Hs, w->A_flow, ctx->zeta, w->tau_d, diva ? nullptr : w->Avav,
-        w->ps, w->ks, p.visc_it_relax, p.Glens_flow_law_epsilon_sq_0, p.Glens_flow_law_exponent);
+        diva ? w->A_pow : nullptr, w->ps, w->ks, p.visc_it_relax, p.Glens_flow_law_epsilon_sq_0,
+        p.Glens_flow_law_exponent);
     UFE_CUDA(cudaMemsetAsync(w->ks + 1, 0, sizeof(KrylovScalars), s));
     UFE_CUDA(cudaGetLastError());
   }
@@ -1514,7 +1523,7 @@ struct Solver {
   void enqueue_picard_pre(bool diva, CondArg inner) {
     if (diva) {
       k_vertex_diva<<<eblocks(w->nV), kThreads, 0, s>>>(
-          w->nV, w->nTri, w->nz, ba, w->uv, w->uv_base, w->tau_b, w->eta_3D_b, w->A_flow, w->Hi, ctx->zeta,
+          w->nV, w->nTri, w->nz, ba, w->uv, w->uv_base, w->tau_b, w->eta_3D_b, w->A_pow, w->Hi, ctx->zeta,
           sliding(), q, w->ps, w->eta_3D_a, w->N_a, w->F2a1, w->beta_a, w->beta_eff_a);
     } else {
       k_vertex_ssa<<<eblocks(w->nV), kThreads, 0, s>>>(w->nV, ba, w->uv, w->Avav, w->Hi, sliding(), q, w->ps,

@@ -109,6 +109,7 @@ struct Work {
   double *beta_b = nullptr;     // applied friction on triangles (SSA) / beta_eff_b (DIVA)
   // vertex inputs
   double *Hi = nullptr, *Hs = nullptr, *Avav = nullptr, *A_flow = nullptr;
+  double *A_pow = nullptr;      // nz x nV: A_flow^(-1/n) of the current DIVA solve
   double *beta_sq = nullptr, *alpha_sq = nullptr, *effp = nullptr, *tys = nullptr;
   int32_t *mask_gr = nullptr;
   int32_t any_grounded = 0;
