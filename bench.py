@@ -656,17 +656,22 @@ def run_ensemble(args):
 
     rank, world, local = dist_env()
     torch.cuda.set_device(local)
+    if world > 1:
+        torch.distributed.init_process_group("nccl")
     pkg = __graft_entry__.load_package()
     pkg.build()
     rng = np.random.default_rng(7)
     sizes = np.exp(rng.uniform(np.log(args.ens_min), np.log(args.ens_max), args.ens_members)).astype(int)
+    # members shard over the ranks by size (no exchange on the data path); each rank builds and
+    # solves its own share side by side
+    mine = pkg.ensemble.shard(rank, world, sizes)
     members = []
-    for k, nv in enumerate(sizes):
-        mesh = pkg.geometry.ensemble_mesh(nV=int(nv), seed=k)
+    for k in mine:
+        mesh = pkg.geometry.ensemble_mesh(nV=int(sizes[k]), seed=k)
         ice, p = pkg.geometry.ensemble_member(mesh, 500 + k)
         members.append((mesh, ice, p))
-        print(f"member {k}: {mesh.nV} vertices", file=sys.stderr, flush=True)
-    p = members[0][2]
+        print(f"rank {rank} member {k}: {mesh.nV} vertices", file=sys.stderr, flush=True)
+    p = members[0][2] if members else pkg.abi.default_params()
     solvers = [pkg.VelocitySolver(m, device=local) for m, _, _ in members]
     tune = []
     for sv, (m, ice, _) in zip(solvers, members):
@@ -679,27 +684,46 @@ def run_ensemble(args):
         st = sv.solve_resident(p, diva=False, cold_start=True)
         seq_ms += st["device_ms"]
         its.append((st["n_visc_its"], st["n_Axb_its"]))
-    pkg.ensemble_solve(solvers, p, diva=False, cold_start=True)   # warm-up of the concurrent launch
+    if solvers:
+        pkg.ensemble_solve(solvers, p, diva=False, cold_start=True)   # warm-up of the concurrent launch
     walls = []
+    if world > 1:
+        torch.distributed.barrier()
     with ClockSampler(local) as clocks:
         for _ in range(args.steps):
-            stats, wall = pkg.ensemble_solve(solvers, p, diva=False, cold_start=True)
+            if solvers:
+                stats, wall = pkg.ensemble_solve(solvers, p, diva=False, cold_start=True)
+            else:
+                wall = 0.0   # more ranks than members: this rank has none
             walls.append(wall)
     for sv in solvers:
         sv.close()
-    n = len(members)
-    value = n / (statistics.mean(walls) / 1000.0)
-    line = {"metric": "ensemble SSA velocity solves/s, members side by side, 1xGB300", "value": round(value, 4),
+    # the only exchange: the per-member results, gathered on the host after the timed region
+    results = pkg.ensemble.gather_results({k: {"nV": m.nV, "its": it, "tune": tu}
+                                           for k, (m, _, _), it, tu in zip(mine, members, its, tune)})
+    wall_max = pkg.ensemble.max_over_ranks(statistics.mean(walls), device=f"cuda:{local}")
+    seq_total = pkg.ensemble.max_over_ranks(seq_ms, device=f"cuda:{local}")
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    if rank != 0:
+        return
+    n = len(results)
+    order = sorted(results)
+    value = n / (wall_max / 1000.0)
+    line = {"metric": f"ensemble SSA velocity solves/s, members side by side, {world}xGB300", "value": round(value, 4),
             "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": 1,
-            "ms_per_step": round(statistics.mean(walls), 2), "higher_is_better": True, "scaling": "weak",
+            "ms_per_step": round(wall_max, 2), "higher_is_better": True,
+            "scaling": "strong" if world > 1 else "weak",
             "vs_baseline": None, "dtype": "f64",
             "data": "synthetic ensemble geometries from seeded random fields on generated meshes (no files)",
-            "config": {"workload": ENSEMBLE_WORKLOAD, "members": n, "vertices": [m.nV for m, _, _ in members],
-                       "total_vertices": int(sum(m.nV for m, _, _ in members)), "rows_per_warp": tune},
-            "one_after_another": {"value": round(n / (seq_ms / 1000.0), 4), "unit": UNIT,
-                                  "ms": round(seq_ms, 1)},
-            "speedup_side_by_side": round(seq_ms / statistics.mean(walls), 3),
-            "picard_its": [a for a, b in its], "krylov_its": [b for a, b in its],
+            "config": {"workload": ENSEMBLE_WORKLOAD, "members": n, "vertices": [results[k]["nV"] for k in order],
+                       "total_vertices": int(sum(results[k]["nV"] for k in order)),
+                       "rows_per_warp": [results[k]["tune"] for k in order],
+                       "parallelism": f"members partitioned over {world} rank(s) by size"},
+            "one_after_another": {"value": round(n / (seq_total / 1000.0), 4), "unit": UNIT,
+                                  "ms": round(seq_total, 1)},
+            "speedup_side_by_side": round(seq_total / wall_max, 3),
+            "picard_its": [results[k]["its"][0] for k in order], "krylov_its": [results[k]["its"][1] for k in order],
             "clocks": clocks.summary()}
     print(json.dumps(line))
 

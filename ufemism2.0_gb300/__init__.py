@@ -11,4 +11,5 @@ from .solver import CSR, UfeError, VelocitySolver, ensemble_solve, new_diva_stat
 from .thermo import ColumnSolver, zeta_operators  # noqa: F401
 from . import thermo  # noqa: F401
 from . import learned  # noqa: F401
+from . import ensemble  # noqa: F401
 from .learned import LearnedStart  # noqa: F401
