@@ -2486,6 +2486,7 @@ extern "C" int32_t ufe_profile_krylov_persistent(ufe_ctx *ctx, int32_t precision
     if (fp32) {
       S.enqueue_inner_init(none);
     } else {
+      UFE_CUDA(cudaMemsetAsync(w->ks, 0, sizeof(KrylovScalars), s));   // no state of the last solve
       BsrMat<double, double, 1> m = S.mat64<1>();
       k_krylov_init<BsrMat<double, double, 1>><<<krylov_grid(m, kThreads, S.grid), kThreads, 0, s>>>(
           m, S.kv64(), w->ks, 0.0, 0.0, iterations, 1, ctx->red.partials, ctx->red.tickets, none, 0);
