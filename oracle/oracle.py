@@ -1,8 +1,8 @@
 """ctypes wrapper of the CPU oracle (TEST INFRASTRUCTURE ONLY).
 
 The oracle restates UFEMISM's velocity-solve routines in C (oracle/ufe_oracle.c).  Tests, the
-smoke check and the benchmark's CPU-baseline leg use it as the checker; the product never imports
-this module.  :class:`Oracle` mirrors the method names of the product's ``VelocitySolver``.
+smoke check and the benchmark's CPU-baseline leg compare the GPU results with it; the product
+never imports this module.  :class:`Oracle` mirrors the method names of the product's ``VelocitySolver``.
 """
 from __future__ import annotations
 

@@ -1,8 +1,8 @@
 /*
  * ufe_oracle.c -- CPU restatement of UFEMISM 2.0's velocity solve (TEST INFRASTRUCTURE ONLY).
  *
- * Used by the tests, the smoke check and the benchmark's CPU-baseline leg as the checker.  The
- * product (the GPU library) never links or calls this code.
+ * Used by the tests, the smoke check and the benchmark's CPU-baseline leg as the reference the
+ * GPU results are compared with.  The product (the GPU library) never links or calls this code.
  *
  * Paths are relative to the UFEMISM2.0 source tree.  Arithmetic follows the Fortran expressions
  * in their left-to-right evaluation order, so that a build without FMA contraction

@@ -1,8 +1,8 @@
 /*
  * ufe_oracle.h -- CPU restatement of UFEMISM 2.0's velocity-solve path, in FP64.
  *
- * TEST INFRASTRUCTURE ONLY.  This library is the checker the GPU library is compared against
- * (tests, the smoke check and the CPU baseline leg of the benchmark).  Nothing in the product
+ * TEST INFRASTRUCTURE ONLY.  This library is what the GPU library is compared against (tests,
+ * the smoke check and the CPU baseline leg of the benchmark).  Nothing in the product
  * links, loads or calls it.
  *
  * Every function restates the Fortran routine it names (file:line relative to the UFEMISM2.0

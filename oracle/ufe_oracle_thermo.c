@@ -1,6 +1,6 @@
 /*
  * ufe_oracle_thermo.c -- CPU restatement of UFEMISM 2.0's column temperature solve
- * (TEST INFRASTRUCTURE ONLY: the checker for the GPU library's thermodynamics entry points).
+ * (TEST INFRASTRUCTURE ONLY: what the GPU library's thermodynamics entry points are compared with).
  *
  * Paths are relative to the UFEMISM2.0 source tree.  Every expression keeps the Fortran
  * evaluation order (left to right for * and /, unary minus applied to the whole product), and

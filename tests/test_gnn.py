@@ -103,7 +103,7 @@ def test_gnn_warm_start_saves_picard_iterations(pkg, gpu_lib):
 
     The criterion (L2 of the relative change < 1e-4, SSA_DIVA_utilities.f90:179) stops this
     slowly contracting Picard iteration some way from its fixed point, from whichever side it
-    comes; so both starts are judged against a tightly converged solve (1e-10), and the learned
+    comes; so both starts are compared with a tightly converged solve (1e-10), and the learned
     start must land no farther from it than the cold start does (within 50 %)."""
     mesh = pkg.geometry.ensemble_mesh(nV=3000, seed=0)
     T = mesh.Tri - 1
