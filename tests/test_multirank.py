@@ -65,3 +65,22 @@ def test_two_ranks_gather_every_member_once(pkg):
         for r, part in enumerate(parts):
             assert all(owner[i] == r for i in part)                # each solved by its owner only
         assert slowest == max(len(parts[0]), len(parts[1]) + 0.5)  # the max over ranks
+
+
+def test_mixed_ensemble_members(pkg):
+    """The mixed-size DIVA ensemble's generator: 64 sizes log-uniform in [20k, 400k] summing to
+    about 8.1M vertices, and a small member with the stated bed statistics and a dome with
+    grounded and floating ice."""
+    G = pkg.geometry
+    sizes = G.mixed_ensemble_sizes()
+    assert len(sizes) == 64 and sizes.min() >= 20_000 and sizes.max() <= 400_000
+    assert abs(sizes.sum() - 8.1e6) < 0.05e6
+    m = G.mixed_ensemble_mesh(6000, seed=2, nz=6)
+    assert 5000 < m.nV < 7500
+    ice, p = G.mixed_ensemble_member(m, 2)
+    bed = ice["Hb"]
+    assert abs(bed.mean() + 300.0) < 1e-6 and abs(bed.std() - 800.0) < 1e-6
+    on_ice = ice["Hi"] > 0
+    assert 0.2 < on_ice.mean() < 0.7
+    g = ice["mask_grounded_ice"].astype(bool)
+    assert g.any() and (on_ice & ~g).any()     # grounded and floating ice both present

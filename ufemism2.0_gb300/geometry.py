@@ -403,3 +403,67 @@ def ensemble_member(mesh, member, A=1e-16, H0=3000.0, R=600e3, bed_sigma=400.0, 
     params = abi.default_params(choice_sliding_law="Weertman", slid_Weertman_m=3.0,
                                 visc_it_norm_dUV_tol=1e-4, stress_balance_PETSc_rtol=1e-8)
     return ice, params
+
+
+# ---- mixed-size DIVA ensemble (64 members, 20k-400k vertices) ---------------------------------
+MIXED_L = 6000e3      # domain side [m]
+MIXED_R = 2200e3      # dome radius [m]
+
+
+def fractal_field(x, y, seed, slope=-2.0, L=MIXED_L, kmax_len=10e3, n_modes=512):
+    """A random field with power spectrum ~ k^slope between wavelengths L and kmax_len: random
+    plane waves with wavenumbers log-uniform in [2 pi / L, 2 pi / kmax_len], random directions
+    and phases, amplitudes k^(slope/2) times the square root of each mode's share of the
+    log-wavenumber band (so the spectral density follows the power law); scaled to zero mean
+    and unit RMS over the points given."""
+    rng = np.random.default_rng(seed)
+    k = np.exp(rng.uniform(np.log(2.0 * np.pi / L), np.log(2.0 * np.pi / kmax_len), n_modes))
+    th = rng.uniform(0.0, 2.0 * np.pi, n_modes)
+    ph = rng.uniform(0.0, 2.0 * np.pi, n_modes)
+    amp = k ** (0.5 * slope) * np.sqrt(k)   # log-uniform k: density ~ 1/k, so weight by sqrt(k)
+    f = np.zeros(np.shape(x))
+    for j in range(n_modes):
+        f += amp[j] * np.cos(k[j] * (np.cos(th[j]) * x + np.sin(th[j]) * y) + ph[j])
+    f = f - f.mean()
+    return f / np.sqrt(np.mean(f * f))
+
+
+def mixed_ensemble_mesh(nV, seed=0, nz=12):
+    """A mesh of about nV vertices over the 6,000 km domain, fine cells in a band around the
+    dome margin r = 2,200 km (the grounding zone), cells twice as large elsewhere."""
+    return ensemble_mesh(nV=nV, L=MIXED_L, seed=seed, nz=nz, R=MIXED_R)
+
+
+def mixed_ensemble_member(mesh, member, A=1e-16, H0=4000.0, bed_rms=800.0, bed_mean=-300.0):
+    """Member `member` of the mixed-size DIVA ensemble: a fractal bed (spectral slope -2, RMS
+    800 m, mean -300 m, seeded by the member), a dome of thickness H0 = 4,000 m and radius 2,200 km,
+    floating where thinner than flotation, log-normal beta^2 as in the learned-start ensemble.
+    Returns (ice, params) for a DIVA solve (Weertman m = 3, n = 3, A = 1e-16, Picard 1e-4,
+    BiCGStab 1e-8)."""
+    x, y = mesh.V[:, 0], mesh.V[:, 1]
+    bed = bed_mean + bed_rms * fractal_field(x, y, 3000 + member)
+    Hi = np.ascontiguousarray(dome_thickness(x, y, H0=H0, R=MIXED_R))
+    SL = np.zeros(mesh.nV)
+    taf = thickness_above_flotation(Hi, bed, SL)
+    Hs = np.ascontiguousarray(surface_elevation(Hi, bed, SL))
+    grounded = (Hi > 0) & (taf > 0)
+    fgr = grounded_fraction_b_vertex(mesh, np.where(Hi > 0, taf, -1.0))
+    beta_sq = np.exp(np.log(1e4) + 0.5 * smooth_field(x, y, 150e3, 4000 + member))
+    ice = dict(Hi=Hi, Hs=Hs, Hb=bed, SL=SL,
+               A_flow=np.asfortranarray(np.full((mesh.nV, mesh.nz), A)),
+               fraction_gr_b=fgr, mask_grounded_ice=np.ascontiguousarray(grounded.astype(np.int32)),
+               beta_sq=np.ascontiguousarray(beta_sq))
+    return ice, mixed_ensemble_params()
+
+
+def mixed_ensemble_params():
+    """Solver parameters of the mixed-size DIVA ensemble (the same for every member)."""
+    return abi.default_params(choice_sliding_law="Weertman", slid_Weertman_m=3.0,
+                              visc_it_norm_dUV_tol=1e-4, stress_balance_PETSc_rtol=1e-8)
+
+
+def mixed_ensemble_sizes(n=64, lo=20_000, hi=400_000, seed=18):
+    """Vertex counts of the mixed-size ensemble: log-uniform in [lo, hi], seeded (seed 18: 8.10M
+    vertices in all, the log-uniform mean of 127k per member)."""
+    rng = np.random.default_rng(seed)
+    return np.exp(rng.uniform(np.log(lo), np.log(hi), n)).astype(int)
