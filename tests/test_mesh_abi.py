@@ -45,6 +45,21 @@ def test_dome_workload_size(pkg):
     assert ice["Hi"].max() == pytest.approx(3000.0, rel=2e-2)
 
 
+def test_benchmark_workload_sizes(pkg):
+    """The synthetic workloads the benchmark measures have the sizes their descriptions state."""
+    G = pkg.geometry
+    mesh, ice, params = G.channel_case(seed=0)                 # DIVA channel: ~58k vertices, nz 12
+    assert 55_000 < mesh.nV < 62_000 and mesh.nz == 12
+    x = mesh.V[:, 0]
+    assert x.max() - x.min() == pytest.approx(640e3, rel=1e-6)
+    mesh3 = G.ensemble_mesh(nV=30_000, seed=0)                # SSA ensemble: ~30k vertices
+    assert 28_500 < mesh3.nV < 31_500
+    mesh2, fields, tp = G.thermo_case()                       # thermodynamics: ~200k columns x 30
+    assert 190_000 < mesh2.nV < 210_000 and mesh2.nz == 30
+    frac_free = np.mean(fields["Hi"] <= 0.0)
+    assert 0.12 < frac_free < 0.2                              # ~15% of the columns ice-free
+
+
 def _header_functions():
     src = open(HEADER).read()
     return sorted(set(re.findall(r"\b(ufe_[a-z0-9_]+)\s*\(", src)))
