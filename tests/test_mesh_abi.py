@@ -65,6 +65,13 @@ def _header_functions():
     return sorted(set(re.findall(r"\b(ufe_[a-z0-9_]+)\s*\(", src)))
 
 
+def test_integration_guide_covers_every_entry_point():
+    """Every function of the C ABI appears in the integration guide (what it replaces or serves)."""
+    guide = open(os.path.join(os.path.dirname(HEADER), "..", "INTEGRATION.md")).read()
+    missing = [f for f in _header_functions() if f not in guide]
+    assert not missing, missing
+
+
 def test_library_exports_every_header_symbol(gpu_lib):
     for name in _header_functions():
         assert hasattr(gpu_lib, name), name
