@@ -219,7 +219,33 @@ def run_ours(args):
     for name in prec:
         sts, rate, _, _ = plain_runs[name]
         plain[name] = summary(sts, rate, u_plain["fp64"] if name != "fp64" else None, u_plain[name])
+        plain[name]["us_per_krylov_it_in_solve"] = round(1000.0 * plain[name]["ms_per_solve"]
+                                                         / max(plain[name]["krylov_its"], 1), 2)
     value64 = plain_runs["fp64"][1]
+
+    # ---- the FP64 reference solution for the velocity errors: the GPU FP64 path with Krylov to
+    # rtol 1e-12, run to the tightest Picard tolerance that the reference's divergence control
+    # (SSA_main.f90:196-213, DIVA_main.f90:211-228) lets finish on this channel
+    F64 = pkg.abi.PREC_FP64
+    ref_info, u_ref, tried = None, None, []
+    for tol in args.ref_tols:
+        p_ref = _with(pkg, params, precision=F64, stress_balance_PETSc_rtol=1e-12, stress_balance_PETSc_abstol=0.0,
+                      visc_it_norm_dUV_tol=tol, visc_it_nit=1000)
+        try:
+            st = solver.solve_resident(p_ref, diva=True, cold_start=True)
+        except pkg.UfeError as e:
+            tried.append({"picard_tol": tol, "status": e.code})
+            continue
+        tried.append({"picard_tol": tol, "status": st["status"]})
+        if st["status"] == 0:
+            u_ref = np.r_[solver.velocity_download()]
+            ref_info = {"picard_tol": tol, "krylov_rtol": 1e-12, "picard_its": st["n_visc_its"],
+                        "krylov_its": st["n_Axb_its"], "relax_applied": round(st["visc_it_relax_applied"], 4),
+                        "ms": round(st["device_ms"], 1), "tried": tried}
+            break
+
+    def err_ref(u):
+        return None if u_ref is None else float("%.3g" % (np.linalg.norm(u - u_ref) / np.linalg.norm(u_ref)))
 
     # the persistent Krylov kernels of the FP64 and double-word solves, per iteration; the
     # three-kernel FP64 iteration beside them.  Algorithmic bytes of one iteration: two 2x2-block
@@ -304,6 +330,9 @@ def run_ours(args):
             u = np.r_[solver.velocity_download()]
             sts, rate, _, _ = learned_runs[name]
             learned[name] = summary(sts, rate, u_plain["fp64"], u)
+            learned[name]["rel_l2_vs_fp64_reference"] = err_ref(u)
+            learned[name]["us_per_krylov_it_in_solve"] = round(1000.0 * learned[name]["ms_per_solve"]
+                                                               / max(learned[name]["krylov_its"], 1), 2)
         best = max(("fp64", "fp32_pair", "fp32_refined"), key=lambda k: learned[k]["value"] or 0.0)
         # end to end through the public C ABI with pinned host buffers: ice upload, prediction,
         # resident solve, velocity download -- every step
@@ -317,6 +346,32 @@ def run_ours(args):
             solver.velocity_download()
         torch.cuda.synchronize()
         t_e2e_l = slowest(time.perf_counter() - t0)
+        # the accuracy target at the tight tolerance: plain FP64 (zero start) against learned start +
+        # double-word Krylov, both run to the reference solution's Picard tolerance with the
+        # benchmark's Krylov tolerance; one solve each after a warm-up
+        if ref_info is not None:
+            solver.ice_upload(ice)
+            tight = {}
+            for tag, pname, learned_start in (("plain_fp64", "fp64", False), ("learned_fp32_pair", "fp32_pair", True)):
+                p_t = _with(pkg, prec[pname], visc_it_norm_dUV_tol=ref_info["picard_tol"], visc_it_nit=1000)
+                run_t = (lambda: learned_solve(p_t)) if learned_start else (lambda: solve(p_t))
+                try:
+                    run_t()
+                    sts_t, rate_t, _, _ = timed(run_t, 1, f"timed_tight_{tag}")
+                    u_t = np.r_[solver.velocity_download()]
+                    tight[tag] = {"value": round(rate_t, 4), "unit": UNIT, "picard_its": sts_t[0]["n_visc_its"],
+                                  "krylov_its": sts_t[0]["n_Axb_its"], "status": sts_t[0]["status"],
+                                  "rel_l2_vs_fp64_reference": err_ref(u_t), "_u": u_t}
+                except pkg.UfeError as e:
+                    tight[tag] = {"status": e.code}
+            if all("_u" in v for v in tight.values()):
+                a, b = tight["plain_fp64"].pop("_u"), tight["learned_fp32_pair"].pop("_u")
+                tight["rel_l2_between"] = float("%.3g" % (np.linalg.norm(b - a) / np.linalg.norm(a)))
+                tight["speedup"] = round(tight["learned_fp32_pair"]["value"] / tight["plain_fp64"]["value"], 3)
+            for v in tight.values():
+                if isinstance(v, dict):
+                    v.pop("_u", None)
+            learned["tight_tolerance_pair"] = tight
         net.close()
         learned["e2e"] = {"value": round(world * args.steps / t_e2e_l, 4), "unit": UNIT, "path": best,
                           "h2d_bytes_per_step": int(sum(v.nbytes for v in ice_h.values())),
@@ -328,7 +383,11 @@ def run_ours(args):
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        cpu = cpu_baseline(pkg, mesh, ice, params, plain_runs["fp64"][0][0]["n_Axb_its"], seconds=args.cpu_seconds)
+        cpu, u_oracle = cpu_baseline(pkg, mesh, ice, params)
+        # the GPU FP64 path against the oracle's own full solve of the same inputs
+        cpu["gpu_fp64_rel_l2_vs_oracle"] = float("%.3g" % (np.linalg.norm(u_plain["fp64"] - u_oracle)
+                                                          / np.linalg.norm(u_oracle)))
+        cpu["gpu_fp64_picard_krylov_its"] = [plain["fp64"]["picard_its"], plain["fp64"]["krylov_its"]]
     # the headline is the fastest measured path (zero or learned start, any Krylov precision); the
     # rates are already the slowest rank's, so every rank picks the same path
     cands = [(f"plain_{k}", plain_runs[k], k) for k in ("fp64", "fp32_pair", "fp32_refined")]
@@ -389,6 +448,7 @@ def run_ours(args):
                                             if head_name.startswith("learned") else " (zero start)")
                                + ", graph-resident solve"},
             "speedup_vs_plain_fp64": round(head_value / value64, 3),
+            "accuracy": accuracy_summary(plain, learned, ref_info, head_name, u_plain, err_ref),
             "plain": plain,
             "learned_start": learned,
             "e2e": head_e2e,
@@ -865,55 +925,108 @@ def run_thermo_reference(args):
     print(json.dumps(line))
 
 
-def cpu_baseline(pkg, mesh, ice, params, full_krylov_its, seconds=20.0, threads=None):
-    """Time the oracle (OpenMP on all host cores) on the first Picard iterations of the same solve
-    and scale by Krylov iterations to full solves."""
+def _oracle():
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
+    return oracle
+
+
+def accuracy_summary(plain, learned, ref_info, head_name, u_plain, err_ref):
+    """Every path's velocity error against the FP64 reference solution, and the target in words."""
+    if ref_info is None:
+        return {"reference": None, "statement": "no FP64 reference solution: every tolerance tried diverged"}
+    out = {"reference": ref_info,
+           "rel_l2_vs_fp64_reference": {f"plain_{k}": err_ref(u_plain[k]) for k in u_plain}}
+    if learned:
+        for k in ("fp64", "fp32_pair", "fp32_refined"):
+            if k in learned:
+                out["rel_l2_vs_fp64_reference"][f"learned_{k}"] = learned[k]["rel_l2_vs_fp64_reference"]
+    tight = (learned or {}).get("tight_tolerance_pair", {})
+    T = ref_info["picard_tol"]
+    e0 = out["rel_l2_vs_fp64_reference"]["plain_fp64"]
+    eh = out["rel_l2_vs_fp64_reference"].get(head_name)
+    parts = [f"At the benchmark's Picard tolerance (1e-4 on the squared relative change) every path, plain FP64 "
+             f"included, stops {e0:.1e} (plain FP64) to {eh:.1e} (headline) from the FP64 reference solution "
+             f"(Picard tolerance {T:g}, Krylov rtol 1e-12), so the 1e-6 target is not met at that tolerance."]
+    if "rel_l2_between" in tight:
+        lt = tight["learned_fp32_pair"]
+        met = lt["rel_l2_vs_fp64_reference"] is not None and lt["rel_l2_vs_fp64_reference"] <= 1e-6
+        parts.append(f"Run to the reference's own Picard tolerance {T:g}, learned start + double-word Krylov is "
+                     f"{lt['rel_l2_vs_fp64_reference']:.1e} from the reference solution (plain FP64 "
+                     f"{tight['plain_fp64']['rel_l2_vs_fp64_reference']:.1e}) at {tight['speedup']:.2f}x the plain FP64 "
+                     f"solves/s: the 1e-6 target is {'met' if met else 'not met'}.")
+    failed = ", ".join("%g" % t["picard_tol"] for t in ref_info["tried"][:-1]) or "none"
+    parts.append(f"Tighter Picard tolerances ({failed}) "
+                 f"end in the reference's divergence stop on this channel: its Picard iteration stalls near "
+                 f"L2 ~ 1e-8, which bounds how close any path can get to the fixed point.")
+    out["statement"] = " ".join(parts)
+    return out
+
+
+def oracle_full_solve(pkg, mesh, ice, params, threads=None):
+    """One complete DIVA solve by the oracle (OpenMP on all host cores): wall time, Picard and Krylov
+    counts and the velocity (u, v) pairs."""
+    oracle = _oracle()
     threads = threads or os.cpu_count()
     os.environ["OMP_NUM_THREADS"] = str(threads)
     orc = oracle.Oracle(mesh)
-    p = pkg.abi.default_params(**{f: getattr(params, f) for f, _ in params._fields_ if f != "reserved"})
-    done_its, elapsed, nit = 0, 0.0, 0
-    while elapsed < seconds and nit < 50:
-        p.visc_it_nit = nit
-        st = pkg.new_diva_state(mesh.nTri, mesh.nz, with_3d=False)
-        t0 = time.perf_counter()
-        nv, na, _ = orc.solve_DIVA(ice, st, p)
-        elapsed = time.perf_counter() - t0
-        done_its = na
-        nit = max(1, 2 * nit)
-    per_its = elapsed / max(done_its, 1)
-    value = 1.0 / (per_its * full_krylov_its)
-    return {"value": round(value, 6), "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"first {nv} Picard iterations ({done_its} Krylov its, {elapsed:.1f} s) of the same solve, "
-                      f"scaled to a full solve of {full_krylov_its} Krylov its"}
+    p = _with(pkg, params)
+    st = pkg.new_diva_state(mesh.nTri, mesh.nz, with_3d=False)
+    t0 = time.perf_counter()
+    nv, na, stats = orc.solve_DIVA(ice, st, p)
+    secs = time.perf_counter() - t0
+    return {"seconds": secs, "picard_its": nv, "krylov_its": na, "status": stats["status"], "cores": threads,
+            "u": np.r_[st["u_vav_b"], st["v_vav_b"]]}
+
+
+def cpu_baseline(pkg, mesh, ice, params, threads=None):
+    """The oracle timed on one full solve of the benchmark channel (no extrapolation)."""
+    full = oracle_full_solve(pkg, mesh, ice, params, threads)
+    d = {"value": round(1.0 / full["seconds"], 6), "unit": UNIT, "cores": full["cores"], "kind": "port",
+         "sample": f"full solve: {full['picard_its']} Picard / {full['krylov_its']} Krylov iterations in "
+                   f"{full['seconds']:.1f} s (status {full['status']})",
+         "picard_its": full["picard_its"], "krylov_its": full["krylov_its"], "seconds": round(full["seconds"], 2)}
+    return d, full["u"]
 
 
 def run_reference(args):
+    """The reference arm: the oracle (the CPU restatement of the reference's algorithm) on the host
+    cores.  One full solve is measured first; each timed step is then a bounded sample -- the first
+    Picard iterations of the same solve -- whose rate is scaled by the Krylov iterations of that full
+    solve, measured in this run."""
     rank, world, local = dist_env()
     if rank != 0:
         return
     pkg = __graft_entry__.load_package()
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import oracle
+    oracle = _oracle()
     oracle.build()
     mesh, ice, params = pkg.geometry.channel_case(seed=0)
-    full_its = args.full_krylov_its
+    full = oracle_full_solve(pkg, mesh, ice, params)
+    orc = oracle.Oracle(mesh)
     vals = []
     for i in range(args.warmup + args.steps):
-        c = cpu_baseline(pkg, mesh, ice, params, full_its, seconds=args.cpu_seconds)
+        p = _with(pkg, params, visc_it_nit=args.ref_sample_picard - 1)
+        st = pkg.new_diva_state(mesh.nTri, mesh.nz, with_3d=False)
+        t0 = time.perf_counter()
+        nv, na, _ = orc.solve_DIVA(ice, st, p)
+        dt = time.perf_counter() - t0
         if i >= args.warmup:
-            vals.append(c)
-    v = statistics.mean(c["value"] for c in vals)
+            vals.append((na / full["krylov_its"]) / dt)
+    v = statistics.mean(vals)
+    sample = (f"first {args.ref_sample_picard} Picard iterations of the solve per step, scaled by the "
+              f"{full['krylov_its']} Krylov iterations of a full solve measured in this run "
+              f"({full['picard_its']} Picard iterations, {full['seconds']:.1f} s = "
+              f"{1.0 / full['seconds']:.4f} solves/s)")
     line = {"metric": METRIC, "value": round(v, 6), "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(1000.0 / v, 1), "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic MISMIP+-shaped channel from formulas (no files)",
             "config": {"workload": "DIVA channel 640x80 km, cold start, Schoof2005, Picard 1e-4, BiCGStab/Jacobi",
                        "nV": mesh.nV, "nTri": mesh.nTri, "nz": mesh.nz},
             "impl": "reference",
-            "cpu_baseline": {"value": round(v, 6), "unit": UNIT, "cores": vals[0]["cores"], "kind": "port",
-                             "sample": vals[0]["sample"]},
+            "cpu_baseline": {"value": round(v, 6), "unit": UNIT, "cores": full["cores"], "kind": "port",
+                             "sample": sample},
+            "full_solve": {"value": round(1.0 / full["seconds"], 6), "unit": UNIT, "seconds": round(full["seconds"], 2),
+                           "picard_its": full["picard_its"], "krylov_its": full["krylov_its"]},
             "e2e": {"value": round(v, 6), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "note": "the reference is Fortran with PETSc and has no compiler or PETSc here; this arm times the "
                     "project's C restatement of its algorithm"}
@@ -963,8 +1076,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
-    ap.add_argument("--full-krylov-its", type=int, default=44600,
-                    help="Krylov iterations of one full FP64 solve (the reference arm's scale)")
+    ap.add_argument("--ref-tols", type=float, nargs="+", default=[1e-10, 1e-9, 1e-8, 1e-7, 1e-6],
+                    help="Picard tolerances tried, tightest first, for the FP64 reference solution")
+    ap.add_argument("--ref-sample-picard", type=int, default=4,
+                    help="Picard iterations per timed step of the reference arm")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--mixed-steps", type=int, default=1,
                     help="solves of the FP32+refinement path measured beside the headline")

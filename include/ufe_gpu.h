@@ -83,11 +83,19 @@ enum ufe_sliding_law {      /* choice_sliding_law (sliding_laws.f90:25-81) */
   UFE_SLIDING_COULOMB    = 2,
   UFE_SLIDING_BUDD       = 3,
   UFE_SLIDING_TSAI2015   = 4,
-  UFE_SLIDING_SCHOOF2005 = 5
+  UFE_SLIDING_SCHOOF2005 = 5,
+  UFE_SLIDING_ZOET_IVERSON = 6,             /* 'Zoet-Iverson' (:353-409), till_yield_stress given  */
+  UFE_SLIDING_IDEALISED_SSA_ICESTREAM = 7   /* 'idealised' with choice_idealised_sliding_law =
+                                               'SSA_icestream' (:411-485): the till yield stress of
+                                               Schoof's (2006) ice stream from the vertex y coordinate */
 };
 enum ufe_bc {               /* BC_{u,v}_{west,east,south,north} (solve_linearised_SSA_DIVA.f90:481-641) */
   UFE_BC_INFINITE = 0,
-  UFE_BC_ZERO     = 1
+  UFE_BC_ZERO     = 1,
+  UFE_BC_INFINITE_SSA_ICESTREAM = 2  /* 'infinite_SSA_icestream' (:562-578), u only: the border value
+                                        is the relaxed previous velocity at the same y, 1/3 or 2/3
+                                        across the domain (find_ti_copy_SSA_icestream_infinite,
+                                        src/UPSY/mesh/mesh_utilities.f90:2681-2729)                */
 };
 enum ufe_precision {
   UFE_PREC_FP64       = 0,  /* FP64 everywhere                                              */
@@ -101,6 +109,16 @@ enum ufe_precision {
                                Where the persistent Krylov kernel is not used (UFE_NO_PERSIST,
                                UFE_NO_SELL, no room for its shared-memory patches) this mode
                                runs as UFE_PREC_FP64                                          */
+};
+enum ufe_rheology {         /* choice_ice_rheology_Glen */
+  UFE_RHEOLOGY_INPUT         = 0, /* ice->A_flow is the flow factor, enhancement included (no reference
+                                     counterpart: the caller ran calc_ice_rheology_Glen itself)          */
+  UFE_RHEOLOGY_UNIFORM       = 1, /* 'uniform': uniform_Glens_flow_factor, then the enhancement factors    */
+  UFE_RHEOLOGY_HUYBRECHTS1992 = 2 /* 'Huybrechts1992': Arrhenius A(Ti), then the enhancement factors       */
+};
+enum ufe_enhancement {      /* choice_enhancement_factor_transition */
+  UFE_ENH_SEPARATE = 0,     /* 'separate': m_enh_sheet on grounded, m_enh_shelf on floating vertices    */
+  UFE_ENH_INTERP   = 1      /* 'interp': by grounded fraction where Hi > 0 and Hib < SL                 */
 };
 enum ufe_initial_guess {
   UFE_X0_ZERO    = 0,       /* every Krylov solve starts from x = 0, as PETSc does by default  */
@@ -135,6 +153,27 @@ typedef struct {
   int32_t precision;                      /* enum ufe_precision, default UFE_PREC_FP64       */
   double  krylov_inner_rtol;              /* FP32 inner-solve reduction per refinement step, default 1e-2;
                                              the linear solve finishes in FP64 if the FP32 steps fail */
+  double  krylov_forcing;                 /* inexact Picard iteration: a linear solve also stops once its
+                                             residual is below krylov_forcing x its initial residual (the
+                                             residual of the current Picard iterate), so early Picard
+                                             iterations, far from the fixed point, are not solved to full
+                                             accuracy.  0 (default) = the fixed tolerance only, as the
+                                             reference's PETSc call; otherwise in (0, 1)                  */
+  /* calc_ice_rheology_Glen (constitutive_equation.f90:84-163), model_configuration.f90:594-601 */
+  int32_t choice_ice_rheology_Glen;       /* enum ufe_rheology, default UFE_RHEOLOGY_INPUT                  */
+  int32_t choice_enhancement_factor_transition; /* enum ufe_enhancement, default UFE_ENH_SEPARATE          */
+  double  uniform_Glens_flow_factor;      /* :596, default 1e-16 [Pa^-3 yr^-1]                             */
+  double  m_enh_sheet;                    /* :600, default 1                                                */
+  double  m_enh_shelf;                    /* :601, default 1                                                */
+  double  slid_ZI_p;                      /* :336, default 5 (Zoet-Iverson velocity exponent)               */
+  double  slid_ZI_ut;                     /* :337, default 200 [m yr^-1] (Zoet-Iverson transition velocity) */
+  /* Schoof (2006) ice stream (refgeo_idealised_SSA_icestream_*, :190-193) read by the idealised
+     sliding law; its flow factor is uniform_Glens_flow_factor and Glens_flow_law_exponent must be 3.
+     Defaults: the reference's suggested values, as its SSA_icestream test sets them                   */
+  double  SSA_icestream_Hi;               /* [m], 2000                                                      */
+  double  SSA_icestream_dhdx;             /* surface slope, -0.0003                                         */
+  double  SSA_icestream_L;                /* [m] ice-stream width, 150e3                                    */
+  double  SSA_icestream_m;                /* margin exponent, 1                                             */
   int32_t reserved[8];
 } ufe_solver_params;
 
@@ -151,6 +190,13 @@ typedef struct {
   const double  *alpha_sq;            /* nV       Tsai/Schoof Coulomb coefficient (or NULL)  */
   const double  *effective_pressure;  /* nV       [Pa] (Tsai/Schoof; or NULL)                */
   const double  *till_yield_stress;   /* nV       [Pa] (Coulomb/Budd, already extended; or NULL) */
+  /* read by calc_ice_rheology_Glen when choice_ice_rheology_Glen is not UFE_RHEOLOGY_INPUT (then
+   * A_flow may be NULL); NULL where the chosen options do not read them */
+  const double  *Ti;                  /* nV x nz  ice temperature [K] ('Huybrechts1992')             */
+  const int32_t *mask_floating_ice;   /* nV       0/1 (enhancement factors)                          */
+  const double  *fraction_gr;         /* nV       grounded fraction on vertices ('interp')           */
+  const double  *Hib;                 /* nV       ice base elevation [m] ('interp')                  */
+  const double  *SL;                  /* nV       sea level [m] ('interp')                           */
 } ufe_ice_state;
 
 /* Prescribed-velocity boundary condition (solve_SSA optional arguments); all NULL = none. */
@@ -342,8 +388,10 @@ int32_t ufe_thermo_step(ufe_ctx *ctx, const ufe_thermo_params *p, int32_t nV, in
  * (thermodynamics_3D_heat_equation.f90:33).  The prelude runs on the GPU from these: the zeta
  * gradients of calc_zeta_gradients (zeta_gradients.f90:19, vertex terms), Cp, K and T_pmp
  * (thermodynamics_utilities.f90:130-229), the upwind advection terms of
- * calc_upwind_heat_flux_derivatives (:339-434) and the annual-mean surface temperature.
- * Strain and frictional heating are inputs (calc_strain_heating / calc_frictional_heating). */
+ * calc_upwind_heat_flux_derivatives (:339-434), the annual-mean surface temperature, and the
+ * two heating terms: calc_strain_heating (:24-78) from A_flow and the 3-D strain rates when
+ * internal_heating is NULL, calc_frictional_heating (:80-128) from the basal friction coefficient
+ * and basal speed when frictional_heating is NULL (a caller that has them can pass them instead). */
 typedef struct {
   const double  *Ti;                     /* nV x nz  [K]                                            */
   const double  *Hi, *Hi_eff, *Hs;       /* nV [m]                                                  */
@@ -360,6 +408,21 @@ typedef struct {
   const double  *SMB;                    /* nV [m yr^-1]                                            */
   const int32_t *mask;                   /* nV enum ufe_column_mask                                 */
   const double  *fraction_gr;            /* nV (UFE_GLBC_SUBGRID only; may be NULL else)            */
+  /* calc_strain_heating inputs (read when internal_heating is NULL): Glen's flow factor and the
+     3-D strain rates of ice%du_dx_3D ... ice%dw_dz_3D, nV x nz each [Pa^-n yr^-1], [yr^-1]        */
+  const double  *A_flow;
+  const double  *du_dx_3D, *du_dy_3D, *du_dz_3D;
+  const double  *dv_dx_3D, *dv_dy_3D, *dv_dz_3D;
+  const double  *dw_dx_3D, *dw_dy_3D, *dw_dz_3D;
+  /* calc_frictional_heating inputs (read when frictional_heating is NULL): nV each; grounded
+     vertices are those with mask UFE_COL_GROUNDED or UFE_COL_GL_GR                                */
+  const double  *basal_friction_coefficient;   /* [Pa yr m^-1]                                     */
+  const double  *uabs_base;                    /* [m yr^-1]                                        */
+  /* configuration scalars of the two heating terms */
+  int32_t        no_sliding;             /* choice_sliding_law is 'no_sliding': no frictional heating
+                                            (calc_frictional_heating, :91-95)                        */
+  int32_t        pad2;
+  double         Glens_flow_law_exponent; /* calc_strain_heating's n (0 is taken as the default 3)   */
 } ufe_heat_fields;
 
 /* solve_3D_heat_equation on the uploaded mesh (operators built or set; the mesh's nz and zeta):
@@ -474,12 +537,18 @@ int32_t ufe_gnn_predict_velocity(ufe_gnn *g, ufe_ctx *mesh_ctx, int32_t use_prev
  *
  * The matrix (d_ptr m+1, d_ind/d_val nnz, `index_base` 0 or 1), right-hand side and solution are
  * the caller's DEVICE buffers; d_xx holds the initial guess on entry and the solution on exit.
- * Work vectors and scalars live in one fixed device array of the library (about 9.1 MiB per GPU,
- * reserved while the library is loaded): no cudaMalloc or cudaFree happens in the call.  Systems
- * with more than 131,072 unknowns are rejected with UFE_ERR_CAPACITY.  Work runs on `cuda_stream`
- * (NULL: the legacy default stream) and the call returns after it finishes.  All calls on a device
- * share the array: calls that overlap on the GPU race.  The first call on a device resolves the
- * array's address and should come before any stream capture begins.  No context is needed. */
+ * Work vectors and scalars live in one fixed device array of the library (about 9.1 MiB per GPU):
+ * no cudaMalloc or cudaFree happens in the call.  Under CUDA's default lazy module loading the
+ * array is reserved on a device by the first call there (with CUDA_MODULE_LOADING=EAGER, when the
+ * CUDA context starts) and held until the process exits; later calls take no device memory.
+ * Systems with more than 131,072 unknowns are rejected with UFE_ERR_CAPACITY.  The matrix is
+ * checked on the device before use (ptr[0] = base, ptr[m] = nnz + base, ptr non-decreasing, every
+ * column inside the matrix): a malformed one returns UFE_ERR_INVALID.  Work runs on `cuda_stream`
+ * (NULL: the legacy default stream), which must belong to the current device, and the call
+ * returns after it finishes.  On entry the call clears any CUDA error left pending by earlier
+ * work.  All calls on a device share the array: calls that overlap on the GPU race.  The first
+ * call on a device resolves the array's address and should come before any stream capture begins.
+ * No context is needed. */
 int32_t ufe_solve_csr_noalloc(int32_t m, int64_t nnz, const int32_t *d_ptr, const int32_t *d_ind,
                               const double *d_val, int32_t index_base, const double *d_bb, double *d_xx,
                               double rtol, double abstol, int32_t max_it, int32_t *n_Axb_its,

@@ -25,6 +25,7 @@
 /* src/UPSY/basic/parameters.f90:20-27 */
 #define ICE_DENSITY 910.0
 #define GRAV 9.81
+#define R_GAS 8.314   /* parameters.f90:27 */
 /* src/UPSY/basic/math_utilities/shape_functions.f90:13 */
 #define SHAPE_Q 1.5
 
@@ -546,12 +547,43 @@ static int bc_choice(const ufe_solver_params *p, int TriBI, int uv) {
   }
 }
 
+/* find_ti_copy_SSA_icestream_infinite (src/UPSY/mesh/mesh_utilities.f90:2681-2729) for triangle
+ * ti (1-based): the point at the triangle's y, one third (x < 0) or two thirds across the domain;
+ * the vertex whose Voronoi cell contains it (find_containing_vertex, :1368-1416: a greedy walk over
+ * vertex neighbours, which on a Delaunay mesh ends at the nearest vertex -- taken here by a scan);
+ * that vertex's triangles with weights 1/dist^2, normalised by their sum.  Returns the count. */
+static int icestream_copy(const ufe_mesh_desc *m, int ti, int32_t *tj_out, double *w_out) {
+  const int nV = m->nV, nTri = m->nTri;
+  double xmin = m->V[0], xmax = m->V[0];
+  for (int v = 1; v < nV; ++v) { if (m->V[v] < xmin) xmin = m->V[v]; if (m->V[v] > xmax) xmax = m->V[v]; }
+  const double gx = m->TriGC[ti - 1], gy = m->TriGC[nTri + ti - 1];
+  const double px = (gx < 0.0) ? xmin + (xmax - xmin) * 1.0 / 3.0 : xmin + (xmax - xmin) * 2.0 / 3.0;
+  const double py = gy;
+  int vi = 0;
+  double best = 0.0;
+  for (int v = 0; v < nV; ++v) {
+    const double dx = m->V[v] - px, dy = m->V[nV + v] - py, d = dx * dx + dy * dy;
+    if (v == 0 || d < best) { best = d; vi = v; }
+  }
+  const int n = m->niTri[vi];
+  double sum = 0.0;
+  for (int iti = 0; iti < n; ++iti) {
+    const int tj = m->iTri[(int64_t)iti * nV + vi];
+    const double dist = norm2_2(px - m->TriGC[tj - 1], py - m->TriGC[nTri + tj - 1]);
+    tj_out[iti] = tj;
+    w_out[iti] = 1.0 / (dist * dist);
+  }
+  for (int iti = 0; iti < n; ++iti) sum = sum + w_out[iti];
+  for (int iti = 0; iti < n; ++iti) w_out[iti] = w_out[iti] / sum;
+  return n;
+}
+
 int32_t orc_assemble_linearised(const ufe_mesh_desc *m, const orc_csr *ops, const ufe_solver_params *p,
                                 const double *N_b, const double *dN_dx_b, const double *dN_dy_b,
                                 const double *beta_b, const double *tau_dx_b, const double *tau_dy_b,
                                 const double *u_prev, const double *v_prev,
                                 const ufe_bc_prescribed *bc, orc_csr *A, double *bb) {
-  (void)u_prev; (void)v_prev;
+  (void)v_prev;
   const int nTri = m->nTri;
   const orc_csr *Mx = &ops[UFE_OP_M2_DDX_B_B], *My = &ops[UFE_OP_M2_DDY_B_B];
   const orc_csr *Mxx = &ops[UFE_OP_M2_D2DX2_B_B], *Mxy = &ops[UFE_OP_M2_D2DXDY_B_B];
@@ -579,6 +611,17 @@ int32_t orc_assemble_linearised(const ufe_mesh_desc *m, const orc_csr *ops, cons
       } else if (choice == UFE_BC_ZERO) {
         csr_add(A, row, row, 1.0);
         bb[row - 1] = 0.0;
+      } else if (choice == UFE_BC_INFINITE_SSA_ICESTREAM && uv == 1) {
+        /* solve_linearised_SSA_DIVA.f90:562-578 */
+        int32_t tjs[64];
+        double ws[64];
+        if (m->nC_mem > 64) return UFE_ERR_CAPACITY;
+        const int n = icestream_copy(m, ti, tjs, ws);
+        csr_add(A, row, row, 1.0);
+        double u_fixed = 0.0;
+        for (int k = 0; k < n; ++k) u_fixed = u_fixed + ws[k] * u_prev[tjs[k] - 1];
+        u_fixed = (p->visc_it_relax * u_fixed) + ((1.0 - p->visc_it_relax) * u_prev[ti - 1]);
+        bb[row - 1] = u_fixed;
       } else {
         return UFE_ERR_INVALID;
       }
@@ -781,6 +824,13 @@ static double sliding_beta(const ufe_solver_params *p, const ufe_ice_state *ice,
               pow(pow(b, m) * uabs + pow(aN, m), 1.0 / m)) * pow(uabs, -1.0);
       break;
     }
+    case UFE_SLIDING_ZOET_IVERSON:   /* calc_sliding_law_ZoetIverson, :399-400 */
+      beta = ice->till_yield_stress[vi0] * (pow(uabs, 1.0 / p->slid_ZI_p - 1.0)) *
+             (pow(uabs + p->slid_ZI_ut, -1.0 / p->slid_ZI_p));
+      break;
+    case UFE_SLIDING_IDEALISED_SSA_ICESTREAM:   /* :477; the yield stress from schoof_yield_stress */
+      beta = ice->till_yield_stress[vi0] / uabs;
+      break;
     default: beta = 0.0;
   }
   return fmin(p->slid_beta_max, beta);
@@ -859,6 +909,71 @@ static int32_t picard_control(double L2, double L2_prev, int *nit_diverg, double
   return UFE_OK;
 }
 
+/* calc_ice_rheology_Glen (constitutive_equation.f90:84-163): A per vertex and layer, uniform or
+ * the Arrhenius relation of Huybrechts (1992), then the enhancement factors ('separate' or
+ * 'interp').  Called once per solve: the reference recomputes the same field every Picard
+ * iteration. */
+static void flow_factor(const ufe_mesh_desc *m, const ufe_solver_params *p, const ufe_ice_state *ice, double *A) {
+  const int nV = m->nV, nz = m->nz;
+  const double T_switch = 263.15, A_low_temp = 1.14E-05, A_high_temp = 5.47E+10;
+  const double Q_low_temp = 6.0E+04, Q_high_temp = 13.9E+04;
+  for (int vi = 0; vi < nV; ++vi)
+    for (int k = 0; k < nz; ++k) {
+      const int64_t ix = (int64_t)k * nV + vi;
+      if (p->choice_ice_rheology_Glen == UFE_RHEOLOGY_UNIFORM) {
+        A[ix] = p->uniform_Glens_flow_factor;
+      } else if (ice->Ti[ix] < T_switch) {
+        A[ix] = A_low_temp * exp(-Q_low_temp / (R_GAS * ice->Ti[ix]));
+      } else {
+        A[ix] = A_high_temp * exp(-Q_high_temp / (R_GAS * ice->Ti[ix]));
+      }
+    }
+  for (int vi = 0; vi < nV; ++vi) {
+    const int gr = ice->mask_grounded_ice[vi] != 0;
+    const int fl = ice->mask_floating_ice && ice->mask_floating_ice[vi] != 0;
+    double f = 1.0;
+    int apply = 0;
+    if (p->choice_enhancement_factor_transition == UFE_ENH_INTERP && ice->Hi[vi] > 0.0 && ice->Hib[vi] < ice->SL[vi]) {
+      f = ice->fraction_gr[vi] * p->m_enh_sheet + (1.0 - ice->fraction_gr[vi]) * p->m_enh_shelf;
+      apply = 1;
+    } else if (gr) {
+      f = p->m_enh_sheet; apply = 1;
+    } else if (fl) {
+      f = p->m_enh_shelf; apply = 1;
+    }
+    if (apply)
+      for (int k = 0; k < nz; ++k) A[(int64_t)k * nV + vi] = A[(int64_t)k * nV + vi] * f;
+  }
+}
+
+/* The till yield stress of Schoof's (2006) ice stream at every vertex (Schoof2006_icestream,
+ * src/UPSY/basic/analytical_solutions/Schoof_SSA_solution.f90:15-64, as
+ * calc_sliding_law_idealised_SSA_icestream calls it, sliding_laws.f90:469-473). */
+static void schoof_yield_stress(const ufe_mesh_desc *m, const ufe_solver_params *p, double *tys) {
+  const double f = -ICE_DENSITY * GRAV * p->SSA_icestream_Hi * p->SSA_icestream_dhdx;
+  for (int vi = 0; vi < m->nV; ++vi) {
+    const double y = m->V[m->nV + vi];
+    tys[vi] = f * pow(fabs(y / p->SSA_icestream_L), p->SSA_icestream_m);
+  }
+}
+
+/* The ice state a solve reads: the flow factor of calc_ice_rheology_Glen and, for the idealised
+ * SSA_icestream law, Schoof's yield stress in place of till_yield_stress.  *owned receives the
+ * allocation to free. */
+static const ufe_ice_state *solve_ice_state(const ufe_mesh_desc *m, const ufe_solver_params *p,
+                                            const ufe_ice_state *ice, ufe_ice_state *eff, double **owned) {
+  *eff = *ice;
+  *owned = NULL;
+  const int rheo = p->choice_ice_rheology_Glen != UFE_RHEOLOGY_INPUT;
+  const int ideal = p->choice_sliding_law == UFE_SLIDING_IDEALISED_SSA_ICESTREAM;
+  if (!rheo && !ideal) return ice;
+  double *buf = (double *)malloc(sizeof(double) * ((size_t)m->nV * m->nz + (size_t)m->nV));
+  *owned = buf;
+  if (rheo) { flow_factor(m, p, ice, buf); eff->A_flow = buf; }
+  if (ideal) { schoof_yield_stress(m, p, buf + (size_t)m->nV * m->nz); eff->till_yield_stress = buf + (size_t)m->nV * m->nz; }
+  return eff;
+}
+
 /* solve_SSA (SSA_main.f90:87-242) with calc_driving_stress (SSA_DIVA_utilities.f90:21-57),
  * calc_horizontal_strain_rates (:59-82), calc_effective_viscosity (SSA_main.f90:339-392),
  * calc_vertically_averaged_flow_parameter (:312-337) and
@@ -875,6 +990,9 @@ int32_t orc_solve_ssa(const ufe_mesh_desc *m, const orc_csr *ops, const ufe_solv
     memset(v_b, 0, sizeof(double) * nTri);
     return UFE_OK;
   }
+  ufe_ice_state ice_eff;
+  double *ice_owned;
+  ice = solve_ice_state(m, p, ice, &ice_eff, &ice_owned);
   double *w = (double *)calloc((size_t)(16 * nV + 16 * nTri), sizeof(double));
   double *Hi_b = w, *dHs_dx = Hi_b + nTri, *dHs_dy = dHs_dx + nTri, *tdx = dHs_dy + nTri, *tdy = tdx + nTri;
   double *N_b = tdy + nTri, *dN_dx_b = N_b + nTri, *dN_dy_b = dN_dx_b + nTri, *beta_b = dN_dy_b + nTri;
@@ -948,6 +1066,7 @@ int32_t orc_solve_ssa(const ufe_mesh_desc *m, const orc_csr *ops, const ufe_solv
   st->visc_it_relax_applied = relax_applied;
   st->status = status;
   free(w);
+  free(ice_owned);
   return status;
 }
 
@@ -971,6 +1090,9 @@ int32_t orc_solve_diva(const ufe_mesh_desc *m, const orc_csr *ops, const ufe_sol
     if (ds->v_3D_b) memset(ds->v_3D_b, 0, sizeof(double) * nTri * nz);
     return UFE_OK;
   }
+  ufe_ice_state ice_eff;
+  double *ice_owned;
+  ice = solve_ice_state(m, p, ice, &ice_eff, &ice_owned);
   int64_t n2 = 20 * (int64_t)nV + 20 * (int64_t)nTri + 8 * (int64_t)nz * (nV + nTri) + 4 * nz;
   double *w = (double *)calloc((size_t)n2, sizeof(double));
   double *Hi_b = w, *dHs_dx = Hi_b + nTri, *dHs_dy = dHs_dx + nTri, *tdx = dHs_dy + nTri, *tdy = tdx + nTri;
@@ -1114,6 +1236,7 @@ int32_t orc_solve_diva(const ufe_mesh_desc *m, const orc_csr *ops, const ufe_sol
   st->visc_it_relax_applied = relax_applied;
   st->status = status;
   free(w);
+  free(ice_owned);
   return status;
 }
 

@@ -381,11 +381,37 @@ int32_t orc_ops_solve_3D_heat_equation(orc_ops *h, const ufe_thermo_params *p, c
   }
   (void)nCm;
 
+  /* calc_strain_heating (thermodynamics_utilities.f90:24-78) when no internal heating is given */
+  double *phi_own = NULL;
+  const double *phi = f->internal_heating;
+  if (!phi) {
+    const double n = f->Glens_flow_law_exponent > 0.0 ? f->Glens_flow_law_exponent : 3.0;
+    phi_own = malloc(sizeof(double) * nl);
+    for (int64_t vi = 0; vi < nV; ++vi)
+      for (int64_t k = 0; k < nz; ++k) {
+        const int64_t o = k * nV + vi;
+        if (f->Hi[vi] < 0.1) { phi_own[o] = 0.0; continue; }
+        const double D = sqrt(0.5 * (f->du_dx_3D[o] * f->du_dx_3D[o] + f->dv_dy_3D[o] * f->dv_dy_3D[o] +
+                                     f->dw_dz_3D[o] * f->dw_dz_3D[o] +
+                                     0.5 * ((f->du_dy_3D[o] + f->dv_dx_3D[o]) * (f->du_dy_3D[o] + f->dv_dx_3D[o])) +
+                                     0.5 * ((f->du_dz_3D[o] + f->dw_dx_3D[o]) * (f->du_dz_3D[o] + f->dw_dx_3D[o])) +
+                                     0.5 * ((f->dv_dz_3D[o] + f->dw_dy_3D[o]) * (f->dv_dz_3D[o] + f->dw_dy_3D[o]))));
+        phi_own[o] = 2.0 * pow(f->A_flow[o], -1.0 / n) * pow(D, 1.0 / n + 1.0);
+      }
+    phi = phi_own;
+  }
   for (int64_t vi = 0; vi < nV; ++vi) {
     double sum = 0.0;
     for (int32_t mo = 0; mo < f->n_months; ++mo) sum = sum + f->T2m[(int64_t)mo * nV + vi];
     Ts[vi] = sum / (double)f->n_months;
-    Q[vi] = f->frictional_heating[vi] + f->geothermal_heat_flux[vi];
+    /* calc_frictional_heating (:80-128) when no frictional heating is given */
+    double fric;
+    if (f->frictional_heating) fric = f->frictional_heating[vi];
+    else if (f->no_sliding) fric = 0.0;
+    else if (f->mask[vi] == UFE_COL_GROUNDED || f->mask[vi] == UFE_COL_GL_GR)
+      fric = f->basal_friction_coefficient[vi] * f->uabs_base[vi];
+    else fric = 0.0;
+    Q[vi] = fric + f->geothermal_heat_flux[vi];
   }
 
   if (rc == UFE_OK) {
@@ -393,13 +419,13 @@ int32_t orc_ops_solve_3D_heat_equation(orc_ops *h, const ufe_thermo_params *p, c
     c.Ti = f->Ti; c.u_3D = f->u_3D; c.v_3D = f->v_3D; c.w_3D = f->w_3D;
     c.u_times_dTdxp_upwind = udx; c.v_times_dTdyp_upwind = vdy;
     c.dzeta_dx = dzx; c.dzeta_dy = dzy; c.dzeta_dz = dzz; c.dzeta_dt = dzt;
-    c.internal_heating = f->internal_heating; c.Hi_eff = f->Hi_eff; c.T_surf_annual = Ts;
+    c.internal_heating = phi; c.Hi_eff = f->Hi_eff; c.T_surf_annual = Ts;
     c.Q_base_grnd = Q; c.mask = f->mask; c.fraction_gr = f->fraction_gr;
     c.geothermal_heat_flux = f->geothermal_heat_flux; c.SMB = f->SMB;
     rc = orc_thermo_step(p, (int32_t)nV, (int32_t)nz, m->zeta, &c, Ti_next, n_unstable, is_unstable);
   }
   free(dHi_dx); free(dHi_dy); free(dHs_dx); free(dHs_dy);
   free(dzx); free(dzy); free(dzz); free(dzt); free(dTdx_b); free(dTdy_b);
-  free(udx); free(vdy); free(Ts); free(Q);
+  free(udx); free(vdy); free(Ts); free(Q); free(phi_own);
   return rc;
 }

@@ -298,3 +298,60 @@ def test_no_grounded_ice_zero_velocity(pkg, dome, gpu_golden_ops):
     ssa = {"u_b": np.ones(mesh.nTri), "v_b": np.ones(mesh.nTri)}
     nv, na, st = gpu_golden_ops.solve_SSA(z, ssa, params)
     assert nv == 0 and not ssa["u_b"].any()
+
+
+# ---- the benchmark configurations at full size ------------------------------------------------
+@pytest.fixture(scope="module")
+def dome_full(pkg, oracle_mod):
+    """Config 0: the ~8,000-vertex dome, with the oracle's operators and the GPU's."""
+    mesh, ice, params = pkg.geometry.dome_case(seed=0)
+    return mesh, ice, params, oracle_mod.Oracle(mesh)
+
+
+def test_dome_stiffness_structure_bitexact_gpu_operators(pkg, dome_full, gpu_lib):
+    """The stiffness matrix of config 0 assembled from GPU-built operators: integer CSR structure
+    identical to the oracle's, values within the operators' 1e-11 agreement."""
+    mesh, ice, params, orc = dome_full
+    rng = np.random.default_rng(11)
+    nT = mesh.nTri
+    args = (1e12 * (1 + rng.random(nT)), 1e7 * rng.normal(size=nT), 1e7 * rng.normal(size=nT),
+            1e3 * rng.random(nT), 1e4 * rng.normal(size=nT), 1e4 * rng.normal(size=nT))
+    with pkg.VelocitySolver(mesh) as g:
+        Ag, bg = g.assemble_linearised(params, *args)
+    Ao, bo = orc.assemble_linearised(params, *args)
+    assert np.array_equal(Ag.ptr, Ao.ptr) and np.array_equal(Ag.ind, Ao.ind)
+    assert np.abs(Ag.val - Ao.val).max() <= 1e-9 * np.abs(Ao.val).max()
+    assert np.array_equal(bg, bo)
+
+
+def test_dome_ssa_matches_oracle_gpu_operators(pkg, dome_full, gpu_lib):
+    """Config 0 solved on the GPU with its own operators against the oracle: the same Picard
+    iteration count and velocities within 1e-8 (Krylov to 1e-12)."""
+    mesh, ice, params, orc = dome_full
+    p = pkg.abi.default_params(**{k: getattr(params, k) for k, _ in params._fields_ if k != "reserved"})
+    p.stress_balance_PETSc_rtol = 1e-12
+    p.stress_balance_PETSc_abstol = 0.0
+    a, b = pkg.new_ssa_state(mesh.nTri), pkg.new_ssa_state(mesh.nTri)
+    with pkg.VelocitySolver(mesh) as g:
+        nvg, nag, sg = g.solve_SSA(ice, a, p)
+    nvo, nao, so = orc.solve_SSA(ice, b, p)
+    assert sg["status"] == so["status"] == 0 and nvg == nvo
+    assert rel_l2(np.r_[a["u_b"], a["v_b"]], np.r_[b["u_b"], b["v_b"]]) < 1e-8
+
+
+@pytest.mark.parametrize("sliding", ["Schoof2005", "Weertman"])
+def test_diva_matches_oracle_gpu_operators(pkg, oracle_mod, gpu_lib, sliding):
+    """DIVA with the operators built on the GPU (the benchmark's setting), against the oracle with
+    its own operators: within 1e-8 in every output field, same Picard count."""
+    mesh, ice, params = pkg.geometry.small_channel(sliding=sliding)
+    params.stress_balance_PETSc_rtol = 1e-12
+    params.stress_balance_PETSc_abstol = 0.0
+    params.visc_it_nit = 12
+    orc = oracle_mod.Oracle(mesh)
+    a, b = pkg.new_diva_state(mesh.nTri, mesh.nz), pkg.new_diva_state(mesh.nTri, mesh.nz)
+    with pkg.VelocitySolver(mesh) as g:
+        nvg, _, sg = g.solve_DIVA(ice, a, params)
+    nvo, _, so = orc.solve_DIVA(ice, b, params)
+    assert nvg == nvo and sg["status"] == so["status"]
+    for k in ("u_vav_b", "v_vav_b", "u_base_b", "tau_bx_b", "eta_3D_b", "u_3D_b", "v_3D_b"):
+        assert rel_l2(a[k], b[k]) < 1e-8, k

@@ -1,0 +1,113 @@
+"""Schoof's (2006) analytic ice stream: the reference's SSA_icestream integrated test
+(automated_testing/integrated_tests/idealised/SSA_icestream/, analysed by analyse_integrated_test.m:
+RMSE of the surface velocity on the south-north transect against Schoof2006_icestream).  The
+reference's scoreboard records RMSE 400.42 m/yr at 32 km and 101.21 m/yr at 4 km
+(scoreboard_files/it_ideal_SSA_icestream_*.xml).  This pins the velocity solve -- Glen viscosity,
+the idealised sliding law, the 'infinite_SSA_icestream' border rows, assembly and the Picard
+control -- on an answer the reference itself holds, in the oracle (CPU) and on the GPU.  The meshes
+come from this package's generator, so the RMSE is comparable to the scoreboard, not identical."""
+import numpy as np
+import pytest
+
+from helpers import rel_l2
+
+
+def _rmse(pkg, mesh, u_a):
+    y, ut = pkg.geometry.transect_values(mesh, u_a)
+    return float(np.sqrt(np.nanmean((ut - pkg.geometry.schoof2006_u(y)) ** 2))), np.nanmax(ut)
+
+
+def test_schoof_solution_closed_form(pkg):
+    """u(0) = -2 f^3 L^4 / (B^3 H^3) * (sum of the four bracketed terms at y = 0), zero beyond W."""
+    f = 910.0 * 9.81 * 2000.0 * 0.0003
+    ua = -2.0 * f ** 3 * 150e3 ** 4 * 1e-18 / 2000.0 ** 3
+    u0 = ua * (0.25 * (0 - 16.0) - 3.0 / 10.0 * (0 - 32.0) + 3.0 / 24.0 * (0 - 64.0) - 1.0 / 56.0 * (0 - 128.0))
+    assert pkg.geometry.schoof2006_u(np.array([0.0]))[0] == pytest.approx(u0, rel=1e-12)
+    assert u0 == pytest.approx(2222.7, abs=0.1)
+    assert pkg.geometry.schoof2006_u(np.array([-300.01e3, 300.01e3, 350e3])).tolist() == [0.0, 0.0, 0.0]
+
+
+def test_oracle_icestream_32km_rmse(pkg, oracle_mod):
+    """The oracle on the 32 km run: converged within the reference's 5000 Picard iterations, RMSE
+    against Schoof's solution of the scoreboard's magnitude (400.42 m/yr)."""
+    mesh, ice, p = pkg.geometry.icestream_case(res=32e3)
+    orc = oracle_mod.Oracle(mesh)
+    s = pkg.new_ssa_state(mesh.nTri)
+    nv, na, st = orc.solve_SSA(ice, s, p)
+    assert st["status"] == 0 and nv < 5000
+    rmse, umax = _rmse(pkg, mesh, orc.apply("MAP_B_A", s["u_b"]))
+    assert 250.0 < rmse < 650.0, rmse
+    assert 1000.0 < umax < 2400.0
+    assert np.all(np.abs(s["v_b"]) < 0.05 * np.abs(s["u_b"]).max())   # flow along x
+
+
+def test_oracle_idealised_law_is_coulomb_with_schoof_yield(pkg, oracle_mod):
+    """calc_sliding_law_idealised_SSA_icestream is beta = tau_yield(y)/|u| (sliding_laws.f90:469-477):
+    the same solve as the Coulomb law given Schoof's tau_yield as the till yield stress."""
+    mesh, ice, p = pkg.geometry.icestream_case(res=64e3)
+    p.visc_it_nit = 40
+    orc = oracle_mod.Oracle(mesh)
+    a, b = pkg.new_ssa_state(mesh.nTri), pkg.new_ssa_state(mesh.nTri)
+    orc.solve_SSA(ice, a, p)
+    f = 910.0 * 9.81 * 2000.0 * 0.0003
+    ice2 = dict(ice, till_yield_stress=np.ascontiguousarray(f * np.abs(mesh.V[:, 1] / 150e3)))
+    p2 = pkg.abi.default_params(**{k: getattr(p, k) for k, _ in p._fields_ if k != "reserved"})
+    p2.choice_sliding_law = pkg.abi.SLIDING["Coulomb"]
+    orc.solve_SSA(ice2, b, p2)
+    assert np.array_equal(a["u_b"], b["u_b"]) and np.array_equal(a["v_b"], b["v_b"])
+
+
+@pytest.mark.gpu
+def test_gpu_icestream_assembly_bitexact(pkg, oracle_mod, gpu_lib):
+    """The stiffness matrix and load vector with the 'infinite_SSA_icestream' border rows, exported
+    in the reference's CSR layout: identical to the oracle's, given the same previous velocity."""
+    mesh, ice, p = pkg.geometry.icestream_case(res=48e3)
+    orc = oracle_mod.Oracle(mesh)
+    rng = np.random.default_rng(3)
+    nT = mesh.nTri
+    N = 1e12 * (1 + rng.random(nT))
+    args = (N, 1e7 * rng.normal(size=nT), 1e7 * rng.normal(size=nT), 1e3 * rng.random(nT),
+            1e4 * rng.normal(size=nT), 1e4 * rng.normal(size=nT))
+    up, vp = 100 * rng.normal(size=nT), 10 * rng.normal(size=nT)
+    with pkg.VelocitySolver(mesh, operators=orc.operators()) as g:
+        Ag, bg = g.assemble_linearised(p, *args, up, vp)
+    Ao, bo = orc.assemble_linearised(p, *args, up, vp)
+    assert np.array_equal(Ag.ptr, Ao.ptr) and np.array_equal(Ag.ind, Ao.ind)
+    assert np.array_equal(Ag.val, Ao.val) and np.array_equal(bg, bo)
+    # west/east border u rows: diagonal one and a non-trivial copied value
+    border = np.where(np.isin(mesh.TriBI, [3, 4, 7, 8]))[0]
+    assert border.size and np.all(bo[2 * border] != 0.0)
+
+
+@pytest.mark.gpu
+def test_gpu_icestream_matches_oracle_32km(pkg, oracle_mod, gpu_lib):
+    """Whole SSA solve of the 32 km run, GPU-built operators, Krylov to 1e-12: the same Picard
+    iteration count as the oracle and velocities within 1e-8."""
+    mesh, ice, p = pkg.geometry.icestream_case(res=32e3)
+    p.stress_balance_PETSc_rtol = 1e-12
+    p.stress_balance_PETSc_abstol = 0.0
+    orc = oracle_mod.Oracle(mesh)
+    a, b = pkg.new_ssa_state(mesh.nTri), pkg.new_ssa_state(mesh.nTri)
+    with pkg.VelocitySolver(mesh) as g:
+        nvg, nag, stg = g.solve_SSA(ice, a, p)
+    nvo, nao, sto = orc.solve_SSA(ice, b, p)
+    assert stg["status"] == sto["status"] == 0
+    assert abs(nvg - nvo) <= 1, (nvg, nvo)
+    assert rel_l2(np.r_[a["u_b"], a["v_b"]], np.r_[b["u_b"], b["v_b"]]) < 1e-8
+
+
+@pytest.mark.gpu
+def test_gpu_icestream_rmse_falls_with_resolution(pkg, gpu_lib):
+    """The reference's four runs (32, 16, 8, 4 km) on the GPU with their own settings: the RMSE
+    against Schoof's solution falls with resolution, from the scoreboard's ~400 m/yr at 32 km to
+    ~100 m/yr at 4 km."""
+    rmses = []
+    for res in (32e3, 16e3, 8e3, 4e3):
+        mesh, ice, p = pkg.geometry.icestream_case(res=res)
+        with pkg.VelocitySolver(mesh) as g:
+            s = pkg.new_ssa_state(mesh.nTri)
+            nv, na, st = g.solve_SSA(ice, s, p)
+            assert st["status"] == 0 and nv < 5000
+            rmses.append(_rmse(pkg, mesh, g.apply("MAP_B_A", s["u_b"]))[0])
+    assert all(b < a for a, b in zip(rmses, rmses[1:])), rmses
+    assert 250.0 < rmses[0] < 650.0 and 40.0 < rmses[-1] < 200.0, rmses

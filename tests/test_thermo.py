@@ -231,3 +231,67 @@ def test_heat_resident_stepping_with_robin_columns(pkg, oracle_mod, gpu_lib):
         T_g = s.heat_download()
     assert n_g == n_o
     np.testing.assert_allclose(T_g, T, rtol=0, atol=1e-7)
+
+
+def _heating_inputs(mesh, fields, seed=5):
+    """Flow factor, 3-D strain rates and basal sliding fields for calc_strain_heating /
+    calc_frictional_heating, smooth in space and depth."""
+    rng = np.random.default_rng(seed)
+    x, y = mesh.V[:, 0] / 1e6, mesh.V[:, 1] / 1e6
+    z = mesh.zeta[None, :]
+    out = {"A_flow": np.asfortranarray(1e-16 * (1.0 + 0.5 * np.sin(3 * x)[:, None]) * (1.0 + z))}
+    for i, name in enumerate(("du_dx_3D", "du_dy_3D", "du_dz_3D", "dv_dx_3D", "dv_dy_3D", "dv_dz_3D",
+                              "dw_dx_3D", "dw_dy_3D", "dw_dz_3D")):
+        a, b = rng.normal(size=2)
+        scale = 1e-2 if name.endswith("dz_3D") else 1e-3
+        out[name] = np.asfortranarray(scale * (np.sin(a + 5 * x + 3 * y)[:, None] * (0.5 + z) + 0.2 * b))
+    out["basal_friction_coefficient"] = np.ascontiguousarray(1e3 * (1.5 + np.cos(4 * y)))
+    out["uabs_base"] = np.ascontiguousarray(50.0 * (1.0 + np.sin(2 * x) ** 2))
+    return out
+
+
+def _heating_given(pkg, mesh, fields, h):
+    """The two heating terms in numpy, the way calc_strain_heating and calc_frictional_heating form
+    them (thermodynamics_utilities.f90:24-128)."""
+    D = np.sqrt(0.5 * (h["du_dx_3D"] ** 2 + h["dv_dy_3D"] ** 2 + h["dw_dz_3D"] ** 2
+                       + 0.5 * (h["du_dy_3D"] + h["dv_dx_3D"]) ** 2 + 0.5 * (h["du_dz_3D"] + h["dw_dx_3D"]) ** 2
+                       + 0.5 * (h["dv_dz_3D"] + h["dw_dy_3D"]) ** 2))
+    phi = 2.0 * h["A_flow"] ** (-1.0 / 3.0) * D ** (1.0 / 3.0 + 1.0)
+    phi[fields["Hi"] < 0.1, :] = 0.0
+    grounded = np.isin(fields["mask"], [pkg.abi.COL_GROUNDED, pkg.abi.COL_GL_GR])
+    fric = np.where(grounded, h["basal_friction_coefficient"] * h["uabs_base"], 0.0)
+    return np.asfortranarray(phi), np.ascontiguousarray(fric)
+
+
+def test_oracle_heating_terms_equal_given_terms(pkg, oracle_mod):
+    """The oracle's strain and frictional heating, computed inside solve_3D_heat_equation, against
+    the same terms computed in numpy and passed in (the host libm's pow is the only difference)."""
+    mesh, fields, p = pkg.geometry.small_thermo(seed=4)
+    h = _heating_inputs(mesh, fields)
+    o = oracle_mod.Oracle(mesh)
+    computed = {k: v for k, v in fields.items() if k not in ("internal_heating", "frictional_heating")}
+    computed.update(h)
+    T_c, n_c, rc_c, _ = o.solve_3D_heat_equation(computed, p)
+    phi, fric = _heating_given(pkg, mesh, fields, h)
+    T_g, n_g, rc_g, _ = o.solve_3D_heat_equation(dict(fields, internal_heating=phi, frictional_heating=fric), p)
+    assert rc_c == rc_g == 0 and n_c == n_g
+    np.testing.assert_allclose(T_c, T_g, rtol=0, atol=1e-10)
+    # without sliding there is no frictional heating
+    T_ns, _, _, _ = o.solve_3D_heat_equation(dict(computed, no_sliding=1), p)
+    T_z, _, _, _ = o.solve_3D_heat_equation(dict(fields, internal_heating=phi, frictional_heating=0 * fric), p)
+    np.testing.assert_allclose(T_ns, T_z, rtol=0, atol=1e-10)
+
+
+@pytest.mark.gpu
+def test_heating_terms_on_gpu_match_oracle(pkg, oracle_mod, gpu_lib):
+    """calc_strain_heating and calc_frictional_heating inside ufe_solve_3D_heat_equation, against the
+    oracle doing the same (CUDA's pow against the host libm: below 1e-9 K)."""
+    mesh, fields, p, o, ops = _heat_setup(pkg, oracle_mod, seed=4)
+    h = _heating_inputs(mesh, fields)
+    computed = {k: v for k, v in fields.items() if k not in ("internal_heating", "frictional_heating")}
+    computed.update(h)
+    T_o, n_o, rc_o, _ = o.solve_3D_heat_equation(computed, p)
+    with pkg.VelocitySolver(mesh, operators=ops) as s:
+        T_g, n_g = s.solve_3D_heat_equation(computed, p)
+    assert rc_o == 0 and n_g == n_o
+    np.testing.assert_allclose(T_g, T_o, rtol=0, atol=1e-9)

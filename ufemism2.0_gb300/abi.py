@@ -29,10 +29,13 @@ OPERATORS = ["MAP_A_B", "DDX_A_B", "DDY_A_B", "MAP_B_A", "DDX_B_A", "DDY_B_A", "
              "M2_DDX_B_B", "M2_DDY_B_B", "M2_D2DX2_B_B", "M2_D2DXDY_B_B", "M2_D2DY2_B_B"]
 OP = {name: i for i, name in enumerate(OPERATORS)}
 
-SLIDING = {"no_sliding": 0, "Weertman": 1, "Coulomb": 2, "Budd": 3, "Tsai2015": 4, "Schoof2005": 5}
-BC = {"infinite": 0, "zero": 1}
+SLIDING = {"no_sliding": 0, "Weertman": 1, "Coulomb": 2, "Budd": 3, "Tsai2015": 4, "Schoof2005": 5,
+           "Zoet-Iverson": 6, "idealised_SSA_icestream": 7}
+BC = {"infinite": 0, "zero": 1, "infinite_SSA_icestream": 2}
 PREC_FP64, PREC_FP32_REFINE, PREC_FP32_PAIR = 0, 1, 2
 X0_ZERO, X0_CURRENT = 0, 1
+RHEOLOGY = {"input": 0, "uniform": 1, "Huybrechts1992": 2}
+ENHANCEMENT = {"separate": 0, "interp": 1}
 
 dptr = C.POINTER(C.c_double)
 iptr = C.POINTER(C.c_int32)
@@ -59,13 +62,20 @@ class SolverParams(C.Structure):
                 ("subgrid_friction_exponent_on_B_grid", C.c_double), ("slid_beta_max", C.c_double),
                 ("slid_delta_v", C.c_double),
                 ("krylov_max_it", C.c_int32), ("krylov_initial_guess", C.c_int32), ("precision", C.c_int32),
-                ("krylov_inner_rtol", C.c_double), ("reserved", C.c_int32 * 8)]
+                ("krylov_inner_rtol", C.c_double), ("krylov_forcing", C.c_double),
+                ("choice_ice_rheology_Glen", C.c_int32), ("choice_enhancement_factor_transition", C.c_int32),
+                ("uniform_Glens_flow_factor", C.c_double), ("m_enh_sheet", C.c_double), ("m_enh_shelf", C.c_double),
+                ("slid_ZI_p", C.c_double), ("slid_ZI_ut", C.c_double),
+                ("SSA_icestream_Hi", C.c_double), ("SSA_icestream_dhdx", C.c_double),
+                ("SSA_icestream_L", C.c_double), ("SSA_icestream_m", C.c_double),
+                ("reserved", C.c_int32 * 8)]
 
 
 class IceState(C.Structure):
     _fields_ = [("Hi", dptr), ("Hs", dptr), ("A_flow", dptr), ("fraction_gr_b", dptr),
                 ("mask_grounded_ice", iptr), ("beta_sq", dptr), ("alpha_sq", dptr),
-                ("effective_pressure", dptr), ("till_yield_stress", dptr)]
+                ("effective_pressure", dptr), ("till_yield_stress", dptr),
+                ("Ti", dptr), ("mask_floating_ice", iptr), ("fraction_gr", dptr), ("Hib", dptr), ("SL", dptr)]
 
 
 class BCPrescribed(C.Structure):
@@ -115,9 +125,24 @@ def default_params(**overrides) -> SolverParams:
     p.krylov_initial_guess = X0_CURRENT
     p.precision = PREC_FP64
     p.krylov_inner_rtol = 1e-2
+    p.krylov_forcing = 0.0
+    p.choice_ice_rheology_Glen = RHEOLOGY["input"]
+    p.choice_enhancement_factor_transition = ENHANCEMENT["separate"]
+    p.uniform_Glens_flow_factor = 1e-16
+    p.m_enh_sheet = 1.0
+    p.m_enh_shelf = 1.0
+    p.slid_ZI_p = 5.0
+    p.slid_ZI_ut = 200.0
+    p.SSA_icestream_Hi = 2000.0
+    p.SSA_icestream_dhdx = -0.0003
+    p.SSA_icestream_L = 150e3
+    p.SSA_icestream_m = 1.0
+    names = {"choice_sliding_law": SLIDING, "choice_ice_rheology_Glen": RHEOLOGY,
+             "choice_enhancement_factor_transition": ENHANCEMENT}
+    names.update({f"BC_{c}_{side}": BC for c in "uv" for side in ("west", "east", "south", "north")})
     for k, v in overrides.items():
-        if k == "choice_sliding_law" and isinstance(v, str):
-            v = SLIDING[v]
+        if k in names and isinstance(v, str):
+            v = names[k][v]
         setattr(p, k, v)
     return p
 
@@ -147,7 +172,10 @@ class HeatFields(C.Structure):
     _fields_ = [(n, dptr) for n in ("Ti", "Hi", "Hi_eff", "Hs", "dHi_dt", "dHs_dt", "u_vav", "v_vav", "u_3D",
                                     "v_3D", "w_3D", "u_3D_b", "v_3D_b", "internal_heating", "frictional_heating",
                                     "geothermal_heat_flux", "T2m")] + \
-              [("n_months", C.c_int32), ("pad", C.c_int32), ("SMB", dptr), ("mask", iptr), ("fraction_gr", dptr)]
+              [("n_months", C.c_int32), ("pad", C.c_int32), ("SMB", dptr), ("mask", iptr), ("fraction_gr", dptr)] + \
+              [(n, dptr) for n in ("A_flow", "du_dx_3D", "du_dy_3D", "du_dz_3D", "dv_dx_3D", "dv_dy_3D", "dv_dz_3D",
+                                    "dw_dx_3D", "dw_dy_3D", "dw_dz_3D", "basal_friction_coefficient", "uabs_base")] + \
+              [("no_sliding", C.c_int32), ("pad2", C.c_int32), ("Glens_flow_law_exponent", C.c_double)]
 
 
 def default_thermo_params(**overrides) -> ThermoParams:
@@ -193,7 +221,10 @@ def heat_fields(f: dict) -> tuple[HeatFields, list]:
     """HeatFields over a dict of the ufe_heat_fields fields (T2m as (nV, n_months))."""
     keep, vals = [], {}
     for name, typ in HeatFields._fields_:
-        if name in ("n_months", "pad"):
+        if name in ("n_months", "pad", "pad2"):
+            continue
+        if name in ("no_sliding", "Glens_flow_law_exponent"):
+            vals[name] = f.get(name, 0)
             continue
         a = f.get(name)
         if a is None:
@@ -205,6 +236,7 @@ def heat_fields(f: dict) -> tuple[HeatFields, list]:
     T2m = np.asarray(f["T2m"])
     vals["n_months"] = T2m.shape[1] if T2m.ndim == 2 else 1
     vals["pad"] = 0
+    vals["pad2"] = 0
     return HeatFields(**vals), keep
 
 
@@ -235,10 +267,15 @@ def mesh_desc(mesh) -> tuple[MeshDesc, list]:
 
 
 def ice_state(ice: dict) -> tuple[IceState, list]:
+    """An IceState over a dict of arrays.  A_flow may be absent when the solve computes the flow
+    factor (choice_ice_rheology_Glen 'uniform' or 'Huybrechts1992'); Ti, mask_floating_ice,
+    fraction_gr, Hib and SL are passed when present."""
     keep = [v for v in ice.values() if isinstance(v, np.ndarray)]
-    s = IceState(as_d(ice["Hi"]), as_d(ice["Hs"]), as_d(ice["A_flow"]), as_d(ice["fraction_gr_b"]),
+    s = IceState(as_d(ice["Hi"]), as_d(ice["Hs"]), as_d(ice.get("A_flow")), as_d(ice["fraction_gr_b"]),
                  as_i(ice["mask_grounded_ice"]), as_d(ice.get("beta_sq")), as_d(ice.get("alpha_sq")),
-                 as_d(ice.get("effective_pressure")), as_d(ice.get("till_yield_stress")))
+                 as_d(ice.get("effective_pressure")), as_d(ice.get("till_yield_stress")),
+                 as_d(ice.get("Ti")), as_i(ice.get("mask_floating_ice")), as_d(ice.get("fraction_gr")),
+                 as_d(ice.get("Hib")), as_d(ice.get("SL")))
     return s, keep
 
 

@@ -85,6 +85,19 @@ extern "C" void ufe_default_params(ufe_solver_params *p) {
   p->krylov_initial_guess = UFE_X0_CURRENT;
   p->precision = UFE_PREC_FP64;
   p->krylov_inner_rtol = 1e-2;
+  p->krylov_forcing = 0.0;
+  // model_configuration.f90:594-601
+  p->choice_ice_rheology_Glen = UFE_RHEOLOGY_INPUT;
+  p->choice_enhancement_factor_transition = UFE_ENH_SEPARATE;
+  p->uniform_Glens_flow_factor = 1e-16;
+  p->m_enh_sheet = 1.0;
+  p->m_enh_shelf = 1.0;
+  p->slid_ZI_p = 5.0;         // model_configuration.f90:336-337
+  p->slid_ZI_ut = 200.0;
+  p->SSA_icestream_Hi = 2000.0;   // the suggested values of :190-193
+  p->SSA_icestream_dhdx = -0.0003;
+  p->SSA_icestream_L = 150e3;
+  p->SSA_icestream_m = 1.0;
 }
 
 extern "C" int32_t ufe_ctx_create(int32_t device, ufe_ctx **out) {

@@ -69,7 +69,8 @@ struct PicardScalars {
   int32_t it, nit_diverg, active, status;
   int32_t n_refine;
   int32_t prev_total_its;
-  int32_t pad[2];
+  int32_t phase;       // inexact Picard (krylov_forcing > 0): 0 while forced, 1 once exact solves verify
+  int32_t pad;
   double hist[kHistMax * kHistCols];
 };
 

@@ -267,11 +267,13 @@ __device__ __forceinline__ Vec lane_reduce(Vec y) {
 
 // r = D^-1 (b - A x), r^ = r, p = v = 0; tests the initial residual (KSPConvergedDefault at
 // iteration 0) and primes rho = (r, r^).
-// With gate = 1 the kernel only runs when the scalars ask for an FP64 fallback solve.
+// With gate = 1 the kernel only runs when the scalars ask for an FP64 fallback solve.  With
+// keep_tol = 1 (a restart inside one linear solve) the stopping tolerance set at the solve's start
+// is kept.
 template <class M>
 __global__ void k_krylov_init(M mat, KV<typename M::Vec> v, KrylovScalars *ks, double rtol,
                               double abstol, int max_it, int x_is_zero, double *partials,
-                              unsigned int *tickets, CondArg cond, int gate = 0) {
+                              unsigned int *tickets, CondArg cond, int gate = 0, int keep_tol = 0) {
   using Vec = typename M::Vec;
   if (gate && !ks->fallback) {
     if (blockIdx.x == 0 && threadIdx.x == 0) set_cond(cond, 0);
@@ -306,9 +308,9 @@ __global__ void k_krylov_init(M mat, KV<typename M::Vec> v, KrylovScalars *ks, d
     double rnorm0 = bnorm != 0.0 ? bnorm : dp;
     KrylovScalars s = *ks;
     s.dp = dp;
-    if (!gate) {
+    if (!gate && !keep_tol) {
       s.rnorm0 = rnorm0;
-      s.ttol = fmax(rtol * rnorm0, abstol);   // a fallback keeps the outer solve's tolerance
+      s.ttol = fmax(rtol * rnorm0, abstol);   // a fallback or a restart keeps the solve's tolerance
     }
     s.fallback = 0;
     s.it = 0;

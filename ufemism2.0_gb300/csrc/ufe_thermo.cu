@@ -565,6 +565,37 @@ __global__ void k_gather_upwind(int64_t nV, int64_t nTri, int nz, const int32_t 
 }
 
 // Hi for the zeta gradients, the annual-mean surface temperature (:118-120), Q_base_grnd (:131-133).
+// calc_strain_heating (thermodynamics_utilities.f90:24-78): Phi = 2 A^(-1/n) D^(1/n + 1) with the
+// total strain rate D = sqrt(Dij Dij / 2); no heating where Hi < 0.1 m.  Caller-ordered inputs
+// (k * nV + vi), internal-ordered output through perm (internal vi holds caller perm[vi]).
+struct StrainRates {
+  const double *ux, *uy, *uz, *vx, *vy, *vz, *wx, *wy, *wz;
+};
+__global__ void k_strain_heating(int64_t nV, int nz, const double *__restrict__ Hi_ext,
+                                 const double *__restrict__ A_ext, StrainRates e, double n_glen,
+                                 const int32_t *__restrict__ perm, double *__restrict__ phi) {
+  const int64_t total = nV * nz, stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t ix = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; ix < total; ix += stride) {
+    const int64_t k = ix / nV, vi = ix % nV, o = k * nV + perm[vi];
+    if (Hi_ext[perm[vi]] < 0.1) { phi[ix] = 0.0; continue; }
+    const double a = e.uy[o] + e.vx[o], b = e.uz[o] + e.wx[o], c = e.vz[o] + e.wy[o];
+    const double D = sqrt(0.5 * (e.ux[o] * e.ux[o] + e.vy[o] * e.vy[o] + e.wz[o] * e.wz[o] + 0.5 * (a * a) +
+                                 0.5 * (b * b) + 0.5 * (c * c)));
+    phi[ix] = 2.0 * pow(A_ext[o], -1.0 / n_glen) * pow(D, 1.0 / n_glen + 1.0);
+  }
+}
+
+// calc_frictional_heating (:80-128): beta * |u_base| on grounded vertices, zero elsewhere and
+// without sliding.  Internal order in and out.
+__global__ void k_frictional_heating(int64_t nV, const double *__restrict__ bfc, const double *__restrict__ ub,
+                                     const int32_t *__restrict__ mask, int no_sliding, double *__restrict__ fric) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t vi = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; vi < nV; vi += stride) {
+    const bool grounded = mask[vi] == UFE_COL_GROUNDED || mask[vi] == UFE_COL_GL_GR;
+    fric[vi] = (!no_sliding && grounded) ? bfc[vi] * ub[vi] : 0.0;
+  }
+}
+
 __global__ void k_vertex_prelude(int64_t nV, int n_months, const double *__restrict__ Hi,
                                  const double *__restrict__ T2m, const double *__restrict__ fric,
                                  const double *__restrict__ geo, double *__restrict__ Hc,
@@ -952,9 +983,19 @@ extern "C" int32_t ufe_heat_upload(ufe_ctx *ctx, const ufe_heat_fields *f) {
                     ctx->ops[UFE_OP_DDX_A_B].ind == ctx->ops[UFE_OP_DDY_A_B].ind,
                 UFE_ERR_INVALID, "heat upload: ddx_a_b and ddy_a_b must share one sparsity pattern");
     const double *need[] = {f->Ti, f->Hi, f->Hi_eff, f->Hs, f->dHi_dt, f->dHs_dt, f->u_vav, f->v_vav, f->u_3D,
-                            f->v_3D, f->w_3D, f->u_3D_b, f->v_3D_b, f->internal_heating, f->frictional_heating,
-                            f->geothermal_heat_flux, f->T2m, f->SMB};
+                            f->v_3D, f->w_3D, f->u_3D_b, f->v_3D_b, f->geothermal_heat_flux, f->T2m, f->SMB};
     for (const double *q : need) UFE_REQUIRE(q, UFE_ERR_INVALID, "heat upload: NULL field");
+    // the heating terms: given, or computed here from their inputs
+    const bool strain = f->internal_heating == nullptr, friction = f->frictional_heating == nullptr;
+    if (strain) {
+      const double *sr[] = {f->A_flow, f->du_dx_3D, f->du_dy_3D, f->du_dz_3D, f->dv_dx_3D, f->dv_dy_3D, f->dv_dz_3D,
+                            f->dw_dx_3D, f->dw_dy_3D, f->dw_dz_3D};
+      for (const double *q : sr)
+        UFE_REQUIRE(q, UFE_ERR_INVALID, "heat upload: strain heating needs A_flow and the nine 3-D strain rates");
+    }
+    if (friction)
+      UFE_REQUIRE(f->basal_friction_coefficient && f->uabs_base, UFE_ERR_INVALID,
+                  "heat upload: frictional heating needs basal_friction_coefficient and uabs_base");
     UFE_REQUIRE(f->mask && f->n_months >= 1, UFE_ERR_INVALID, "heat upload: need mask and n_months >= 1");
     const int64_t nV = ctx->nV, nTri = ctx->nTri;
     const int nz = ctx->nz;
@@ -987,8 +1028,32 @@ extern "C" int32_t ufe_heat_upload(ufe_ctx *ctx, const ufe_heat_fields *f) {
     to_internal(ctx, t->u, f->u_3D, false, nz);
     to_internal(ctx, t->v, f->v_3D, false, nz);
     to_internal(ctx, t->w, f->w_3D, false, nz);
-    to_internal(ctx, t->phi, f->internal_heating, false, nz);
     to_internal_i32(ctx, t->mask, f->mask, false);
+    if (!strain) {
+      to_internal(ctx, t->phi, f->internal_heating, false, nz);
+    } else {
+      // the inputs go up in the caller's order; the kernel gathers them while it computes
+      const size_t nl = (size_t)nV * nz;
+      double *buf = (double *)dev_alloc(sizeof(double) * (nl * 10 + nV));
+      try {
+        const double *src[] = {f->A_flow, f->du_dx_3D, f->du_dy_3D, f->du_dz_3D, f->dv_dx_3D, f->dv_dy_3D,
+                               f->dv_dz_3D, f->dw_dx_3D, f->dw_dy_3D, f->dw_dz_3D};
+        for (int q = 0; q < 10; ++q)
+          UFE_CUDA(cudaMemcpyAsync(buf + q * nl, src[q], sizeof(double) * nl, cudaMemcpyHostToDevice, s));
+        UFE_CUDA(cudaMemcpyAsync(buf + 10 * nl, f->Hi, sizeof(double) * nV, cudaMemcpyHostToDevice, s));
+        StrainRates e{buf + nl, buf + 2 * nl, buf + 3 * nl, buf + 4 * nl, buf + 5 * nl, buf + 6 * nl, buf + 7 * nl,
+                      buf + 8 * nl, buf + 9 * nl};
+        k_strain_heating<<<(unsigned)std::min<int64_t>((nl + 255) / 256, 65535), 256, 0, s>>>(
+            nV, nz, buf + 10 * nl, buf, e, f->Glens_flow_law_exponent > 0.0 ? f->Glens_flow_law_exponent : 3.0, ctx->perm_v,
+            t->phi);
+        UFE_CUDA(cudaGetLastError());
+        UFE_CUDA(cudaStreamSynchronize(s));
+      } catch (...) {
+        dev_free(buf);
+        throw;
+      }
+      dev_free(buf);
+    }
     double *vt = t->vert;
     // slots: 0 gHs_x, 1 gHi_x, 2 gHs_y, 3 gHi_y, 4 dHs_dt, 5 dHi_dt, 6 Hc, 7 Hi_eff, 8 T_surf, 9 Q,
     //        10 fr, 11 geo, 12 SMB
@@ -1015,7 +1080,16 @@ extern "C" int32_t ufe_heat_upload(ufe_ctx *ctx, const ufe_heat_fields *f) {
       to_internal(ctx, Hs, f->Hs, false, 1);
       to_internal(ctx, uv, f->u_vav, false, 1);
       to_internal(ctx, vv, f->v_vav, false, 1);
-      to_internal(ctx, fric, f->frictional_heating, false, 1);
+      if (!friction) {
+        to_internal(ctx, fric, f->frictional_heating, false, 1);
+      } else {
+        double *bfc = ubt, *uab = ubt + nV;   // ubt is filled below; use it as scratch first
+        to_internal(ctx, bfc, f->basal_friction_coefficient, false, 1);
+        to_internal(ctx, uab, f->uabs_base, false, 1);
+        k_frictional_heating<<<(unsigned)((nV + 255) / 256), 256, 0, s>>>(nV, bfc, uab, t->mask, f->no_sliding,
+                                                                          fric);
+        UFE_CUDA(cudaGetLastError());
+      }
       to_internal(ctx, T2m, f->T2m, false, f->n_months);
       to_internal(ctx, ubt, f->u_3D_b, true, nz);
       to_internal(ctx, vbt, f->v_3D_b, true, nz);

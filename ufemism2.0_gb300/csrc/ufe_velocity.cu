@@ -29,6 +29,7 @@ namespace {
 
 constexpr double kIceDensity = 910.0;  // src/UPSY/basic/parameters.f90:23
 constexpr double kGrav = 9.81;         // parameters.f90:20
+constexpr double kRGas = 8.314;        // parameters.f90:27
 constexpr int kMaxNz = 64;
 constexpr int kThreads = 256;
 constexpr int kMaxRefine = 60;
@@ -56,6 +57,9 @@ struct PhysParams {
   int bc_u[4], bc_v[4];   // N, E, S, W
   double n_glen, visc_eff_min, vel_max, m_weertman, delta_v, beta_max, fgr_exp;
   double budd_q, budd_u0;
+  double zi_p, zi_ut;
+  int inexact;        // krylov_forcing > 0: the two-phase inexact Picard iteration
+  double relax_cfg;   // visc_it_relax as configured (the 'infinite_SSA_icestream' border rows)
   double picard_tol;
   int visc_it_nit;
 };
@@ -77,6 +81,10 @@ PhysParams make_phys(const ufe_solver_params &p, int has_bc) {
   q.fgr_exp = p.subgrid_friction_exponent_on_B_grid;
   q.budd_q = p.slid_Budd_q_plastic;
   q.budd_u0 = p.slid_Budd_u_threshold;
+  q.zi_p = p.slid_ZI_p;
+  q.zi_ut = p.slid_ZI_ut;
+  q.relax_cfg = p.visc_it_relax;
+  q.inexact = p.krylov_forcing > 0.0;
   q.picard_tol = p.visc_it_norm_dUV_tol;
   q.visc_it_nit = p.visc_it_nit;
   return q;
@@ -120,6 +128,12 @@ __device__ double sliding_beta(const PhysParams &q, const SlidingIn &s, int vi, 
              pow(uabs, -1.0);
       break;
     }
+    case UFE_SLIDING_ZOET_IVERSON:   // :399-400
+      beta = s.tys[vi] * pow(uabs, 1.0 / q.zi_p - 1.0) * pow(uabs + q.zi_ut, -1.0 / q.zi_p);
+      break;
+    case UFE_SLIDING_IDEALISED_SSA_ICESTREAM:   // :477 (tys: Schoof's yield stress, k_icestream_yield)
+      beta = s.tys[vi] / uabs;
+      break;
     default: beta = 0.0;
   }
   return fmin(q.beta_max, beta);
@@ -170,11 +184,56 @@ __global__ void k_prologue(int nV, int nTri, int nz, OpRow ab, const double *Hi,
     p.status = UFE_OK;
     p.n_refine = 0;
     p.prev_total_its = 0;
+    p.phase = 0;
     p.active = 1;
     KrylovScalars k;
     memset(&k, 0, sizeof(k));
     *ks = k;
   }
+}
+
+// ---- calc_ice_rheology_Glen (constitutive_equation.f90:84-163) --------------------------------
+// Per vertex and layer: the uniform flow factor or the Arrhenius relation of Huybrechts (1992),
+// then the enhancement factor of the vertex.  The reference evaluates it inside every Picard
+// iteration; it depends only on the ice state, so one evaluation per solve gives the same field.
+struct RheologyIn {
+  int choice, enh;
+  double A_uniform, m_sheet, m_shelf;
+  const double *Ti, *Hi, *Hib, *SL, *fgr;
+  const int32_t *mask_gr, *mask_fl;
+};
+__global__ void k_rheology(int nV, int nz, RheologyIn r, double *A_out) {
+  int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t ix = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; ix < (int64_t)nV * nz; ix += stride) {
+    const int vi = (int)(ix % nV);
+    double A;
+    if (r.choice == UFE_RHEOLOGY_UNIFORM) {
+      A = r.A_uniform;
+    } else {
+      const double T = r.Ti[ix];
+      // T_switch 263.15 K; a = 1.14e-5 / 5.47e10 Pa^-3 yr^-1; Q = 6.0e4 / 13.9e4 J mol^-1 (:94-98)
+      A = (T < 263.15) ? 1.14E-05 * exp(-6.0E+04 / (kRGas * T)) : 5.47E+10 * exp(-13.9E+04 / (kRGas * T));
+    }
+    const bool gr = r.mask_gr[vi] != 0, fl = r.mask_fl && r.mask_fl[vi] != 0;
+    if (r.enh == UFE_ENH_INTERP && r.Hi[vi] > 0.0 && r.Hib[vi] < r.SL[vi])
+      A = A * (r.fgr[vi] * r.m_sheet + (1.0 - r.fgr[vi]) * r.m_shelf);
+    else if (gr)
+      A = A * r.m_sheet;
+    else if (fl)
+      A = A * r.m_shelf;
+    A_out[ix] = A;
+  }
+}
+
+// The till yield stress of Schoof's (2006) ice stream at each vertex's y coordinate
+// (Schoof2006_icestream, src/UPSY/basic/analytical_solutions/Schoof_SSA_solution.f90:15-64, the
+// part calc_sliding_law_idealised_SSA_icestream reads, sliding_laws.f90:469-473).
+__global__ void k_icestream_yield(int nV, const double *Vy, double H, double tantheta, double L, double m,
+                                  double *tys) {
+  int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  const double f = -kIceDensity * kGrav * H * tantheta;
+  for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < nV; v += stride)
+    tys[v] = f * pow(fabs(Vy[v] / L), m);
 }
 
 // ---- SSA vertex kernel ----------------------------------------------------------------------
@@ -284,6 +343,9 @@ struct AssembleArgs {
   const int32_t *bc_mask;
   const double2 *bc_uv;
   const double2 *x0;        // Krylov initial guess (or null = zero)
+  const double2 *uprev;     // velocity before this linear solve (u_b_prev, v_b_prev)
+  const int32_t *cp_ptr, *cp_idx;   // 'infinite_SSA_icestream' copy triangles (null: none built)
+  const double *cp_w;
   // outputs
   double4 *blk;
   float4 *blk32, *rowsum32;
@@ -293,7 +355,8 @@ struct AssembleArgs {
   int *err;
   // Krylov
   KrylovScalars *ks;
-  double rtol, abstol;
+  const PicardScalars *ps;  // the Picard phase (null outside a Picard solve)
+  double rtol, abstol, forcing;
   int max_it;
   double *partials;
   unsigned int *tickets;
@@ -367,7 +430,16 @@ __global__ void k_assemble(AssembleArgs a, PhysParams q, CondArg cond) {
         for (int uvc = 0; uvc < 2; ++uvc) {
           const int choice = uvc == 0 ? q.bc_u[side] : q.bc_v[side];
           const int comp = uvc == 0 ? 0 : 3;  // uu or vv entry of the block
-          if (choice == UFE_BC_INFINITE) {
+          if (choice == UFE_BC_INFINITE_SSA_ICESTREAM) {
+            // u = relaxed previous u at the copy point (:562-578); validated to be u only
+            bd[4 * (int64_t)kd + comp] = 1.0;
+            double u_fixed = 0.0;
+            if (a.cp_ptr)
+              for (int k = a.cp_ptr[t]; k < a.cp_ptr[t + 1]; ++k) u_fixed = u_fixed + a.cp_w[k] * a.uprev[a.cp_idx[k]].x;
+            else
+              atomicOr(a.err, kErrBcNeighbour);
+            rhs.x = (q.relax_cfg * u_fixed) + ((1.0 - q.relax_cfg) * a.uprev[t].x);
+          } else if (choice == UFE_BC_INFINITE) {
             int nnb = 0;
             for (int n = 0; n < 3; ++n) {
               int tj = a.TriC[(int64_t)n * nTri + t];
@@ -453,7 +525,10 @@ __global__ void k_assemble(AssembleArgs a, PhysParams q, CondArg cond) {
     KrylovScalars s = *a.ks;
     s.dp = dp;
     s.rnorm0 = rnorm0;
-    s.ttol = fmax(a.rtol * rnorm0, a.abstol);
+    // the reference's fixed tolerance (KSPSetTolerances, petsc_basic.f90:110), or for an inexact
+    // Picard iteration krylov_forcing times this Picard iterate's own residual, if larger
+    const double forcing = (a.ps && a.ps->phase != 0) ? 0.0 : a.forcing;
+    s.ttol = fmax(fmax(a.rtol * rnorm0, a.abstol), forcing * dp);
     s.it = 0;
     s.max_it = a.max_it;
     s.rho = tot[0];
@@ -617,6 +692,14 @@ __device__ void picard_step(PicardScalars *psp, KrylovScalars *ks, double r1, do
   }
   if (isnan(p.L2)) { p.status = UFE_ERR_NAN; stop = 1; }
   int converged = p.L2 < q.picard_tol;
+  // inexact Picard: the first time the change norm meets the tolerance, the forced (inexact)
+  // linear solves end and the iteration goes on with solves to the full Krylov tolerance, until
+  // the change norm meets the tolerance after such a solve -- a small step from a loosely solved
+  // system is not taken as convergence
+  if (!stop && converged && q.inexact && p.phase == 0) {
+    p.phase = 1;
+    converged = 0;
+  }
   if (!stop && !converged && p.it > q.visc_it_nit) {
     if (p.status == UFE_OK) p.status = UFE_WARN_PICARD_MAXIT;
     stop = 1;
@@ -1082,7 +1165,9 @@ void free_work(ufe_ctx *ctx) {
                   w->eta_3D_a, w->F1_3D_a, w->N_b_in, w->dNx_b_in, w->dNy_b_in, w->beta_b_in, w->ks,
                   w->ps, w->err, w->ppart, w->gsync, w->sell_off, w->sell_col, w->sell_map, w->sell_blk,
                   w->sell_blk32, w->halo_off, w->halo_idx, w->halo_lcol, w->pX, w->pR, w->pRP, w->pS, w->pT,
-                  w->pdinv, w->pP[0], w->pP[1], w->pV[0], w->pV[1], w->sell_blkp, w->pair_bad};
+                  w->pdinv, w->pP[0], w->pP[1], w->pV[0], w->pV[1], w->sell_blkp, w->pair_bad,
+                  w->Ti, w->mask_fl, w->fgr_v, w->Hib, w->SL, w->A_rheo, w->tys_ideal, w->cp_ptr, w->cp_idx,
+                  w->cp_w};
   for (void *p : ptrs) dev_free(p);
   if (w->ks_host) cudaFreeHost(w->ks_host);
   if (w->ps_host) cudaFreeHost(w->ps_host);
@@ -1099,6 +1184,85 @@ int32_t bsr_lanes(ufe_ctx *ctx) {
     lanes = (v == 1 || v == 2 || v == 4 || v == 8) ? v : 1;
   }
   return lanes;
+}
+
+// gfortran's NORM2 of a 2-vector: the scaled sum of squares with a running scale
+static double host_norm2(double a, double b) {
+  const double xs[2] = {a, b};
+  double scale = 1.0, result = 0.0;
+  for (double x : xs) {
+    if (x == 0.0) continue;
+    const double ax = fabs(x);
+    if (scale < ax) {
+      const double r = scale / ax;
+      result = 1.0 + result * r * r;
+      scale = ax;
+    } else {
+      const double r = ax / scale;
+      result += r * r;
+    }
+  }
+  return sqrt(result) * scale;
+}
+
+static bool icestream_bc(const ufe_solver_params &p) {
+  return p.BC_u_west == UFE_BC_INFINITE_SSA_ICESTREAM || p.BC_u_east == UFE_BC_INFINITE_SSA_ICESTREAM ||
+         p.BC_u_south == UFE_BC_INFINITE_SSA_ICESTREAM || p.BC_u_north == UFE_BC_INFINITE_SSA_ICESTREAM;
+}
+
+// Copy triangles and weights of every border triangle for the 'infinite_SSA_icestream' rows
+// (find_ti_copy_SSA_icestream_infinite, src/UPSY/mesh/mesh_utilities.f90:2681-2729): the point
+// at the triangle's y, one third (x < 0) or two thirds (x >= 0) across the domain; the vertex
+// whose Voronoi cell holds it (the nearest vertex; find_containing_vertex's walk, :1368-1416,
+// ends there on a Delaunay mesh); that vertex's triangles weighted by 1/distance^2, normalised.
+// Host computation on the internal numbering, once per mesh.
+void build_icestream_copy(ufe_ctx *ctx, Work *w) {
+  const int64_t nV = ctx->nV, nTri = ctx->nTri, nCm = ctx->nC_mem;
+  cudaStream_t s = ctx->stream;
+  std::vector<double> V(2 * nV), GC(2 * nTri);
+  std::vector<int32_t> niTri(nV), iTri(nV * nCm), TriBI(nTri);
+  UFE_CUDA(cudaMemcpyAsync(V.data(), ctx->V, sizeof(double) * 2 * nV, cudaMemcpyDeviceToHost, s));
+  UFE_CUDA(cudaMemcpyAsync(GC.data(), ctx->TriGC, sizeof(double) * 2 * nTri, cudaMemcpyDeviceToHost, s));
+  UFE_CUDA(cudaMemcpyAsync(niTri.data(), ctx->niTri, sizeof(int32_t) * nV, cudaMemcpyDeviceToHost, s));
+  UFE_CUDA(cudaMemcpyAsync(iTri.data(), ctx->iTri, sizeof(int32_t) * nV * nCm, cudaMemcpyDeviceToHost, s));
+  UFE_CUDA(cudaMemcpyAsync(TriBI.data(), ctx->TriBI, sizeof(int32_t) * nTri, cudaMemcpyDeviceToHost, s));
+  UFE_CUDA(cudaStreamSynchronize(s));
+  double xmin = V[0], xmax = V[0];
+  for (int64_t v = 1; v < nV; ++v) { xmin = std::min(xmin, V[v]); xmax = std::max(xmax, V[v]); }
+  std::vector<int32_t> ptr(nTri + 1, 0), idx;
+  std::vector<double> wts;
+  for (int64_t t = 0; t < nTri; ++t) {
+    if (TriBI[t] > 0) {
+      const double py = GC[nTri + t];
+      const double px = GC[t] < 0.0 ? xmin + (xmax - xmin) * 1.0 / 3.0 : xmin + (xmax - xmin) * 2.0 / 3.0;
+      int64_t vi = 0;
+      double best = 0.0;
+      for (int64_t v = 0; v < nV; ++v) {
+        const double dx = V[v] - px, dy = V[nV + v] - py, d = dx * dx + dy * dy;
+        if (v == 0 || d < best) { best = d; vi = v; }
+      }
+      const size_t k0 = wts.size();
+      double sum = 0.0;
+      for (int c = 0; c < niTri[vi]; ++c) {
+        const int32_t tj = iTri[c * nV + vi] - 1;
+        const double dist = host_norm2(px - GC[tj], py - GC[nTri + tj]);
+        idx.push_back(tj);
+        wts.push_back(1.0 / (dist * dist));
+      }
+      for (size_t k = k0; k < wts.size(); ++k) sum = sum + wts[k];
+      for (size_t k = k0; k < wts.size(); ++k) wts[k] = wts[k] / sum;
+    }
+    ptr[t + 1] = (int32_t)idx.size();
+  }
+  w->cp_ptr = alloc_n<int32_t>(nTri + 1);
+  w->cp_idx = alloc_n<int32_t>(idx.size());
+  w->cp_w = alloc_n<double>(wts.size());
+  UFE_CUDA(cudaMemcpyAsync(w->cp_ptr, ptr.data(), sizeof(int32_t) * (nTri + 1), cudaMemcpyHostToDevice, s));
+  if (!idx.empty()) {
+    UFE_CUDA(cudaMemcpyAsync(w->cp_idx, idx.data(), sizeof(int32_t) * idx.size(), cudaMemcpyHostToDevice, s));
+    UFE_CUDA(cudaMemcpyAsync(w->cp_w, wts.data(), sizeof(double) * wts.size(), cudaMemcpyHostToDevice, s));
+  }
+  UFE_CUDA(cudaStreamSynchronize(s));
 }
 
 // ============================================================================================
@@ -1162,13 +1326,38 @@ struct Solver {
     const DevCSR &mba = ctx->ops[UFE_OP_MAP_B_A];
     ba = OpRow{mba.ptr, mba.ind, mba.val, ctx->ops[UFE_OP_DDX_B_A].val, ctx->ops[UFE_OP_DDY_B_A].val};
     if (pair_ok()) ensure_pair();
+    if (icestream_bc(p) && !w->cp_ptr) build_icestream_copy(ctx, w);
   }
 
   int eblocks(int64_t n) const { return pick_blocks(n, kThreads, grid); }
 
-  SlidingIn sliding() const { return SlidingIn{w->beta_sq, w->alpha_sq, w->effp, w->tys}; }
+  SlidingIn sliding() const {
+    const double *tys = p.choice_sliding_law == UFE_SLIDING_IDEALISED_SSA_ICESTREAM ? w->tys_ideal : w->tys;
+    return SlidingIn{w->beta_sq, w->alpha_sq, w->effp, tys};
+  }
+  // the flow factor the solve reads: the caller's A_flow, or calc_ice_rheology_Glen's
+  const double *A_src() const {
+    return p.choice_ice_rheology_Glen == UFE_RHEOLOGY_INPUT ? w->A_flow : w->A_rheo;
+  }
+  // Inputs a resident solve needs beyond the uploaded ice state, checked and allocated before
+  // any graph is captured.
+  void setup_solve_inputs() {
+    const size_t nV = w->nV, nz = w->nz;
+    if (p.choice_ice_rheology_Glen == UFE_RHEOLOGY_INPUT) {
+      UFE_REQUIRE(w->has_A, UFE_ERR_INVALID, "A_flow missing (choice_ice_rheology_Glen is 'input')");
+    } else {
+      UFE_REQUIRE(p.choice_ice_rheology_Glen != UFE_RHEOLOGY_HUYBRECHTS1992 || w->has_Ti, UFE_ERR_INVALID,
+                  "Huybrechts1992 rheology needs the ice temperature Ti");
+      UFE_REQUIRE(p.choice_enhancement_factor_transition != UFE_ENH_INTERP ||
+                      (w->has_fgr_v && w->has_Hib && w->has_SL),
+                  UFE_ERR_INVALID, "'interp' enhancement factors need fraction_gr, Hib and SL");
+      if (!w->A_rheo) w->A_rheo = alloc_n<double>(nV * nz);
+    }
+    if (p.choice_sliding_law == UFE_SLIDING_IDEALISED_SSA_ICESTREAM && !w->tys_ideal)
+      w->tys_ideal = alloc_n<double>(nV);
+  }
 
-  AssembleArgs assemble_args(const double2 *x0) const {
+  AssembleArgs assemble_args(const double2 *x0, int mode) const {
     AssembleArgs a;
     memset(&a, 0, sizeof(a));
     a.nV = w->nV; a.nTri = w->nTri; a.nz = w->nz;
@@ -1183,6 +1372,8 @@ struct Solver {
     a.N_a = w->N_a; a.beta_a = w->beta_a; a.beta_eff_a = w->beta_eff_a; a.F2a1 = w->F2a1; a.eta_3D_a = w->eta_3D_a;
     a.fgr_b = w->fgr_b; a.tau_d = w->tau_d; a.bc_mask = w->bc_mask; a.bc_uv = w->bc_uv;
     a.x0 = x0;
+    a.uprev = w->uv;
+    a.cp_ptr = w->cp_ptr; a.cp_idx = w->cp_idx; a.cp_w = w->cp_w;
     a.blk = w->blk;
     a.blk32 = (p.precision == UFE_PREC_FP32_REFINE) ? w->blk32 : nullptr;
     a.rowsum32 = w->rowsum32;
@@ -1193,6 +1384,8 @@ struct Solver {
     a.ks = w->ks;
     a.rtol = p.stress_balance_PETSc_rtol;
     a.abstol = p.stress_balance_PETSc_abstol;
+    a.forcing = p.krylov_forcing;
+    a.ps = (mode == kFromTriangles) ? nullptr : w->ps;
     a.max_it = p.krylov_max_it;
     a.partials = ctx->red.partials;
     a.tickets = ctx->red.tickets;
@@ -1200,7 +1393,7 @@ struct Solver {
   }
 
   void enqueue_assemble(int mode, bool x0_current, CondArg c) {
-    AssembleArgs a = assemble_args(x0_current ? w->uv : nullptr);
+    AssembleArgs a = assemble_args(x0_current ? w->uv : nullptr, mode);
     int g = eblocks(w->nTri);
     if (mode == kFromTriangles) k_assemble<kFromTriangles><<<g, kThreads, 0, s>>>(a, q, c);
     else if (mode == kFromSSA) k_assemble<kFromSSA><<<g, kThreads, 0, s>>>(a, q, c);
@@ -1422,7 +1615,7 @@ struct Solver {
     CondArg none{0, 0};
     k_krylov_init<BsrMat<double, double, 1>><<<krylov_grid(m, kThreads, grid), kThreads, 0, s>>>(
         m, kv64(), w->ks, p.stress_balance_PETSc_rtol, p.stress_balance_PETSc_abstol, p.krylov_max_it, 0,
-        ctx->red.partials, ctx->red.tickets, none, 0);
+        ctx->red.partials, ctx->red.tickets, none, 0, 1);
     k_pair_gate<<<1, 1, 0, s>>>(w->ks, c);
     UFE_CUDA(cudaGetLastError());
   }
@@ -1512,8 +1705,18 @@ struct Solver {
   }
 
   void enqueue_prologue(bool diva) {
+    if (p.choice_ice_rheology_Glen != UFE_RHEOLOGY_INPUT) {
+      RheologyIn r{p.choice_ice_rheology_Glen, p.choice_enhancement_factor_transition, p.uniform_Glens_flow_factor,
+                   p.m_enh_sheet, p.m_enh_shelf, w->Ti, w->Hi, w->Hib, w->SL, w->fgr_v, w->mask_gr,
+                   w->has_mask_fl ? w->mask_fl : nullptr};
+      k_rheology<<<eblocks((int64_t)w->nV * w->nz), kThreads, 0, s>>>(w->nV, w->nz, r, w->A_rheo);
+    }
+    if (p.choice_sliding_law == UFE_SLIDING_IDEALISED_SSA_ICESTREAM)
+      k_icestream_yield<<<eblocks(w->nV), kThreads, 0, s>>>(w->nV, ctx->V + w->nV, p.SSA_icestream_Hi,
+                                                           p.SSA_icestream_dhdx, p.SSA_icestream_L, p.SSA_icestream_m,
+                                                           w->tys_ideal);
     k_prologue<<<eblocks(std::max(w->nV, w->nTri)), kThreads, 0, s>>>(
-        w->nV, w->nTri, w->nz, ab, w->Hi, w->Hs, w->A_flow, ctx->zeta, w->tau_d, diva ? nullptr : w->Avav,
+        w->nV, w->nTri, w->nz, ab, w->Hi, w->Hs, A_src(), ctx->zeta, w->tau_d, diva ? nullptr : w->Avav,
         diva ? w->A_pow : nullptr, w->ps, w->ks, p.visc_it_relax, p.Glens_flow_law_epsilon_sq_0,
         p.Glens_flow_law_exponent);
     UFE_CUDA(cudaMemsetAsync(w->ks + 1, 0, sizeof(KrylovScalars), s));
@@ -1763,8 +1966,16 @@ bool use_graphs() {
 
 void validate_params(const ufe_solver_params *p) {
   UFE_REQUIRE(p, UFE_ERR_INVALID, "null params");
-  UFE_REQUIRE(p->choice_sliding_law >= 0 && p->choice_sliding_law <= UFE_SLIDING_SCHOOF2005, UFE_ERR_INVALID,
-              "unknown sliding law");
+  UFE_REQUIRE(p->choice_sliding_law >= 0 && p->choice_sliding_law <= UFE_SLIDING_IDEALISED_SSA_ICESTREAM,
+              UFE_ERR_INVALID, "unknown sliding law");
+  // Schoof only derived his ice-stream solution for n = 3 (Schoof_SSA_solution.f90:40)
+  UFE_REQUIRE(p->choice_sliding_law != UFE_SLIDING_IDEALISED_SSA_ICESTREAM || p->Glens_flow_law_exponent == 3.0,
+              UFE_ERR_INVALID, "the SSA_icestream sliding law needs Glens_flow_law_exponent = 3");
+  UFE_REQUIRE(p->choice_ice_rheology_Glen >= UFE_RHEOLOGY_INPUT &&
+                  p->choice_ice_rheology_Glen <= UFE_RHEOLOGY_HUYBRECHTS1992 &&
+                  (p->choice_enhancement_factor_transition == UFE_ENH_SEPARATE ||
+                   p->choice_enhancement_factor_transition == UFE_ENH_INTERP),
+              UFE_ERR_INVALID, "unknown rheology or enhancement-factor choice");
   UFE_REQUIRE(p->visc_it_nit >= 0 && p->krylov_max_it >= 1, UFE_ERR_INVALID, "iteration limits out of range");
   UFE_REQUIRE(p->precision == UFE_PREC_FP64 || p->precision == UFE_PREC_FP32_REFINE ||
                   p->precision == UFE_PREC_FP32_PAIR,
@@ -1774,10 +1985,12 @@ void validate_params(const ufe_solver_params *p) {
   const int32_t bcs[8] = {p->BC_u_west, p->BC_u_east, p->BC_u_south, p->BC_u_north,
                           p->BC_v_west, p->BC_v_east, p->BC_v_south, p->BC_v_north};
   for (int i = 0; i < 8; ++i)
-    UFE_REQUIRE(bcs[i] == UFE_BC_INFINITE || bcs[i] == UFE_BC_ZERO, UFE_ERR_INVALID, "unsupported boundary condition");
+    UFE_REQUIRE(bcs[i] == UFE_BC_INFINITE || bcs[i] == UFE_BC_ZERO || (i < 4 && bcs[i] == UFE_BC_INFINITE_SSA_ICESTREAM),
+                UFE_ERR_INVALID, "unsupported boundary condition");   // the ice-stream copy is u only (:562)
   UFE_REQUIRE(p->Glens_flow_law_exponent > 0 && p->visc_it_relax > 0 && p->visc_it_relax <= 1, UFE_ERR_INVALID,
               "flow law exponent or relaxation out of range");
   UFE_REQUIRE(p->krylov_inner_rtol > 0 && p->krylov_inner_rtol < 1, UFE_ERR_INVALID, "krylov_inner_rtol out of range");
+  UFE_REQUIRE(p->krylov_forcing >= 0 && p->krylov_forcing < 1, UFE_ERR_INVALID, "krylov_forcing out of range");
 }
 
 int32_t check_err_flag(Solver &S) {
@@ -1799,6 +2012,7 @@ int32_t check_err_flag(Solver &S) {
 // reads the result.  Ensembles launch all members before collecting any.
 void picard_launch(ufe_ctx *ctx, const ufe_solver_params &p, bool diva) {
   Solver S(ctx, p);
+  S.setup_solve_inputs();
   Work *w = S.w;
   UFE_REQUIRE(ctx->nz <= kMaxNz, UFE_ERR_CAPACITY, "nz exceeds 64 layers");
   cudaEventRecord(ctx->ev0, S.s);
@@ -1885,7 +2099,7 @@ static void upload_bc(ufe_ctx *ctx, Work *w, const ufe_bc_prescribed *bc) {
 
 extern "C" int32_t ufe_ice_upload(ufe_ctx *ctx, const ufe_ice_state *ice, const ufe_bc_prescribed *bc) {
   return guarded(ctx, [&]() -> int32_t {
-    UFE_REQUIRE(ice && ice->Hi && ice->Hs && ice->A_flow && ice->fraction_gr_b && ice->mask_grounded_ice,
+    UFE_REQUIRE(ice && ice->Hi && ice->Hs && ice->fraction_gr_b && ice->mask_grounded_ice,
                 UFE_ERR_INVALID, "ice state arrays missing");
     UFE_CUDA(cudaSetDevice(ctx->device));
     Work *w = ensure_work(ctx);
@@ -1893,7 +2107,27 @@ extern "C" int32_t ufe_ice_upload(ufe_ctx *ctx, const ufe_ice_state *ice, const 
     const size_t nV = ctx->nV, nTri = ctx->nTri, nz = ctx->nz;
     to_internal(ctx, w->Hi, ice->Hi, false, 1);
     to_internal(ctx, w->Hs, ice->Hs, false, 1);
-    to_internal(ctx, w->A_flow, ice->A_flow, false, (int)nz);
+    // A_flow may be absent when the solve computes it (calc_ice_rheology_Glen)
+    w->has_A = ice->A_flow != nullptr;
+    if (ice->A_flow) to_internal(ctx, w->A_flow, ice->A_flow, false, (int)nz);
+    else UFE_CUDA(cudaMemsetAsync(w->A_flow, 0, sizeof(double) * nV * nz, s));
+    // calc_ice_rheology_Glen inputs: buffers allocated on first use and kept (captured solve
+    // graphs hold their addresses); the flags say which were given with this ice state
+    auto opt_vertex = [&](double *&dst, int32_t &has, const double *src, int ncols) {
+      has = src != nullptr;
+      if (!src) return;
+      if (!dst) dst = alloc_n<double>(nV * ncols);
+      to_internal(ctx, dst, src, false, ncols);
+    };
+    opt_vertex(w->Ti, w->has_Ti, ice->Ti, (int)nz);
+    opt_vertex(w->fgr_v, w->has_fgr_v, ice->fraction_gr, 1);
+    opt_vertex(w->Hib, w->has_Hib, ice->Hib, 1);
+    opt_vertex(w->SL, w->has_SL, ice->SL, 1);
+    w->has_mask_fl = ice->mask_floating_ice != nullptr;
+    if (ice->mask_floating_ice) {
+      if (!w->mask_fl) w->mask_fl = alloc_n<int32_t>(nV);
+      to_internal_i32(ctx, w->mask_fl, ice->mask_floating_ice, false);
+    }
     to_internal(ctx, w->fgr_b, ice->fraction_gr_b, true, 1);
     to_internal_i32(ctx, w->mask_gr, ice->mask_grounded_ice, false);
     upload_vertex_opt(ctx, w->beta_sq, ice->beta_sq);
@@ -1904,10 +2138,14 @@ extern "C" int32_t ufe_ice_upload(ufe_ctx *ctx, const ufe_ice_state *ice, const 
     {
       int *flag = w->err;
       UFE_CUDA(cudaMemsetAsync(flag, 0, sizeof(int), s));
-      const double *arrs[] = {w->Hi, w->Hs, w->A_flow, w->fgr_b, w->beta_sq, w->alpha_sq, w->effp, w->tys};
-      const size_t lens[] = {nV, nV, nV * nz, nTri, nV, nV, nV, nV};
-      for (int k = 0; k < 8; ++k)
-        k_check_finite<<<pick_blocks((int64_t)lens[k], kThreads, 256), kThreads, 0, s>>>(arrs[k], (int64_t)lens[k], flag);
+      const double *arrs[] = {w->Hi, w->Hs, w->A_flow, w->fgr_b, w->beta_sq, w->alpha_sq, w->effp, w->tys,
+                              w->has_Ti ? w->Ti : nullptr, w->has_fgr_v ? w->fgr_v : nullptr,
+                              w->has_Hib ? w->Hib : nullptr, w->has_SL ? w->SL : nullptr};
+      const size_t lens[] = {nV, nV, nV * nz, nTri, nV, nV, nV, nV, nV * nz, nV, nV, nV};
+      for (int k = 0; k < 12; ++k)
+        if (arrs[k])
+          k_check_finite<<<pick_blocks((int64_t)lens[k], kThreads, 256), kThreads, 0, s>>>(arrs[k], (int64_t)lens[k],
+                                                                                          flag);
       UFE_CUDA(cudaGetLastError());
       int hflag = 0;
       UFE_CUDA(cudaMemcpyAsync(&hflag, flag, sizeof(int), cudaMemcpyDeviceToHost, s));
@@ -2340,11 +2578,11 @@ extern "C" int32_t ufe_assemble_linearised(ufe_ctx *ctx, const ufe_solver_params
                                            const ufe_bc_prescribed *bc, int32_t *ptr, int32_t *ind, double *val,
                                            double *bb, int64_t cap, int64_t *nnz_out) {
   return guarded(ctx, [&]() -> int32_t {
-    (void)u_b_prev; (void)v_b_prev;
     validate_params(p);
     UFE_CUDA(cudaSetDevice(ctx->device));
     Work *w = ensure_work(ctx);
     upload_linearised_inputs(ctx, w, N_b, dN_dx_b, dN_dy_b, basal_friction_coefficient_b, tau_dx_b, tau_dy_b, bc);
+    upload_pair(ctx, w->uv, u_b_prev, v_b_prev);   // the 'infinite_SSA_icestream' border rows read it
     Solver S(ctx, *p);
     CondArg none{0, 0};
     S.enqueue_assemble(kFromTriangles, false, none);

@@ -113,6 +113,20 @@ struct Work {
   double *beta_sq = nullptr, *alpha_sq = nullptr, *effp = nullptr, *tys = nullptr;
   int32_t *mask_gr = nullptr;
   int32_t any_grounded = 0;
+  // inputs of calc_ice_rheology_Glen (allocated when first given, then kept for the Work's life so
+  // captured graphs never see a freed pointer) and the flow factor it computes
+  int32_t has_A = 0;              // the caller gave A_flow
+  int32_t has_Ti = 0, has_mask_fl = 0, has_fgr_v = 0, has_Hib = 0, has_SL = 0;
+  double *Ti = nullptr;           // nz x nV
+  int32_t *mask_fl = nullptr;
+  double *fgr_v = nullptr, *Hib = nullptr, *SL = nullptr;
+  double *A_rheo = nullptr;       // nz x nV
+  // the idealised SSA_icestream sliding law: Schoof's till yield stress per vertex
+  double *tys_ideal = nullptr;
+  // 'infinite_SSA_icestream' border rows: copy triangles and weights per triangle (CSR over
+  // triangles, empty rows elsewhere), built on first use
+  int32_t *cp_ptr = nullptr, *cp_idx = nullptr;
+  double *cp_w = nullptr;
   // vertex work
   double *N_a = nullptr, *beta_a = nullptr, *beta_eff_a = nullptr, *F2a1 = nullptr;
   double *eta_3D_a = nullptr;   // nz x nV

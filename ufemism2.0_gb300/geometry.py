@@ -151,6 +151,81 @@ def channel_case(seed=0, nz=12, H=250.0, A=2e-17, res_scale=1.0, sliding="Schoof
     return mesh, ice, params
 
 
+# -- Schoof (2006) ice stream: the reference's SSA_icestream integrated test ---------------------
+def schoof2006_u(y, A=1e-18, H=2000.0, tantheta=-0.0003, L=150e3, m=1.0):
+    """Along-stream velocity of Schoof's (2006) ice stream on an inclined plane with a weak band of
+    width L along y = 0 (Schoof2006_icestream, src/UPSY/basic/analytical_solutions/
+    Schoof_SSA_solution.f90:15-64, n = 3): zero beyond the half-width W = L (m+1)^(1/m)."""
+    y = np.asarray(y, float)
+    f = -ICE_DENSITY * GRAV * H * tantheta
+    B = A ** (-1.0 / 3.0)
+    W = L * (m + 1.0) ** (1.0 / m)
+    a = np.abs(y / L)
+    ua = -2.0 * f ** 3 * L ** 4 / (B ** 3 * H ** 3)
+    ub = 0.25 * ((y / L) ** 4 - (m + 1.0) ** (4.0 / m))
+    uc = (-3.0 / ((m + 1.0) * (m + 4.0))) * (a ** (m + 4.0) - (m + 1.0) ** (1.0 + 4.0 / m))
+    ud = (3.0 / ((m + 1.0) ** 2 * (2.0 * m + 4.0))) * (a ** (2.0 * m + 4.0) - (m + 1.0) ** (2.0 + 4.0 / m))
+    ue = (-1.0 / ((m + 1.0) ** 3 * (3.0 * m + 4.0))) * (a ** (3.0 * m + 4.0) - (m + 1.0) ** (3.0 + 4.0 / m))
+    u = ua * (ub + uc + ud + ue)
+    return np.where(np.abs(y) > W, 0.0, u)
+
+
+def icestream_case(res=32e3, seed=0, nz=12):
+    """The SSA_icestream integrated test of the reference
+    (automated_testing/integrated_tests/idealised/SSA_icestream/config_0*_*km.cfg): an 800 km x 800 km
+    slab, 2000 m thick on a bed sloping at -0.0003 in x, uniform resolution `res` (32, 16, 8 or 4 km
+    in the reference's four runs), all grounded (sea level -10 km); SSA with the idealised
+    SSA_icestream sliding law, uniform A = 1e-18, eps0^2 = 1e-10, Picard relaxation 0.3 to 5e-8
+    (up to 5000 iterations), Krylov rtol 1e-7 / abstol 1e-5, u copied across the west and east
+    borders ('infinite_SSA_icestream'), u = 0 on the south and north borders, v = 0 on every border.
+    The flow factor is computed by the solve (choice_ice_rheology_Glen 'uniform'), so no A_flow is
+    passed.  Mesh: this package's generator at uniform resolution (the reference refines with its
+    own Ruppert scheme), so the error against Schoof's solution is comparable, not identical."""
+    L = 400e3
+    mesh = generate_mesh(-L, L, -L, L, lambda x, y: np.full(np.shape(x), float(res)), seed=seed, nz=nz)
+    x = mesh.V[:, 0]
+    Hi = np.full(mesh.nV, 2000.0)
+    Hb = -0.0003 * x                                   # calc_idealised_geometry_SSA_icestream
+    SL = np.full(mesh.nV, -10000.0)
+    Hs = surface_elevation(Hi, Hb, SL)
+    ice = dict(Hi=np.ascontiguousarray(Hi), Hs=np.ascontiguousarray(Hs), Hb=Hb, SL=SL,
+               fraction_gr_b=np.ones(mesh.nTri), mask_grounded_ice=np.ones(mesh.nV, np.int32))
+    params = abi.default_params(choice_sliding_law="idealised_SSA_icestream", visc_it_norm_dUV_tol=5e-8,
+                                visc_it_nit=5000, visc_it_relax=0.3, visc_eff_min=1e4,
+                                stress_balance_PETSc_rtol=1e-7, stress_balance_PETSc_abstol=1e-5,
+                                Glens_flow_law_epsilon_sq_0=1e-10, choice_ice_rheology_Glen="uniform",
+                                uniform_Glens_flow_factor=1e-18,
+                                BC_u_west="infinite_SSA_icestream", BC_u_east="infinite_SSA_icestream",
+                                BC_u_south="zero", BC_u_north="zero", BC_v_west="zero", BC_v_east="zero",
+                                BC_v_south="zero", BC_v_north="zero")
+    return mesh, ice, params
+
+
+def transect_values(mesh, values_a, x0=0.0, dy=1e3):
+    """A field on the vertices sampled along the south-north transect x = x0 of the reference's
+    transect output ('southnorth,dx=1e3'): linear interpolation in the triangle holding each
+    point.  Returns (y, values)."""
+    from scipy.spatial import cKDTree
+    ymin, ymax = mesh.V[:, 1].min(), mesh.V[:, 1].max()
+    y = np.arange(ymin, ymax + 0.5 * dy, dy)
+    pts = np.stack([np.full_like(y, x0), y], axis=1)
+    T = mesh.Tri - 1
+    tree = cKDTree(mesh.TriGC)
+    _, cand = tree.query(pts, k=min(12, mesh.nTri))
+    out = np.full(len(y), np.nan)
+    for i, p in enumerate(pts):
+        for t in np.atleast_1d(cand[i]):
+            a, b, c = mesh.V[T[t, 0]], mesh.V[T[t, 1]], mesh.V[T[t, 2]]
+            det = (b[0] - a[0]) * (c[1] - a[1]) - (c[0] - a[0]) * (b[1] - a[1])
+            l1 = ((b[0] - p[0]) * (c[1] - p[1]) - (c[0] - p[0]) * (b[1] - p[1])) / det
+            l2 = ((c[0] - p[0]) * (a[1] - p[1]) - (a[0] - p[0]) * (c[1] - p[1])) / det
+            l3 = 1.0 - l1 - l2
+            if min(l1, l2, l3) >= -1e-9:
+                out[i] = l1 * values_a[T[t, 0]] + l2 * values_a[T[t, 1]] + l3 * values_a[T[t, 2]]
+                break
+    return y, out
+
+
 def small_dome(seed=0, nz=12):
     """A ~1,000-vertex dome for tests the CPU oracle finishes in seconds."""
     return dome_case(seed=seed, nz=nz, res_scale=3.0)

@@ -189,8 +189,11 @@ class VelocitySolver:
         val = np.zeros(cap, np.float64)
         bb = np.zeros(2 * nT)
         nnz = C.c_int64()
+        up = _d(u_prev) if u_prev is not None else None
+        vp = _d(v_prev) if v_prev is not None else None
         self._check(self.lib.ufe_assemble_linearised(self.ctx, C.byref(params), *[abi.as_d(a) for a in args],
-                                                     None, None, C.byref(bc) if bc else None, abi.as_i(ptr),
+                                                     abi.as_d(up), abi.as_d(vp), C.byref(bc) if bc else None,
+                                                     abi.as_i(ptr),
                                                      abi.as_i(ind), abi.as_d(val), abi.as_d(bb), cap, C.byref(nnz)))
         n = nnz.value
         return CSR(2 * nT, 2 * nT, ptr, ind[:n].copy(), val[:n].copy(), 1), bb
