@@ -153,12 +153,16 @@ typedef struct {
   int32_t precision;                      /* enum ufe_precision, default UFE_PREC_FP64       */
   double  krylov_inner_rtol;              /* FP32 inner-solve reduction per refinement step, default 1e-2;
                                              the linear solve finishes in FP64 if the FP32 steps fail */
-  double  krylov_forcing;                 /* inexact Picard iteration: a linear solve also stops once its
-                                             residual is below krylov_forcing x its initial residual (the
-                                             residual of the current Picard iterate), so early Picard
-                                             iterations, far from the fixed point, are not solved to full
-                                             accuracy.  0 (default) = the fixed tolerance only, as the
-                                             reference's PETSc call; otherwise in (0, 1)                  */
+  double  krylov_forcing;                 /* two-phase inexact Picard iteration (no reference counterpart).
+                                             Phase 1: each linear solve also stops once its residual is
+                                             below krylov_forcing x its initial residual (the residual of
+                                             the current Picard iterate), so iterations far from the fixed
+                                             point are not solved to full accuracy.  When the change norm
+                                             first meets visc_it_norm_dUV_tol, phase 2 begins: solves to
+                                             the full Krylov tolerance, until the change norm meets the
+                                             tolerance again -- a small step from a loosely solved system
+                                             never ends the solve.  0 (default) = the fixed tolerance only,
+                                             as the reference's PETSc call; otherwise in (0, 1)            */
   /* calc_ice_rheology_Glen (constitutive_equation.f90:84-163), model_configuration.f90:594-601 */
   int32_t choice_ice_rheology_Glen;       /* enum ufe_rheology, default UFE_RHEOLOGY_INPUT                  */
   int32_t choice_enhancement_factor_transition; /* enum ufe_enhancement, default UFE_ENH_SEPARATE          */

@@ -28,13 +28,15 @@ def test_schoof_solution_closed_form(pkg):
 
 
 def test_oracle_icestream_32km_rmse(pkg, oracle_mod):
-    """The oracle on the 32 km run: converged within the reference's 5000 Picard iterations, RMSE
-    against Schoof's solution of the scoreboard's magnitude (400.42 m/yr)."""
+    """The oracle on the 32 km run: two velocity solves as the reference's short transient run
+    makes them (the second warm-started from the first), each converged within its 5000 Picard
+    iterations; RMSE against Schoof's solution of the scoreboard's magnitude (400.42 m/yr)."""
     mesh, ice, p = pkg.geometry.icestream_case(res=32e3)
     orc = oracle_mod.Oracle(mesh)
     s = pkg.new_ssa_state(mesh.nTri)
-    nv, na, st = orc.solve_SSA(ice, s, p)
-    assert st["status"] == 0 and nv < 5000
+    for _ in range(2):
+        nv, na, st = orc.solve_SSA(ice, s, p)
+        assert st["status"] == 0 and nv < 5000
     rmse, umax = _rmse(pkg, mesh, orc.apply("MAP_B_A", s["u_b"]))
     assert 250.0 < rmse < 650.0, rmse
     assert 1000.0 < umax < 2400.0
@@ -98,16 +100,19 @@ def test_gpu_icestream_matches_oracle_32km(pkg, oracle_mod, gpu_lib):
 
 @pytest.mark.gpu
 def test_gpu_icestream_rmse_falls_with_resolution(pkg, gpu_lib):
-    """The reference's four runs (32, 16, 8, 4 km) on the GPU with their own settings: the RMSE
-    against Schoof's solution falls with resolution, from the scoreboard's ~400 m/yr at 32 km to
-    ~100 m/yr at 4 km."""
+    """The reference's four runs (32, 16, 8, 4 km) on the GPU with their own settings, each as the
+    reference's short transient makes its velocity solves (a cold solve, then one warm-started
+    from it): the RMSE against Schoof's solution falls with resolution, from the scoreboard's
+    ~400 m/yr at 32 km to ~100 m/yr at 4 km.  (From a cold start the Picard iteration at 4 km stops
+    at its tolerance while still ~14% below the fixed point; the warm solve finishes the approach.)"""
     rmses = []
     for res in (32e3, 16e3, 8e3, 4e3):
         mesh, ice, p = pkg.geometry.icestream_case(res=res)
         with pkg.VelocitySolver(mesh) as g:
             s = pkg.new_ssa_state(mesh.nTri)
-            nv, na, st = g.solve_SSA(ice, s, p)
-            assert st["status"] == 0 and nv < 5000
+            for _ in range(2):
+                nv, na, st = g.solve_SSA(ice, s, p)
+                assert st["status"] == 0 and nv < 5000
             rmses.append(_rmse(pkg, mesh, g.apply("MAP_B_A", s["u_b"]))[0])
     assert all(b < a for a, b in zip(rmses, rmses[1:])), rmses
     assert 250.0 < rmses[0] < 650.0 and 40.0 < rmses[-1] < 200.0, rmses

@@ -121,13 +121,17 @@ def test_thermo_step_matches_oracle(pkg, oracle_mod, gpu_lib, cp, k, glbc):
     with pkg.ColumnSolver() as s:
         T_g, n_g = s.thermo_step(p, zeta, cols)
     assert n_g == n_o
-    robin = flags == 1
+    robin, retried = flags == 1, flags == 2
+    plain = ~robin & ~retried
     if cp == "uniform":
-        # same arithmetic, same roundings, except erf/exp in the Robin profile
-        assert np.array_equal(T_g[~robin], T_o[~robin])
+        # same arithmetic, same roundings, for columns solved at the full step
+        assert np.array_equal(T_g[plain], T_o[plain])
     else:
         # exp (Ritz conductivity) is the device's: last-bit differences, carried through the solve
-        np.testing.assert_allclose(T_g[~robin], T_o[~robin], rtol=0, atol=1e-9)
+        np.testing.assert_allclose(T_g[plain], T_o[plain], rtol=0, atol=1e-9)
+    # the dt-halving retries evaluate the Thomas recurrences as warp-parallel scans (reassociated
+    # sums), and the Robin profile uses the device's erf/exp: within 1e-9 K
+    np.testing.assert_allclose(T_g[retried], T_o[retried], rtol=0, atol=1e-9)
     np.testing.assert_allclose(T_g[robin], T_o[robin], rtol=0, atol=1e-9)
 
 
@@ -178,7 +182,7 @@ def test_heat_equation_on_mesh_matches_oracle(pkg, oracle_mod, gpu_lib, uniform)
     with pkg.VelocitySolver(mesh, operators=ops) as s:   # the oracle's operators: identical upwind terms
         T_g, n_g = s.solve_3D_heat_equation(fields, p)
     assert n_g == n_o
-    if uniform:
+    if uniform and n_o == 0:
         assert np.array_equal(T_g, T_o)
     else:
         np.testing.assert_allclose(T_g, T_o, rtol=0, atol=1e-9)
@@ -209,7 +213,8 @@ def test_heat_resident_stepping_matches_oracle(pkg, oracle_mod, gpu_lib):
         n_tot, ms = s.heat_step_resident(p, 5)
         T_g = s.heat_download()
     assert n_tot == 0 and ms > 0
-    assert np.array_equal(T_g, T)
+    # bit-exact unless a column needed the dt-halving retries (warp-parallel recurrences, < 1e-9 K)
+    np.testing.assert_allclose(T_g, T, rtol=0, atol=1e-9)
 
 
 @pytest.mark.gpu

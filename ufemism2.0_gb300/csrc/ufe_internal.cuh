@@ -70,7 +70,7 @@ struct PicardScalars {
   int32_t n_refine;
   int32_t prev_total_its;
   int32_t phase;       // inexact Picard (krylov_forcing > 0): 0 while forced, 1 once exact solves verify
-  int32_t pad;
+  int32_t nconv0;      // consecutive forced iterations whose change norm met the tolerance
   double hist[kHistMax * kHistCols];
 };
 

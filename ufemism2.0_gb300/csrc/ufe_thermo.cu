@@ -320,13 +320,39 @@ __global__ void __launch_bounds__(128) k_heat_columns(In in, ZOps z, Consts c, V
 // The dt-halving retries (:161-239), one warp per listed column.  Per column the row
 // coefficients that do not depend on dt or on the current profile (c_ddzeta, c_d2dzeta2, the
 // off-diagonals, the advection and heating terms) are computed once, one row per lane.  Per dt
-// level the matrix part of the Thomas elimination (w = a / b', b' = b - w c) is done once: it is
-// the same in every substep, so hoisting it changes no value.  Per substep the lanes build the
-// right-hand side in parallel, lane 0 runs the two short recurrences (d' and the back
-// substitution), and the lanes clamp, mix and check the rows in parallel.
-constexpr int kRetryArrays = 14;
+// level the matrix part of the Thomas elimination (w = a / b', b' = b - w c) is done once by lane 0:
+// it is the same in every substep, so hoisting it changes no value.  Per substep the two
+// recurrences of the solve -- the forward sweep d'_k = d_k - w_k d'_{k-1} and the back substitution
+// x_k = (d'_k - c_k x_{k+1}) / b'_k -- are first-order affine recurrences, evaluated across the warp
+// as parallel prefix compositions of affine maps y -> a + b y (Kogge-Stone, 5 shuffle steps; rows
+// beyond 32 are composed sequentially inside each lane first).  The back substitution is split as
+// x_k = A_k + B_k x_base, so both basal conditions of a subgrid grounding-line column come from one
+// scan.  Divisions by b'_k and dt become multiplications by reciprocals formed once per dt level
+// (FP64 division is a long dependent sequence on GB300).  The scans reassociate the sums and the
+// reciprocals round differently, so retried columns differ from the sequential recurrence in the
+// last bits (well below 1e-9 K); the lanes then clamp, mix and check the rows in parallel.
+constexpr int kRetryArrays = 16;
 constexpr int kRetryWarps = 1;
 constexpr int kRetryBlocks = 4 * 152;
+
+struct Affine {   // y -> a + b y
+  double a, b;
+};
+// g after f
+__device__ __forceinline__ Affine compose(const Affine &g, const Affine &f) {
+  return Affine{fma(g.b, f.a, g.a), g.b * f.b};
+}
+// Inclusive scan over the lanes in increasing (up = true) or decreasing lane order: lane l gets
+// M_l o M_{l-1} o ... o M_0 (up) or M_l o M_{l+1} o ... o M_31 (down).
+__device__ __forceinline__ Affine warp_scan(Affine m, int lane, bool up) {
+#pragma unroll
+  for (int off = 1; off < 32; off <<= 1) {
+    const double qa = up ? __shfl_up_sync(0xffffffffu, m.a, off) : __shfl_down_sync(0xffffffffu, m.a, off);
+    const double qb = up ? __shfl_up_sync(0xffffffffu, m.b, off) : __shfl_down_sync(0xffffffffu, m.b, off);
+    if (up ? lane >= off : lane + off < 32) m = compose(m, Affine{qa, qb});
+  }
+  return m;
+}
 
 template <class In>
 __global__ void __launch_bounds__(32 * kRetryWarps) k_heat_retry(In in, ZOps z, Consts c, VertexFields vf,
@@ -336,10 +362,12 @@ __global__ void __launch_bounds__(32 * kRetryWarps) k_heat_retry(In in, ZOps z, 
   extern __shared__ double sm[];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int nz = z.nz;
+  const int R = (nz + 31) / 32;                      // rows per lane: [lane*R, lane*R + R)
+  const int k0 = lane * R, k1 = min(k0 + R, nz);
   double *base = sm + (size_t)warp * kRetryArrays * nz;
   double *C1 = base, *C2 = C1 + nz, *UDX = C2 + nz, *VDY = UDX + nz, *PHI = VDY + nz, *A = PHI + nz,
-         *Cc = A + nz, *Bp = Cc + nz, *W = Bp + nz, *D = W + nz, *X = D + nz, *PMP = X + nz, *XG = PMP + nz,
-         *XF = XG + nz;
+         *Cc = A + nz, *Bp = Cc + nz, *W = Bp + nz, *D = W + nz, *X = D + nz, *PMP = X + nz, *NB = PMP + nz,
+         *XB = NB + nz, *SB = XB + nz, *RB = SB + nz;
   const int32_t n = cnt->n_retry;
   const int warps_total = gridDim.x * kRetryWarps;
   for (int32_t j = blockIdx.x * kRetryWarps + warp; j < n; j += warps_total) {
@@ -407,41 +435,62 @@ __global__ void __launch_bounds__(32 * kRetryWarps) k_heat_retry(In in, ZOps z, 
         Bp[kb] = 1.0 - wgt * cprev;
       }
       __syncwarp();
+      // per row for this dt: 1 / b'_k and the back
+      // substitution's slope, x_k = d'_k / b'_k - (c_k / b'_k) x_{k+1}
+      for (int k = lane; k < nz; k += 32) {
+        const double rb = 1.0 / Bp[k];
+        RB[k] = rb;
+        NB[k] = (k < kb) ? -(Cc[k] * rb) : 0.0;
+      }
+      __syncwarp();
       const int nsub = 1 << (it_dt - 1);
       bool ok = true;
       for (int sub = 0; sub < nsub; ++sub) {
+        // right-hand side (rows 0 .. nz-2) and the basal row's value from the current profile
         for (int k = lane; k < nz - 1; k += 32)
-          D[k] = (k == 0) ? fmin(Ts, kT0) : X[k] / dt - UDX[k] - VDY[k] + PHI[k];
+          D[k] = (k == 0) ? fmin(Ts, kT0) : X[k] * inv_dt - UDX[k] - VDY[k] + PHI[k];
+        const double d_gr = fmin(pmp_b, X[nz - 2] - dzeta_b * Q / (dzzb * Kb));
         __syncwarp();
-        if (lane == 0) {
-          double dprev = D[0];
-          for (int k = 1; k < nz - 1; ++k) {
-            dprev = D[k] - W[k] * dprev;
-            D[k] = dprev;
-          }
-          // back substitution for one basal value, unclamped x into out[]
-          auto backward = [&](double d_b, double *out) {
-            const double dl = d_b - W[kb] * dprev;
-            double x = dl / Bp[kb];
-            out[kb] = x;
-            for (int k = nz - 2; k >= 0; --k) {
-              x = (D[k] - Cc[k] * x) / Bp[k];
-              out[k] = x;
-            }
-          };
-          const double d_gr = fmin(pmp_b, X[nz - 2] - dzeta_b * Q / (dzzb * Kb));
-          if (two_solves) {
-            backward(pmp_b, XF);
-            backward(d_gr, XG);
-          } else {
-            backward(grounded ? d_gr : pmp_b, XG);
-          }
+        // forward sweep over rows 0 .. nz-2: d'_k = D_k - W_k d'_{k-1} (row 0: the constant D_0)
+        Affine mine{0.0, 1.0};
+        for (int k = k0; k < min(k1, kb); ++k)
+          mine = compose(Affine{D[k], k == 0 ? 0.0 : -W[k]}, mine);
+        const Affine pre = warp_scan(mine, lane, true);
+        double y = __shfl_up_sync(0xffffffffu, pre.a, 1);   // d' of the row before this lane's first
+        if (lane == 0) y = 0.0;
+        for (int k = k0; k < min(k1, kb); ++k) {
+          y = (k == 0) ? D[0] : fma(-W[k], y, D[k]);
+          D[k] = y;
         }
         __syncwarp();
+        const double dprev = D[kb - 1];
+        // back substitution over rows nz-2 .. 0 as x_k = XB_k + SB_k x_base: each lane composes its
+        // rows (m_k: x_{k+1} -> x_k), the suffix scan gives the map from x_base to each lane's rows
+        Affine mb{0.0, 1.0};
+        for (int k = min(k1, kb) - 1; k >= k0; --k) mb = compose(Affine{D[k] * RB[k], NB[k]}, mb);
+        const Affine suf = warp_scan(mb, lane, false);
+        double sa = __shfl_down_sync(0xffffffffu, suf.a, 1), sb = __shfl_down_sync(0xffffffffu, suf.b, 1);
+        if (lane == 31) { sa = 0.0; sb = 1.0; }
+        for (int k = min(k1, kb) - 1; k >= k0; --k) {   // (sa, sb): x_base -> x_{k+1}
+          const Affine r = compose(Affine{D[k] * RB[k], NB[k]}, Affine{sa, sb});
+          XB[k] = r.a;
+          SB[k] = r.b;
+          sa = r.a;
+          sb = r.b;
+        }
+        __syncwarp();
+        // basal values and the rows' solutions, clamped (and mixed for the subgrid condition)
+        const double x_gr = ((grounded ? d_gr : pmp_b) - W[kb] * dprev) * RB[kb];
+        const double x_fl = (pmp_b - W[kb] * dprev) * RB[kb];
+        const double x_sel = two_solves ? (d_gr - W[kb] * dprev) * RB[kb] : x_gr;
         bool bad = false;
         for (int k = lane; k < nz; k += 32) {
-          double v = fmin(XG[k], PMP[k]);
-          if (two_solves) v = fr * v + (1.0 - fr) * fmin(XF[k], PMP[k]);
+          const double xg = (k == kb) ? x_sel : fma(SB[k], x_sel, XB[k]);
+          double v = fmin(xg, PMP[k]);
+          if (two_solves) {
+            const double xf = (k == kb) ? x_fl : fma(SB[k], x_fl, XB[k]);
+            v = fr * v + (1.0 - fr) * fmin(xf, PMP[k]);
+          }
           X[k] = v;
           bad |= unstable_value(v);
         }

@@ -185,6 +185,7 @@ __global__ void k_prologue(int nV, int nTri, int nz, OpRow ab, const double *Hi,
     p.n_refine = 0;
     p.prev_total_its = 0;
     p.phase = 0;
+    p.nconv0 = 0;
     p.active = 1;
     KrylovScalars k;
     memset(&k, 0, sizeof(k));
@@ -527,7 +528,9 @@ __global__ void k_assemble(AssembleArgs a, PhysParams q, CondArg cond) {
     s.rnorm0 = rnorm0;
     // the reference's fixed tolerance (KSPSetTolerances, petsc_basic.f90:110), or for an inexact
     // Picard iteration krylov_forcing times this Picard iterate's own residual, if larger
-    const double forcing = (a.ps && a.ps->phase != 0) ? 0.0 : a.forcing;
+    // the forced solves' reduction also tightens with the last Picard change norm (its square root,
+    // the relative step), so forced steps near convergence are close to exact ones
+    const double forcing = !a.ps ? a.forcing : (a.ps->phase != 0) ? 0.0 : fmin(a.forcing, sqrt(a.ps->L2));
     s.ttol = fmax(fmax(a.rtol * rnorm0, a.abstol), forcing * dp);
     s.it = 0;
     s.max_it = a.max_it;
@@ -692,12 +695,13 @@ __device__ void picard_step(PicardScalars *psp, KrylovScalars *ks, double r1, do
   }
   if (isnan(p.L2)) { p.status = UFE_ERR_NAN; stop = 1; }
   int converged = p.L2 < q.picard_tol;
-  // inexact Picard: the first time the change norm meets the tolerance, the forced (inexact)
-  // linear solves end and the iteration goes on with solves to the full Krylov tolerance, until
-  // the change norm meets the tolerance after such a solve -- a small step from a loosely solved
-  // system is not taken as convergence
-  if (!stop && converged && q.inexact && p.phase == 0) {
-    p.phase = 1;
+  // inexact Picard: once the change norm has met the tolerance in two forced iterations in a row
+  // (one tiny step from a loosely solved system does not count), the forced linear solves end and
+  // the iteration goes on with solves to the full Krylov tolerance, until the change norm meets
+  // the tolerance after such a solve
+  if (!stop && q.inexact && p.phase == 0) {
+    p.nconv0 = converged ? p.nconv0 + 1 : 0;
+    if (converged && p.nconv0 >= 2) p.phase = 1;
     converged = 0;
   }
   if (!stop && !converged && p.it > q.visc_it_nit) {

@@ -81,13 +81,14 @@ def dome_resolution(band=140e3, ramp=200e3, fine=10e3, coarse=40e3, R=500e3):
     return res
 
 
-def dome_case(seed=0, nz=12, L=800e3, res_scale=1.0, A=1e-16, beta_sq=1e4):
-    """Config 0 (or a coarser copy with res_scale > 1 for quick tests)."""
+def dome_case(seed=0, nz=12, L=800e3, res_scale=1.0, A=1e-16, beta_sq=1e4, H0=3000.0, R=500e3):
+    """Config 0 (or a coarser copy with res_scale > 1 for quick tests; H0, R and beta_sq vary it
+    for the learned start's training set)."""
     res = dome_resolution(band=140e3 * min(res_scale, 1.0) if res_scale < 1 else 140e3,
-                          fine=10e3 * res_scale, coarse=40e3 * res_scale)
+                          fine=10e3 * res_scale, coarse=40e3 * res_scale, R=R)
     mesh = generate_mesh(-L / 2, L / 2, -L / 2, L / 2, res, seed=seed, nz=nz)
     x, y = mesh.V[:, 0], mesh.V[:, 1]
-    Hi = np.ascontiguousarray(dome_thickness(x, y))
+    Hi = np.ascontiguousarray(dome_thickness(x, y, H0=H0, R=R))
     Hb = np.zeros(mesh.nV)
     SL = np.full(mesh.nV, -10000.0)   # no ocean (idealised_geometries.f90:140)
     Hs = np.ascontiguousarray(surface_elevation(Hi, Hb, SL))
