@@ -846,6 +846,46 @@ def run_dome(args):
         print(json.dumps(line))
 
 
+def run_icestream(args):
+    """The reference's SSA_icestream integrated test on the GPU: for each of its four resolutions a
+    cold velocity solve and one warm-started from it (as its short transient run makes them), the
+    RMSE of u on the south-north transect against Schoof's (2006) analytic ice stream, the
+    reference scoreboard's figures beside it, and the GPU against the oracle on the 32 km run."""
+    pkg = __graft_entry__.load_package()
+    pkg.build()
+    scoreboard = {32e3: 400.42, 4e3: 101.21}   # RMSE_32km, RMSE_4km (it_ideal_SSA_icestream_*.xml)
+    rows = []
+    for res in (32e3, 16e3, 8e3, 4e3):
+        mesh, ice, p = pkg.geometry.icestream_case(res=res)
+        with pkg.VelocitySolver(mesh) as g:
+            s = pkg.new_ssa_state(mesh.nTri)
+            its, ms = [], 0.0
+            for _ in range(2):
+                nv, na, st = g.solve_SSA(ice, s, p)
+                its.append([nv, na])
+                ms += st["device_ms"]
+            ua = g.apply("MAP_B_A", s["u_b"])
+        y, ut = pkg.geometry.transect_values(mesh, ua)
+        an = pkg.geometry.schoof2006_u(y)
+        rows.append({"resolution_km": res / 1e3, "nV": mesh.nV, "picard_krylov_its": its, "device_ms": round(ms, 1),
+                     "rmse_m_per_yr": round(float(np.sqrt(np.nanmean((ut - an) ** 2))), 2),
+                     "u_max_transect": round(float(np.nanmax(ut)), 1), "u_max_schoof": round(float(an.max()), 1),
+                     "reference_scoreboard_rmse": scoreboard.get(res)})
+    # GPU against the oracle, 32 km, Krylov to 1e-12
+    mesh, ice, p = pkg.geometry.icestream_case(res=32e3)
+    p = _with(pkg, p, stress_balance_PETSc_rtol=1e-12, stress_balance_PETSc_abstol=0.0)
+    orc = _oracle().Oracle(mesh)
+    a, b = pkg.new_ssa_state(mesh.nTri), pkg.new_ssa_state(mesh.nTri)
+    with pkg.VelocitySolver(mesh) as g:
+        nvg, _, _ = g.solve_SSA(ice, a, p)
+    nvo, _, _ = orc.solve_SSA(ice, b, p)
+    ug, uo = np.r_[a["u_b"], a["v_b"]], np.r_[b["u_b"], b["v_b"]]
+    print(json.dumps({"workload": "SSA_icestream integrated test (Schoof 2006), 800 km square, 32/16/8/4 km",
+                      "runs": rows, "gpu_vs_oracle_32km": {"rel_l2": float("%.3g" % (np.linalg.norm(ug - uo)
+                                                                                       / np.linalg.norm(uo))),
+                                                           "picard_its_gpu_oracle": [nvg, nvo]}}))
+
+
 ENSEMBLE_WORKLOAD = ("ensemble of SSA solves on meshes of uneven size (log-uniform vertex counts), each its own "
                      "geometry of the learned-start ensemble family; autotuned rows per warp per mesh; members "
                      "solved one after another vs side by side (ufe_ensemble_solve)")
@@ -1183,6 +1223,45 @@ def run_probe(args):
     os.environ["UFE_NO_GRAPH"] = "1"
     pkg = __graft_entry__.load_package()
     pkg.build()
+    if args.probe == "solve":
+        # one channel solve of the headline's kernel mix (double-word Krylov, inexact Picard) in
+        # host-loop mode, after one warm-up solve: the launch list names every kernel of the path
+        mesh, ice, params = pkg.geometry.channel_case(seed=0)
+        p = _with(pkg, params, precision=pkg.abi.PREC_FP32_PAIR, krylov_forcing=args.forcing,
+                  visc_it_nit=args.picard_nit)
+        with pkg.VelocitySolver(mesh) as s:
+            s.ice_upload(ice)
+            for _ in range(2):
+                st = s.solve_resident(p, diva=True, cold_start=True)
+        print(json.dumps({"probe": "solve", "picard_its": st["n_visc_its"], "krylov_its": st["n_Axb_its"],
+                          "device_ms": round(st["device_ms"], 1)}))
+        return
+    if args.probe == "big":
+        # the largest member size of the mixed ensemble (400k vertices; the Krylov matrix, ~0.25 GB,
+        # exceeds L2): one DIVA Picard iteration in host-loop mode with the Krylov solve capped at
+        # 200 iterations, then the persistent kernels timed by CUDA events over 200 iterations
+        mesh = pkg.geometry.mixed_ensemble_mesh(args.big_nv, seed=7)
+        ice, p0 = pkg.geometry.mixed_ensemble_member(mesh, 7)
+        out = {"nV": mesh.nV, "nTri": mesh.nTri}
+        with pkg.VelocitySolver(mesh) as s:
+            s.ice_upload(ice)
+            for name, prec in (("fp64", pkg.abi.PREC_FP64), ("fp32_pair", pkg.abi.PREC_FP32_PAIR)):
+                p = _with(pkg, p0, visc_it_nit=0, krylov_max_it=200, precision=prec)
+                st = s.solve_resident(p, diva=True, cold_start=True)
+                us_it = s.profile_krylov_persistent(prec, 200)
+                us3, (nb, nnzb) = s.profile_krylov_kernels(pkg.abi.PREC_FP64, repeats=20)
+                bytes_it = 2 * (nnzb * 36 + (nb + 1) * 4 + 2 * 16 * nb) + 15 * 16 * nb
+                bytes_p = nnzb * (32 + 4) + (nb + 1) * 4 + nb * 7 * 16
+                out[name] = {"krylov_its": st["n_Axb_its"], "us_per_iteration": round(us_it, 2),
+                             "algorithmic_bytes_per_iteration": int(bytes_it),
+                             "achieved_gbs": round(bytes_it / (us_it * 1e-6) / 1e9, 1)}
+                out["three_kernel_fp64_us"] = [round(float(x), 2) for x in us3]
+                out["k_p_spmv_fp64_gbs"] = round(bytes_p / (us3[0] * 1e-6) / 1e9, 1)
+                out["blocks_2x2"] = int(nnzb)
+        peaks, kind = measured_peaks()
+        out["hbm_peak_gbs"] = peaks.get("hbm_gbs")
+        print(json.dumps(out))
+        return
     if args.probe in ("krylov", "krylov_pair"):
         mesh, ice, params = pkg.geometry.channel_case(seed=0)
         p = _with(pkg, params, visc_it_nit=0, krylov_max_it=200,
@@ -1216,7 +1295,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
-    ap.add_argument("--forcing", type=float, default=0.03,
+    ap.add_argument("--forcing", type=float, default=0.1,
                     help="krylov_forcing of the inexact-Picard path (the early linear solves' residual reduction)")
     ap.add_argument("--picard-nit", type=int, default=200,
                     help="visc_it_nit of every channel path (a limit only: the tolerance ends the solves)")
@@ -1230,7 +1309,7 @@ def main():
     ap.add_argument("--dome-tight", type=float, default=1e-15, help="the tight Picard tolerance of --workload dome")
     ap.add_argument("--dome-ref-tol", type=float, default=1e-16, help="Picard tolerance of the dome's reference solution")
     ap.add_argument("--dome-epochs", type=int, default=200)
-    ap.add_argument("--workload", default="diva", choices=["diva", "thermo", "learned", "ensemble", "mixed", "dome"],
+    ap.add_argument("--workload", default="diva", choices=["diva", "thermo", "learned", "ensemble", "mixed", "dome", "icestream"],
                     help="diva: the headline velocity solve; thermo: the batched column thermodynamics; "
                          "learned: the learned Picard start on the SSA ensemble")
     ap.add_argument("--ens-members", type=int, default=12)
@@ -1248,7 +1327,8 @@ def main():
     ap.add_argument("--learned-err-members", type=int, default=8,
                     help="held-out members also solved to 1e-8 as the reference for the velocity errors")
     ap.add_argument("--thermo-steps", type=int, default=100, help="time steps per thermodynamics run")
-    ap.add_argument("--probe", choices=["krylov", "krylov_pair", "gnn"], default=None,
+    ap.add_argument("--big-nv", type=int, default=400_000, help="vertices of the --probe big mesh")
+    ap.add_argument("--probe", choices=["krylov", "krylov_pair", "gnn", "big", "solve"], default=None,
                     help="run one small fixed case of a kernel family for a profiler capture and exit")
     args = ap.parse_args()
     if args.probe:
@@ -1259,6 +1339,8 @@ def main():
         run_learned(args)
     elif args.workload == "dome":
         run_dome(args)
+    elif args.workload == "icestream":
+        run_icestream(args)
     elif args.workload == "ensemble":
         run_ensemble(args)
     elif args.workload == "mixed":
