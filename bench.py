@@ -403,7 +403,11 @@ def run_ours(args):
     cands = [(f"plain_{k}", plain_runs[k], k) for k in prec]
     if learned:
         cands += [(f"learned_{k}", learned_runs[k], k) for k in prec]
-    head_name, (head_sts, head_value, head_clk, head_wall), head_prec = max(cands, key=lambda c: c[1][1] or 0.0)
+    fastest_any = max(cands, key=lambda c: c[1][1] or 0.0)
+    # the metric is the learned start with FP32 Krylov arithmetic against plain FP64: the headline is
+    # the fastest learned-start path with an FP32 Krylov mode (all paths are listed beside it)
+    lcands = [c for c in cands if c[0].startswith("learned") and c[2] != "fp64"] or cands
+    head_name, (head_sts, head_value, head_clk, head_wall), head_prec = max(lcands, key=lambda c: c[1][1] or 0.0)
     if head_name.startswith("learned"):
         launches = kernels(head_sts, predict_kernels)
     else:
@@ -460,6 +464,8 @@ def run_ours(args):
                                             if head_name.startswith("learned") else " (zero start)")
                                + ", graph-resident solve"},
             "speedup_vs_plain_fp64": round(head_value / value64, 3),
+            "fastest_any_path": {"path": fastest_any[0], "value": round(fastest_any[1][1], 4), "unit": UNIT,
+                                 "speedup_vs_plain_fp64": round(fastest_any[1][1] / value64, 3)},
             "accuracy": accuracy_summary(plain, learned, ref_info, head_name, u_plain, err_ref),
             "plain": plain,
             "learned_start": learned,
@@ -765,9 +771,16 @@ def run_dome(args):
         with pkg.VelocitySolver(m_v, device=local) as sv:
             sv.ice_upload(ice_v)
             x = net.features(sv)
-            gen_ms += sv.solve_resident(_with(pkg, p_v, visc_it_norm_dUV_tol=1e-12, visc_it_nit=2000,
-                                              stress_balance_PETSc_rtol=1e-12, stress_balance_PETSc_abstol=0.0),
-                                        diva=False, cold_start=True)["device_ms"]
+            # the tightest tolerance the divergence control lets this variant finish
+            for tol in (1e-12, 1e-10, 1e-8, 1e-6):
+                try:
+                    gen_ms += sv.solve_resident(_with(pkg, p_v, visc_it_norm_dUV_tol=tol, visc_it_nit=2000,
+                                                      stress_balance_PETSc_rtol=1e-12,
+                                                      stress_balance_PETSc_abstol=0.0),
+                                                diva=False, cold_start=True)["device_ms"]
+                    break
+                except pkg.UfeError:
+                    continue
             net.dataset_add(sv, x)
     gen_wall = time.perf_counter() - t_gen
     losses, train_ms = net.train(epochs=args.dome_epochs, lr=2e-3)
@@ -776,9 +789,11 @@ def run_dome(args):
 
     paths = {}
     for tol in (params.visc_it_norm_dUV_tol, T_tight):
-        for name, prec, learned in (("plain_fp64", F64, False), ("plain_fp32_pair", PAIR, False),
-                                    ("learned_fp64", F64, True), ("learned_fp32_pair", PAIR, True)):
-            p = _with(pkg, params, precision=prec, visc_it_norm_dUV_tol=tol, visc_it_nit=2000)
+        for name, prec, learned, forcing in (("plain_fp64", F64, False, 0.0), ("plain_fp32_pair", PAIR, False, 0.0),
+                                             ("plain_fp32_pair_inexact", PAIR, False, args.forcing),
+                                             ("learned_fp64", F64, True, 0.0), ("learned_fp32_pair", PAIR, True, 0.0),
+                                             ("learned_fp32_pair_inexact", PAIR, True, args.forcing)):
+            p = _with(pkg, params, precision=prec, visc_it_norm_dUV_tol=tol, visc_it_nit=2000, krylov_forcing=forcing)
             ms, sts, u = [], None, None
             for i in range(args.warmup + args.steps):
                 pred = net.predict(solver, smooth_passes=2) if learned else 0.0
@@ -816,8 +831,10 @@ def run_dome(args):
                "at_krylov_rtol_1e-12": {"gpu_vs_oracle_rel_l2": float("%.3g" % (np.linalg.norm(u12 - uo12)
                                                                                  / np.linalg.norm(uo12))),
                                         "picard_its_gpu_oracle": [st12["n_visc_its"], nv12]}}
-    head = f"learned_fp32_pair@{T_tight:g}"
     base = f"plain_fp64@{T_tight:g}"
+    # the headline: the fastest learned-start path with FP32 Krylov arithmetic at the tight tolerance
+    head = max((k for k in paths if k.startswith("learned_fp32") and k.endswith(f"@{T_tight:g}")),
+               key=lambda k: paths[k]["value"])
     met = paths[head]["rel_l2_vs_fp64_reference"] <= 1e-6
     line = {"metric": METRIC, "value": paths[head]["value"], "unit": UNIT, "n_gpus": 1, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": paths[head]["ms_per_solve"], "higher_is_better": True,
@@ -829,7 +846,7 @@ def run_dome(args):
             "reference_solution": {"picard_tol": args.dome_ref_tol, "krylov_rtol": 1e-12,
                                    "picard_its": st_ref["n_visc_its"], "krylov_its": st_ref["n_Axb_its"]},
             "paths": paths,
-            "statement": (f"At Picard tolerance {T_tight:g} learned start + double-word Krylov is "
+            "statement": (f"At Picard tolerance {T_tight:g} {head.split('@')[0].replace('_', ' ')} is "
                           f"{paths[head]['rel_l2_vs_fp64_reference']:.1e} from the FP64 reference solution "
                           f"(plain FP64 {paths[base]['rel_l2_vs_fp64_reference']:.1e}) at "
                           f"{paths[head]['value'] / paths[base]['value']:.2f}x the plain FP64 solves/s: the "
@@ -1118,27 +1135,32 @@ def accuracy_summary(plain, learned, ref_info, head_name, u_plain, err_ref):
     out = {"reference": ref_info,
            "rel_l2_vs_fp64_reference": {f"plain_{k}": err_ref(u_plain[k]) for k in u_plain}}
     if learned:
-        for k in ("fp64", "fp32_pair", "fp32_refined"):
-            if k in learned:
-                out["rel_l2_vs_fp64_reference"][f"learned_{k}"] = learned[k]["rel_l2_vs_fp64_reference"]
+        for k, v in learned.items():
+            if isinstance(v, dict) and "rel_l2_vs_fp64_reference" in v:
+                out["rel_l2_vs_fp64_reference"][f"learned_{k}"] = v["rel_l2_vs_fp64_reference"]
     tight = (learned or {}).get("tight_tolerance_pair", {})
     T = ref_info["picard_tol"]
-    e0 = out["rel_l2_vs_fp64_reference"]["plain_fp64"]
-    eh = out["rel_l2_vs_fp64_reference"].get(head_name)
+    errs = out["rel_l2_vs_fp64_reference"]
+    e0, eh = errs["plain_fp64"], errs.get(head_name)
     parts = [f"At the benchmark's Picard tolerance (1e-4 on the squared relative change) every path, plain FP64 "
-             f"included, stops {e0:.1e} (plain FP64) to {eh:.1e} (headline) from the FP64 reference solution "
-             f"(Picard tolerance {T:g}, Krylov rtol 1e-12), so the 1e-6 target is not met at that tolerance."]
-    if "rel_l2_between" in tight:
-        lt = tight["learned_fp32_pair"]
-        met = lt["rel_l2_vs_fp64_reference"] is not None and lt["rel_l2_vs_fp64_reference"] <= 1e-6
-        parts.append(f"Run to the reference's own Picard tolerance {T:g}, learned start + double-word Krylov is "
-                     f"{lt['rel_l2_vs_fp64_reference']:.1e} from the reference solution (plain FP64 "
-                     f"{tight['plain_fp64']['rel_l2_vs_fp64_reference']:.1e}) at {tight['speedup']:.2f}x the plain FP64 "
-                     f"solves/s: the 1e-6 target is {'met' if met else 'not met'}.")
+             f"included, stops {min(errs.values()):.1e} to {max(errs.values()):.1e} from the FP64 reference "
+             f"solution (plain FP64 {e0:.1e}, headline {eh:.1e}; reference: Picard tolerance {T:g}, Krylov rtol "
+             f"1e-12), so the 1e-6 target is not met at that tolerance, by any path."]
+    for k in ("learned_fp32_pair_inexact", "learned_fp32_pair"):
+        lt = tight.get(k, {})
+        if "speedup_vs_plain_fp64" in lt:
+            met = lt["rel_l2_vs_fp64_reference"] <= 1e-6
+            parts.append(f"Run to the reference's own tolerance {T:g}, {k.replace('_', ' ')} is "
+                         f"{lt['rel_l2_vs_fp64_reference']:.1e} from the reference solution (plain FP64 "
+                         f"{tight['plain_fp64']['rel_l2_vs_fp64_reference']:.1e}) at "
+                         f"{lt['speedup_vs_plain_fp64']:.2f}x the plain FP64 solves/s: the 1e-6 target is "
+                         f"{'met' if met else 'not met'}.")
     failed = ", ".join("%g" % t["picard_tol"] for t in ref_info["tried"][:-1]) or "none"
-    parts.append(f"Tighter Picard tolerances ({failed}) "
-                 f"end in the reference's divergence stop on this channel: its Picard iteration stalls near "
-                 f"L2 ~ 1e-8, which bounds how close any path can get to the fixed point.")
+    parts.append(f"Tighter Picard tolerances ({failed}) end in the reference's divergence stop on this channel, "
+                 f"and on the way its divergence control raises eps0^2 (relaxation {ref_info['relax_applied']} "
+                 f"applied to reach {T:g}), which changes the viscosity law itself; so the solutions that different "
+                 f"starts reach differ by ~1e-2 even at {T:g}.  The dome (config 0, --workload dome) converges "
+                 f"without such steps and is where the 1e-6 target is measured.")
     out["statement"] = " ".join(parts)
     return out
 
