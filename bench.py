@@ -557,10 +557,17 @@ def run_thermo(args):
     nbytes = heat_bytes(mesh.nz, n_act, n_inact)
     peaks, peak_kind = measured_peaks()
     achieved = nbytes / (us[0] * 1e-6) / 1e9
-    traffic = None
+    # DRAM bytes per launch from the ncu capture recorded in profiles/traffic.json; a capture on a
+    # different column count is scaled by the columns with ice (the kernel's traffic grows with them)
+    traffic, traffic_note = None, None
     try:
         with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
-            traffic = json.load(f).get("k_heat_columns_bytes_per_launch")
+            tj = json.load(f)
+        t_cap, n_cap = tj.get("k_heat_columns_bytes_per_launch"), tj.get("k_heat_columns_active_columns")
+        if t_cap and n_cap:
+            traffic = int(round(t_cap * n_act / n_cap))
+            traffic_note = (f"ncu capture of {n_cap} columns with ice scaled to this run's {n_act}"
+                            if n_cap != n_act else "ncu capture of this workload")
     except OSError:
         pass
 
@@ -604,7 +611,7 @@ def run_thermo(args):
             "roofline": {"bound": "hbm", "kernel": "k_heat_columns<HeatMesh> (prelude + Thomas per column)",
                          "achieved": round(achieved, 1), "peak": peaks.get("hbm_gbs"), "unit": "GB/s",
                          "frac": round(achieved / peaks.get("hbm_gbs"), 4), "peak_source": peak_kind,
-                         "traffic": traffic, "algorithmic_bytes_per_launch": int(nbytes),
+                         "traffic": traffic, "traffic_source": traffic_note, "algorithmic_bytes_per_launch": int(nbytes),
                          "us_per_launch": round(float(us[0]), 2),
                          "step_kernels_us": [round(float(x), 2) for x in us]},
             "cpu_baseline": cpu,
@@ -1020,6 +1027,8 @@ def run_mixed(args):
         torch.distributed.init_process_group("nccl")
     pkg.build()
     p = pkg.geometry.mixed_ensemble_params()
+    if args.mixed_mode == "sequential":
+        return run_mixed_sequential(args, pkg, built, p, gen_s, rank, world, local)
     solvers = []
     for k, mesh, ice in built:
         sv = pkg.VelocitySolver(mesh, device=local)
@@ -1063,6 +1072,62 @@ def run_mixed(args):
             "picard_its": [results[k]["its"][0] for k in order],
             "krylov_its": [results[k]["its"][1] for k in order],
             "statuses": [results[k]["status"] for k in order],
+            "host_build_s": round(gen_s, 1),
+            "clocks": clocks.summary()}
+    print(json.dumps(line))
+
+
+def run_mixed_sequential(args, pkg, built, p, gen_s, rank, world, local):
+    """Config 4 member by member: each member's solve has the whole GPU, so it runs with the
+    persistent Krylov kernels (members side by side cannot: a persistent kernel needs every SM).
+    Two paths per member, each solved once (the device time of a solve excludes its graph
+    capture): plain FP64 -- the reference's algorithm -- and double-word Krylov inside the inexact
+    Picard iteration; the per-member distance between their answers is reported."""
+    import torch
+
+    p64 = _with(pkg, p, precision=pkg.abi.PREC_FP64, visc_it_nit=args.picard_nit)
+    pfast = _with(pkg, p, precision=pkg.abi.PREC_FP32_PAIR, krylov_forcing=args.forcing, visc_it_nit=args.picard_nit)
+    rows = {}
+    with ClockSampler(local) as clocks:
+        for k, mesh, ice in built:
+            with pkg.VelocitySolver(mesh, device=local) as sv:
+                sv.ice_upload(ice)
+                r = {"nV": mesh.nV}
+                for name, pp in (("fp64", p64), ("fp32_pair_inexact", pfast)):
+                    try:
+                        st = sv.solve_resident(pp, diva=True, cold_start=True)
+                        r[name] = {"ms": st["device_ms"], "picard": st["n_visc_its"], "krylov": st["n_Axb_its"],
+                                   "status": st["status"], "u": np.r_[sv.velocity_download()]}
+                    except pkg.UfeError as e:
+                        r[name] = {"ms": None, "status": e.code}
+                if r["fp64"].get("u") is not None and r["fp32_pair_inexact"].get("u") is not None:
+                    a, b = r["fp64"].pop("u"), r["fp32_pair_inexact"].pop("u")
+                    r["rel_l2_fast_vs_fp64"] = float("%.3g" % (np.linalg.norm(b - a) / np.linalg.norm(a)))
+                rows[k] = r
+            print(f"member {k}: {mesh.nV} vertices, FP64 {r['fp64'].get('ms')} ms, fast "
+                  f"{r['fp32_pair_inexact'].get('ms')} ms", file=sys.stderr, flush=True)
+    results = pkg.ensemble.gather_results(rows)
+    if rank != 0:
+        return
+    order = sorted(results)
+    n = len(order)
+    t64 = sum(results[k]["fp64"]["ms"] or 0.0 for k in order) / 1000.0
+    tf = sum(results[k]["fp32_pair_inexact"]["ms"] or 0.0 for k in order) / 1000.0
+    errs = [results[k].get("rel_l2_fast_vs_fp64") for k in order if results[k].get("rel_l2_fast_vs_fp64") is not None]
+    line = {"metric": f"mixed-size DIVA ensemble solves/s, members one after another, {world}xGB300",
+            "value": round(world * n / tf, 4), "unit": UNIT, "n_gpus": world, "steps": 1, "warmup": 0,
+            "ms_per_step": round(1000.0 * tf, 1), "higher_is_better": True,
+            "scaling": "strong" if world > 1 else "weak", "vs_baseline": None,
+            "dtype": "f64; Krylov in f32 pairs (double-word), inexact Picard",
+            "data": "synthetic ensemble geometries from seeded random fields on generated meshes (no files)",
+            "config": {"workload": MIXED_WORKLOAD.replace("members side by side (ufe_ensemble_solve)",
+                                                          "members one after another, persistent kernels"),
+                       "members": n, "total_vertices": int(sum(results[k]["nV"] for k in order)),
+                       "forcing": args.forcing},
+            "plain_fp64": {"value": round(world * n / t64, 4), "unit": UNIT, "device_s": round(t64, 2)},
+            "speedup_vs_plain_fp64": round(t64 / tf, 3),
+            "rel_l2_fast_vs_fp64": {"median": float(np.median(errs)), "max": float(np.max(errs))} if errs else None,
+            "members": {str(k): results[k] for k in order},
             "host_build_s": round(gen_s, 1),
             "clocks": clocks.summary()}
     print(json.dumps(line))
@@ -1321,6 +1386,8 @@ def main():
                     help="krylov_forcing of the inexact-Picard path (the early linear solves' residual reduction)")
     ap.add_argument("--picard-nit", type=int, default=200,
                     help="visc_it_nit of every channel path (a limit only: the tolerance ends the solves)")
+    ap.add_argument("--mixed-mode", choices=["sequential", "side_by_side"], default="sequential",
+                    help="config 4: members one after another with the persistent kernels, or side by side")
     ap.add_argument("--ref-tols", type=float, nargs="+", default=[1e-10, 1e-9, 1e-8, 1e-7, 1e-6],
                     help="Picard tolerances tried, tightest first, for the FP64 reference solution")
     ap.add_argument("--ref-sample-picard", type=int, default=4,

@@ -237,6 +237,24 @@ __global__ void k_icestream_yield(int nV, const double *Vy, double H, double tan
     tys[v] = f * pow(fabs(Vy[v] / L), m);
 }
 
+// The triangle terms of calc_vertical_shear_strain_rates (DIVA_main.f90:375-410):
+// du/dz_b = tau_bx_b zeta / max(visc_eff_min, eta_3D_b) (and v), per triangle and layer, from the
+// previous iteration's basal stress and 3-D viscosity.  Formed once per triangle (the vertex
+// kernel's b->a sums then read them) rather than once per vertex row entry; same expression.
+__device__ __forceinline__ void diva_shear_b(int64_t t, int nTri, int nz, double2 tb, const double *eta_3D_b,
+                                             const double *zeta, double visc_eff_min, double2 *duz_b) {
+  for (int l = 0; l < nz; ++l) {
+    const double e = fmax(visc_eff_min, eta_3D_b[(int64_t)l * nTri + t]);
+    duz_b[(int64_t)l * nTri + t] = make_double2(tb.x * zeta[l] / e, tb.y * zeta[l] / e);
+  }
+}
+__global__ void k_diva_shear_b(int nTri, int nz, const double2 *tau_b, const double *eta_3D_b, const double *zeta,
+                               double visc_eff_min, double2 *duz_b) {
+  int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < nTri; t += stride)
+    diva_shear_b(t, nTri, nz, tau_b[t], eta_3D_b, zeta, visc_eff_min, duz_b);
+}
+
 // ---- SSA vertex kernel ----------------------------------------------------------------------
 // calc_horizontal_strain_rates (SSA_DIVA_utilities.f90:59-82), calc_effective_viscosity
 // (SSA_main.f90:339-392) up to N_a, and the vertex part of calc_basal_friction_coefficient
@@ -268,62 +286,83 @@ __global__ void k_vertex_ssa(int nV, OpRow ba, const double2 *uv, const double *
 // calc_horizontal_strain_rates, calc_vertical_shear_strain_rates (DIVA_main.f90:375-410),
 // calc_effective_viscosity (:412-479), the surface value of calc_F_integrals' F2 (:481-520) and
 // the vertex part of calc_effective_basal_friction_coefficient (:522-574).
-__global__ void k_vertex_diva(int nV, int nTri, int nz, OpRow ba, const double2 *uv, const double2 *uv_base,
-                              const double2 *tau_b, const double *eta_3D_b, const double *A_pow,
-                              const double *Hi, const double *zeta_g, SlidingIn sl, PhysParams q,
-                              const PicardScalars *ps, double *eta_3D_a, double *N_a, double *F2a1,
-                              double *beta_a, double *beta_eff_a) {
+// One group of G lanes per vertex, one lane per layer (layers beyond G strided): the 3-D
+// viscosity of each layer -- a pow per layer, FP64 and latency-bound -- runs in parallel across the
+// group instead of in one thread's loop.  Every lane forms the vertex's horizontal strain rates (the
+// same loads, broadcast within the warp); lane 0 then sums the vertical average and the F2 integral
+// over the layers in the reference's order and evaluates the sliding law, so every value is the
+// one the one-thread-per-vertex form gives.  The loop runs over whole warps so that __syncwarp()
+// sees all 32 lanes.
+template <int G>
+__global__ void __launch_bounds__(256) k_vertex_diva(int nV, int nTri, int nz, OpRow ba, const double2 *uv,
+                                                     const double2 *uv_base, const double2 *duz_b,
+                                                     const double *A_pow, const double *Hi, const double *zeta_g,
+                                                     SlidingIn sl, PhysParams q, const PicardScalars *ps,
+                                                     double *eta_3D_a, double *N_a, double *F2a1, double *beta_a,
+                                                     double *beta_eff_a) {
+  constexpr int kGroups = 256 / G;
   __shared__ double zeta[kMaxNz];
+  __shared__ double eta_s[kGroups][kMaxNz];
+  __shared__ double f2_s[kGroups][kMaxNz];
   for (int k = threadIdx.x; k < nz; k += blockDim.x) zeta[k] = zeta_g[k];
   __syncthreads();
   const double eps0 = ps->eps0, eta_max = ps->eta_max;
   const float h_floor_sp = 0.1f;  // max(0.1, Hi) with a default-real literal (DIVA_main.f90:468)
-  int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t vi = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; vi < nV; vi += stride) {
-    const int k1 = ba.ptr[vi], k2 = ba.ptr[vi + 1];
-    double ux = 0, uy = 0, vx = 0, vy = 0, ua = 0, va = 0;
-    for (int k = k1; k < k2; ++k) {
-      int tj = ba.ind[k];
-      double2 w = uv[tj], wb = uv_base[tj];
-      double m = ba.v0[k], dx = ba.v1[k], dy = ba.v2[k];
-      ux = ux + dx * w.x;
-      uy = uy + dy * w.x;
-      vx = vx + dx * w.y;
-      vy = vy + dy * w.y;
-      ua = ua + m * wb.x;
-      va = va + m * wb.y;
-    }
-    double eta_k[kMaxNz];
-    for (int l = 0; l < nz; ++l) {
-      double duz = 0.0, dvz = 0.0;
+  const int lane = threadIdx.x % G, grp = threadIdx.x / G;
+  const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / 32;
+  const int64_t warps = (int64_t)gridDim.x * blockDim.x / 32;
+  for (int64_t v0 = warp * (32 / G); v0 < nV; v0 += warps * (32 / G)) {
+    const int64_t vi = v0 + (threadIdx.x % 32) / G;
+    const bool live = vi < nV;
+    if (live) {
+      const int k1 = ba.ptr[vi], k2 = ba.ptr[vi + 1];
+      double ux = 0, uy = 0, vx = 0, vy = 0;
       for (int k = k1; k < k2; ++k) {
-        int tj = ba.ind[k];
-        double e = fmax(q.visc_eff_min, eta_3D_b[(int64_t)l * nTri + tj]);
-        double2 tb = tau_b[tj];
-        double m = ba.v0[k];
-        duz = duz + m * (tb.x * zeta[l] / e);
-        dvz = dvz + m * (tb.y * zeta[l] / e);
+        const double2 w = uv[ba.ind[k]];
+        const double dx = ba.v1[k], dy = ba.v2[k];
+        ux = ux + dx * w.x;
+        uy = uy + dy * w.x;
+        vx = vx + dx * w.y;
+        vy = vy + dy * w.y;
       }
-      int64_t ix = (int64_t)l * nV + vi;
-      double e = glen_apow(eps0, ux, uy, vx, vy, duz, dvz, A_pow[ix], q.n_glen);
-      e = fmin(fmax(e, q.visc_eff_min), eta_max);
-      eta_k[l] = e;
-      eta_3D_a[ix] = e;
+      for (int l = lane; l < nz; l += G) {
+        double duz = 0.0, dvz = 0.0;
+        for (int k = k1; k < k2; ++k) {
+          const double2 d = duz_b[(int64_t)l * nTri + ba.ind[k]];
+          const double m = ba.v0[k];
+          duz = duz + m * d.x;
+          dvz = dvz + m * d.y;
+        }
+        const int64_t ix = (int64_t)l * nV + vi;
+        double e = glen_apow(eps0, ux, uy, vx, vy, duz, dvz, A_pow[ix], q.n_glen);
+        e = fmin(fmax(e, q.visc_eff_min), eta_max);
+        eta_s[grp][l] = e;
+        f2_s[grp][l] = zeta[l] * zeta[l] / e;
+        eta_3D_a[ix] = e;
+      }
     }
-    double vav = 0.0;
-    for (int l = 1; l < nz; ++l) vav = vav + 0.5 * (eta_k[l] + eta_k[l - 1]) * (zeta[l] - zeta[l - 1]);
-    N_a[vi] = vav * fmax((double)h_floor_sp, Hi[vi]);
-    // F2 at the surface: integrate zeta^2/eta from the base (zeta = 1) up to zeta(1) = 0
-    double intg = 0.0;
-    for (int l = nz - 1; l >= 1; --l) {
-      double f1 = zeta[l] * zeta[l] / eta_k[l], f0 = zeta[l - 1] * zeta[l - 1] / eta_k[l - 1];
-      intg = intg - 0.5 * (f1 + f0) * (zeta[l] - zeta[l - 1]);
+    __syncwarp();
+    if (live && lane == 0) {
+      double vav = 0.0;
+      for (int l = 1; l < nz; ++l) vav = vav + 0.5 * (eta_s[grp][l] + eta_s[grp][l - 1]) * (zeta[l] - zeta[l - 1]);
+      N_a[vi] = vav * fmax((double)h_floor_sp, Hi[vi]);
+      // F2 at the surface: integrate zeta^2/eta from the base (zeta = 1) up to zeta(1) = 0
+      double intg = 0.0;
+      for (int l = nz - 1; l >= 1; --l) intg = intg - 0.5 * (f2_s[grp][l] + f2_s[grp][l - 1]) * (zeta[l] - zeta[l - 1]);
+      const double F2 = -fmax(0.1, Hi[vi]) * intg;
+      F2a1[vi] = F2;
+      double ua = 0, va = 0;
+      for (int k = ba.ptr[vi]; k < ba.ptr[vi + 1]; ++k) {
+        const double2 wb = uv_base[ba.ind[k]];
+        const double m = ba.v0[k];
+        ua = ua + m * wb.x;
+        va = va + m * wb.y;
+      }
+      const double b = sliding_beta(q, sl, (int)vi, ua, va);
+      beta_a[vi] = b;
+      beta_eff_a[vi] = (q.sliding_law == UFE_SLIDING_NO_SLIDING) ? 1.0 / F2 : b / (1.0 + b * F2);
     }
-    double F2 = -fmax(0.1, Hi[vi]) * intg;
-    F2a1[vi] = F2;
-    double b = sliding_beta(q, sl, (int)vi, ua, va);
-    beta_a[vi] = b;
-    beta_eff_a[vi] = (q.sliding_law == UFE_SLIDING_NO_SLIDING) ? 1.0 / F2 : b / (1.0 + b * F2);
+    __syncwarp();
   }
 }
 
@@ -721,7 +760,8 @@ template <bool DIVA>
 __global__ void k_finalize(int nTri, const double2 *X, double2 *uv, PhysParams q, PicardScalars *ps,
                            KrylovScalars *ks, const double *beta_eff_b, const double *bfc_b, const double *F2b1,
                            double2 *uv_base, double2 *tau_b, double *partials, unsigned int *tickets,
-                           CondArg cond) {
+                           CondArg cond, int nz = 0, const double *eta_3D_b = nullptr,
+                           const double *zeta = nullptr, double2 *duz_b = nullptr) {
   const double r = ps->relax;
   double acc[2] = {0.0, 0.0};
   int64_t stride = (int64_t)gridDim.x * blockDim.x;
@@ -740,7 +780,9 @@ __global__ void k_finalize(int nTri, const double2 *X, double2 *uv, PhysParams q
         uv_base[t] = make_double2(u / den, v / den);
       }
       double be = beta_eff_b[t];
-      tau_b[t] = make_double2(u * be, v * be);
+      const double2 tb = make_double2(u * be, v * be);
+      tau_b[t] = tb;
+      diva_shear_b(t, nTri, nz, tb, eta_3D_b, zeta, q.visc_eff_min, duz_b);   // for the next iteration
     }
     acc[0] += (u - o.x) * (u - o.x) + (v - o.y) * (v - o.y);
     acc[1] += (u + o.x) * (u + o.x) + (v + o.y) * (v + o.y);
@@ -1111,6 +1153,7 @@ Work *ensure_work(ufe_ctx *ctx) {
   w->uv_base = alloc_n<double2>(nTri);
   w->tau_b = alloc_n<double2>(nTri);
   w->eta_3D_b = alloc_n<double>((size_t)nTri * nz);
+  w->duz_b = alloc_n<double2>((size_t)nTri * nz);
   w->bfc_b = alloc_n<double>(nTri);
   w->F2b1 = alloc_n<double>(nTri);
   w->beta_b = alloc_n<double>(nTri);
@@ -1171,7 +1214,7 @@ void free_work(ufe_ctx *ctx) {
                   w->sell_blk32, w->halo_off, w->halo_idx, w->halo_lcol, w->pX, w->pR, w->pRP, w->pS, w->pT,
                   w->pdinv, w->pP[0], w->pP[1], w->pV[0], w->pV[1], w->sell_blkp, w->pair_bad,
                   w->Ti, w->mask_fl, w->fgr_v, w->Hib, w->SL, w->A_rheo, w->tys_ideal, w->cp_ptr, w->cp_idx,
-                  w->cp_w};
+                  w->cp_w, w->duz_b};
   for (void *p : ptrs) dev_free(p);
   if (w->ks_host) cudaFreeHost(w->ks_host);
   if (w->ps_host) cudaFreeHost(w->ps_host);
@@ -1334,6 +1377,8 @@ struct Solver {
   }
 
   int eblocks(int64_t n) const { return pick_blocks(n, kThreads, grid); }
+  // blocks of 256 threads for one G-lane group per vertex
+  int vertex_blocks(int G) const { return pick_blocks((int64_t)w->nV * G, 256, 1 << 20); }
 
   SlidingIn sliding() const {
     const double *tys = p.choice_sliding_law == UFE_SLIDING_IDEALISED_SSA_ICESTREAM ? w->tys_ideal : w->tys;
@@ -1723,15 +1768,23 @@ struct Solver {
         w->nV, w->nTri, w->nz, ab, w->Hi, w->Hs, A_src(), ctx->zeta, w->tau_d, diva ? nullptr : w->Avav,
         diva ? w->A_pow : nullptr, w->ps, w->ks, p.visc_it_relax, p.Glens_flow_law_epsilon_sq_0,
         p.Glens_flow_law_exponent);
+    if (diva)
+      k_diva_shear_b<<<eblocks(w->nTri), kThreads, 0, s>>>(w->nTri, w->nz, w->tau_b, w->eta_3D_b, ctx->zeta,
+                                                           p.visc_eff_min, w->duz_b);
     UFE_CUDA(cudaMemsetAsync(w->ks + 1, 0, sizeof(KrylovScalars), s));
     UFE_CUDA(cudaGetLastError());
   }
 
   void enqueue_picard_pre(bool diva, CondArg inner) {
     if (diva) {
-      k_vertex_diva<<<eblocks(w->nV), kThreads, 0, s>>>(
-          w->nV, w->nTri, w->nz, ba, w->uv, w->uv_base, w->tau_b, w->eta_3D_b, w->A_pow, w->Hi, ctx->zeta,
-          sliding(), q, w->ps, w->eta_3D_a, w->N_a, w->F2a1, w->beta_a, w->beta_eff_a);
+      if (w->nz <= 16)
+        k_vertex_diva<16><<<vertex_blocks(16), 256, 0, s>>>(
+            w->nV, w->nTri, w->nz, ba, w->uv, w->uv_base, w->duz_b, w->A_pow, w->Hi, ctx->zeta,
+            sliding(), q, w->ps, w->eta_3D_a, w->N_a, w->F2a1, w->beta_a, w->beta_eff_a);
+      else
+        k_vertex_diva<32><<<vertex_blocks(32), 256, 0, s>>>(
+            w->nV, w->nTri, w->nz, ba, w->uv, w->uv_base, w->duz_b, w->A_pow, w->Hi, ctx->zeta,
+            sliding(), q, w->ps, w->eta_3D_a, w->N_a, w->F2a1, w->beta_a, w->beta_eff_a);
     } else {
       k_vertex_ssa<<<eblocks(w->nV), kThreads, 0, s>>>(w->nV, ba, w->uv, w->Avav, w->Hi, sliding(), q, w->ps,
                                                        w->N_a, w->beta_a);
@@ -1744,7 +1797,8 @@ struct Solver {
     if (diva)
       k_finalize<true><<<eblocks(w->nTri), kThreads, 0, s>>>(w->nTri, w->kv.X, w->uv, q, w->ps, w->ks, w->beta_b,
                                                              w->bfc_b, w->F2b1, w->uv_base, w->tau_b,
-                                                             ctx->red.partials, ctx->red.tickets, outer);
+                                                             ctx->red.partials, ctx->red.tickets, outer, w->nz,
+                                                             w->eta_3D_b, ctx->zeta, w->duz_b);
     else
       k_finalize<false><<<eblocks(w->nTri), kThreads, 0, s>>>(w->nTri, w->kv.X, w->uv, q, w->ps, w->ks, nullptr,
                                                               nullptr, nullptr, nullptr, nullptr,

@@ -105,6 +105,7 @@ struct Work {
   // DIVA state on triangles
   double2 *uv_base = nullptr, *tau_b = nullptr;
   double *eta_3D_b = nullptr;   // nz x nTri
+  double2 *duz_b = nullptr;     // nz x nTri: (du/dz, dv/dz) on triangles for the next vertex pass
   double *bfc_b = nullptr, *F2b1 = nullptr;
   double *beta_b = nullptr;     // applied friction on triangles (SSA) / beta_eff_b (DIVA)
   // vertex inputs
