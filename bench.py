@@ -45,6 +45,7 @@ METRIC = "converged SSA/DIVA velocity solves/s, learned+FP32 vs plain FP64, 1xGB
 CHANNEL_VARIANTS = [(210.0, 1.5e-17), (230.0, 2.5e-17), (270.0, 1.5e-17), (290.0, 2.5e-17),
                     (220.0, 3e-17), (240.0, 1.2e-17), (260.0, 3e-17), (280.0, 1.2e-17)]
 LEARNED_SMOOTH = 8
+LEARNED_VISC_PATHS = ("fp64", "fp32_pair", "fp32_pair_inexact")   # learned paths also run with the predicted viscosity
 UNIT = "solves/s"
 
 
@@ -323,8 +324,8 @@ def run_ours(args):
         solver.ice_upload(ice)
         predict_kernels = int(solver.lib.ufe_gnn_predict_kernels(LEARNED_SMOOTH))
 
-        def learned_solve(p):
-            ms = net.predict(solver, smooth_passes=LEARNED_SMOOTH)
+        def learned_solve(p, visc=False):
+            ms = net.predict(solver, smooth_passes=LEARNED_SMOOTH, viscosity=visc)
             st = dict(solver.solve_resident(p, diva=True, cold_start=False))
             st["device_ms"] += ms
             return st
@@ -339,16 +340,30 @@ def run_ours(args):
             learned[name]["rel_l2_vs_fp64_reference"] = err_ref(u)
             learned[name]["us_per_krylov_it_in_solve"] = round(1000.0 * learned[name]["ms_per_solve"]
                                                                / max(learned[name]["krylov_its"], 1), 2)
-        best = max(prec, key=lambda k: learned[k]["value"] or 0.0)
+        # the same with the predicted viscosity in the first Picard iteration (every layer a
+        # depth-uniform viscosity) in place of Glen's law on the predicted velocity
+        for name in LEARNED_VISC_PATHS:
+            key = f"visc_{name}"
+            learned_solve(prec[name], True)
+            learned_runs[key] = timed(lambda: learned_solve(prec[name], True), steps_of[name], f"timed_learned_{key}")
+            u = np.r_[solver.velocity_download()]
+            sts, rate, _, _ = learned_runs[key]
+            learned[key] = summary(sts, rate, u_plain["fp64"], u)
+            learned[key]["rel_l2_vs_fp64_reference"] = err_ref(u)
+        # the headline's rule: the fastest learned path with FP32 Krylov arithmetic
+        lkeys = [k for k in prec if k != "fp64"] + [f"visc_{k}" for k in LEARNED_VISC_PATHS if k != "fp64"]
+        best_key = max(lkeys, key=lambda k: learned[k]["value"] or 0.0)
+        best_visc = best_key.startswith("visc_")
+        best = best_key[len("visc_"):] if best_visc else best_key
         # end to end through the public C ABI with pinned host buffers: ice upload, prediction,
         # resident solve, velocity download -- every step
         solver.ice_upload(ice_h)
-        learned_solve(prec[best])
+        learned_solve(prec[best], best_visc)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         for _ in range(args.steps):
             solver.ice_upload(ice_h)
-            learned_solve(prec[best])
+            learned_solve(prec[best], best_visc)
             solver.velocity_download()
         torch.cuda.synchronize()
         t_e2e_l = slowest(time.perf_counter() - t0)
@@ -383,7 +398,7 @@ def run_ours(args):
                     v.pop("_u", None)
             learned["tight_tolerance_pair"] = tight
         net.close()
-        learned["e2e"] = {"value": round(world * args.steps / t_e2e_l, 4), "unit": UNIT, "path": best,
+        learned["e2e"] = {"value": round(world * args.steps / t_e2e_l, 4), "unit": UNIT, "path": f"learned_{best_key}",
                           "h2d_bytes_per_step": int(sum(v.nbytes for v in ice_h.values())),
                           "d2h_bytes_per_step": int(2 * 8 * mesh.nTri)}
         learned["training"] = {"variants": args.learned_variants, "solves_device_s": round(gen_ms / 1000.0, 2),
@@ -403,6 +418,8 @@ def run_ours(args):
     cands = [(f"plain_{k}", plain_runs[k], k) for k in prec]
     if learned:
         cands += [(f"learned_{k}", learned_runs[k], k) for k in prec]
+        cands += [(f"learned_visc_{k}", learned_runs[f"visc_{k}"], k) for k in LEARNED_VISC_PATHS]
+    assert not learned or {c[0] for c in cands} >= {learned["e2e"]["path"]}
     fastest_any = max(cands, key=lambda c: c[1][1] or 0.0)
     # the metric is the learned start with FP32 Krylov arithmetic against plain FP64: the headline is
     # the fastest learned-start path with an FP32 Krylov mode (all paths are listed beside it)
@@ -412,7 +429,7 @@ def run_ours(args):
         launches = kernels(head_sts, predict_kernels)
     else:
         launches = kernels(head_sts)
-    if learned and head_name == f"learned_{best}":
+    if learned and head_name == learned["e2e"]["path"]:
         head_e2e = learned["e2e"]
     else:
         # end to end through the public C ABI with pinned host buffers: ice upload, the solve
@@ -662,7 +679,8 @@ def run_learned(args):
         gen_wall = time.perf_counter() - t0
         losses, train_ms = net.train(epochs=args.learned_epochs, lr=args.learned_lr)
         net.dataset_clear()
-        keys = ("cold_fp64", "cold_fp32_pair", "learned_fp64", "learned_fp32_pair", "learned_fp32")
+        keys = ("cold_fp64", "cold_fp32_pair", "learned_fp64", "learned_fp32_pair", "learned_fp32",
+                "learned_visc_fp64", "learned_visc_fp32_pair")
         rows = {k: [] for k in keys}
         errs = {k: [] for k in keys}
         pred_ms = []
@@ -691,8 +709,10 @@ def run_learned(args):
                 if ut is not None:
                     u = np.r_[s.velocity_download()]
                     errs["cold_fp32_pair"].append(np.linalg.norm((u - ut)[sel]) / np.linalg.norm(ut[sel]))
-                for key, pp in (("learned_fp64", p), ("learned_fp32_pair", pair_of(p)), ("learned_fp32", p32_of(p))):
-                    pred_ms.append(net.predict(s))
+                for key, pp in (("learned_fp64", p), ("learned_fp32_pair", pair_of(p)), ("learned_fp32", p32_of(p)),
+                                ("learned_visc_fp64", p), ("learned_visc_fp32_pair", pair_of(p))):
+                    # learned_visc_*: the predicted viscosity also replaces Glen's law in the first iteration
+                    pred_ms.append(net.predict(s, viscosity=key.startswith("learned_visc")))
                     st = s.solve_resident(pp, diva=False, cold_start=False)
                     rows[key].append(st)
                     if ut is not None:
@@ -1364,7 +1384,7 @@ def run_probe(args):
         nbr = np.stack([i ^ 1, (i + 2) % n, (i - 2) % n], axis=1).astype(np.int32)
         rng = np.random.default_rng(0)
         x = rng.normal(size=(n, 16)).astype(np.float32)
-        tgt = rng.normal(size=(n, 2)).astype(np.float32)
+        tgt = rng.normal(size=(n, 3)).astype(np.float32)
         w = np.full(n, 1.0 / n, np.float32)
         with pkg.ColumnSolver() as s:
             net = pkg.LearnedStart(s, seed=1)

@@ -491,9 +491,11 @@ int32_t ufe_umma_gemm_bf16(ufe_ctx *ctx, int32_t M, int32_t N, int32_t K, const 
 
 /* ---- learned Picard start: the mesh-graph network ---------------------------------------------- */
 /* A network on the triangle b-grid (nodes: triangles, edges: TriC neighbours) that predicts the
- * velocity a Picard solve starts from.  Width 64: an encoder from 16 per-triangle features, four
- * message-passing layers h <- h + W2 relu(W1 [h, mean of the neighbours' h] + b1) + b2, and a
- * linear decoder to (u, v) / 1000 m/yr.  Forward and backward run in hand-written kernels on the
+ * velocity and the effective viscosity a Picard solve starts from.  Width 64: an encoder from 16
+ * per-triangle features, four message-passing layers h <- h + W2 relu(W1 [h, mean of the
+ * neighbours' h] + b1) + b2, and a linear decoder to three outputs: (u, v) / 1000 m/yr and
+ * (log10(eta_vav) - 7.5) / 2 with eta_vav the vertically averaged effective viscosity in Pa yr.
+ * Forward and backward run in hand-written kernels on the
  * tcgen05 tensor cores (BF16 operands, FP32 accumulation); Adam in FP32.  The solve still iterates
  * to its own tolerance: the prediction only replaces the zero (or previous-step) start.  No
  * reference counterpart; it feeds solve_SSA / solve_DIVA (SSA_main.f90:87, DIVA_main.f90:88). */
@@ -506,24 +508,30 @@ int32_t ufe_gnn_get_params(ufe_gnn *g, float *params);                /* ufe_gnn
 int32_t ufe_gnn_set_params(ufe_gnn *g, const float *params);          /* also resets the Adam state   */
 
 /* Explicit graphs (host arrays): n nodes, nbr n x 3 row-major (-1: no neighbour; the adjacency must
- * be symmetric), x n x 16 features, y / target n x 2, w n loss weights.  loss = sum_i w_i |y_i - t_i|^2;
+ * be symmetric), x n x 16 features, y / target n x 3, w n loss weights.  loss = sum_i w_i |y_i - t_i|^2;
  * grad receives its gradient with respect to the parameters. */
 int32_t ufe_gnn_forward(ufe_gnn *g, int64_t n, const int32_t *nbr, const float *x, float *y);
 int32_t ufe_gnn_loss_grad(ufe_gnn *g, int64_t n, const int32_t *nbr, const float *x, const float *target,
                           const float *w, double *loss, float *grad);
 
-/* Kernels one ufe_gnn_predict_velocity call launches with this many smoothing passes. */
+/* Kernels one ufe_gnn_predict_velocity call launches with this many smoothing passes (one more
+ * for ufe_gnn_predict_start with with_viscosity = 1). */
 int32_t ufe_gnn_predict_kernels(int32_t smooth_passes);
 
 /* The mesh path.  ufe_gnn_features: the 16 features of a mesh context's resident ice state (after
  * ufe_ice_upload), nTri x 16 in the caller's triangle order; use_prev_velocity = 0 zeroes the
  * previous-velocity features (a cold start).  ufe_gnn_dataset_add: store one training member on the
  * device -- the features (given, as taken before the solve, or NULL to take them now with a zero
- * previous velocity) and the context's resident solution as the target; returns the member count.
+ * previous velocity) and the context's resident solution (velocity, and the vertically averaged
+ * viscosity of its last Picard iteration) as the target; returns the member count.
  * ufe_gnn_train: `epochs` passes over the stored members, one Adam step per member.
  * ufe_gnn_predict_velocity: write the predicted velocity into the context's resident state for a
  * following resident solve with cold_start = 0, after `smooth_passes` (0: none) averaging passes over
- * each triangle and its neighbours (noise in the prediction roughens the first viscosity field). */
+ * each triangle and its neighbours (noise in the prediction roughens the first viscosity field).
+ * ufe_gnn_predict_start: the same, and with with_viscosity = 1 also the predicted viscosity on the
+ * vertices, which the next resident solve with cold_start = 0 uses in its first Picard iteration in
+ * place of Glen's law (SSA: the vertex viscosity; DIVA: every layer, a depth-uniform first
+ * viscosity), clamped as Glen's law is.  A cold start, a velocity upload or a solve consumes it. */
 int32_t ufe_gnn_features(ufe_gnn *g, ufe_ctx *mesh_ctx, int32_t use_prev_velocity, float *x);
 int32_t ufe_gnn_dataset_add(ufe_gnn *g, ufe_ctx *mesh_ctx, const float *features_before);
 int32_t ufe_gnn_dataset_clear(ufe_gnn *g);
@@ -532,6 +540,8 @@ int32_t ufe_gnn_train(ufe_gnn *g, int32_t epochs, float lr, uint64_t seed, float
 int32_t ufe_gnn_evaluate(ufe_gnn *g, double *mean_loss);
 int32_t ufe_gnn_predict_velocity(ufe_gnn *g, ufe_ctx *mesh_ctx, int32_t use_prev_velocity, int32_t smooth_passes,
                                  double *device_ms);
+int32_t ufe_gnn_predict_start(ufe_gnn *g, ufe_ctx *mesh_ctx, int32_t use_prev_velocity, int32_t smooth_passes,
+                              int32_t with_viscosity, double *device_ms);
 
 /* ---- allocation-free solve -------------------------------------------------------------------- */
 /* The CSR matrix-equation solve of ufe_solve_csr (same BiCGStab/Jacobi, same convergence test)

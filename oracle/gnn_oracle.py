@@ -7,13 +7,14 @@ kernels, so the two differ only by accumulation order (FP32 on the GPU, FP64 her
 ``bf16=False`` it is the exact network, which the finite-difference test pins.
 
 Parameter vector layout (float32 in the library): We [64x16], be [64], then per layer
-W1 [64x128], b1 [64], W2 [64x64], b2 [64] (4 layers), then Wd [2x64], bd [2].
+W1 [64x128], b1 [64], W2 [64x64], b2 [64] (4 layers), then Wd [3x64], bd [3] (outputs: u, v and
+the log-viscosity).
 """
 from __future__ import annotations
 
 import numpy as np
 
-C, FIN, LAYERS, NB = 64, 16, 4, 3
+C, FIN, LAYERS, NB, OUT = 64, 16, 4, 3, 3
 
 
 def layout():
@@ -31,8 +32,8 @@ def layout():
         add(f"b1_{l}", (C,))
         add(f"W2_{l}", (C, C))
         add(f"b2_{l}", (C,))
-    add("Wd", (2, C))
-    add("bd", (2,))
+    add("Wd", (OUT, C))
+    add("bd", (OUT,))
     return off, o
 
 

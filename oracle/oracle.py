@@ -60,6 +60,7 @@ def load():
         "orc_ops_solve_diva": (C.c_int32, [vp, C.POINTER(abi.SolverParams), C.POINTER(abi.IceState),
                                            C.POINTER(abi.BCPrescribed), C.POINTER(abi.DivaState),
                                            C.POINTER(abi.SolveStats)]),
+        "orc_ops_set_first_viscosity": (C.c_int32, [vp, dp]),
         "orc_ops_assemble": (C.c_int32, [vp, C.POINTER(abi.SolverParams), dp, dp, dp, dp, dp, dp, dp, dp,
                                          C.POINTER(abi.BCPrescribed), ip, ip, dp, dp, C.c_int64,
                                          C.POINTER(C.c_int64)]),
@@ -187,6 +188,14 @@ class Oracle:
             raise OracleError(rc)
         n = nnz.value
         return CSR(2 * nT, 2 * nT, ptr, ind[:n].copy(), val[:n].copy(), 1), bb
+
+    def set_first_viscosity(self, eta_a=None):
+        """Viscosity per vertex for the first Picard iteration of the next solve (the learned
+        start's prediction; no reference counterpart), or None to clear it."""
+        arr = None if eta_a is None else np.ascontiguousarray(eta_a, dtype=np.float64)
+        rc = self.lib.orc_ops_set_first_viscosity(self.h, None if arr is None else self.abi.as_d(arr))
+        if rc < 0:
+            raise OracleError(rc)
 
     def solve_SSA(self, ice, SSA, params, BC=None):
         st, keep = self.abi.ice_state(ice)

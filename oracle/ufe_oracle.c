@@ -980,7 +980,7 @@ static const ufe_ice_state *solve_ice_state(const ufe_mesh_desc *m, const ufe_so
  * calc_applied_basal_friction_coefficient (:394-430). */
 int32_t orc_solve_ssa(const ufe_mesh_desc *m, const orc_csr *ops, const ufe_solver_params *p,
                       const ufe_ice_state *ice, const ufe_bc_prescribed *bc,
-                      double *u_b, double *v_b, ufe_solve_stats *st) {
+                      double *u_b, double *v_b, ufe_solve_stats *st, const double *eta_first) {
   const int nV = m->nV, nTri = m->nTri, nz = m->nz;
   ufe_solve_stats dummy;
   if (!st) st = &dummy;
@@ -1028,7 +1028,10 @@ int32_t orc_solve_ssa(const ufe_mesh_desc *m, const orc_csr *ops, const ufe_solv
     double A_min = 1e-18;
     double eta_max = 0.5 * pow(A_min, -1.0 / n_glen) * pow(eps0_applied, (1.0 - n_glen) / (2.0 * n_glen));
     for (int vi = 0; vi < nV; ++vi) {
-      double e = glen_2d(eps0_applied, ux[vi], uy[vi], vx[vi], vy[vi], Avav[vi], n_glen);
+      /* eta_first (the learned start's predicted viscosity, no reference counterpart) replaces
+       * Glen's law in the first iteration only */
+      double e = (eta_first && it == 1) ? eta_first[vi]
+                                        : glen_2d(eps0_applied, ux[vi], uy[vi], vx[vi], vy[vi], Avav[vi], n_glen);
       e = fmin(fmax(e, p->visc_eff_min), eta_max);
       eta[vi] = e;
       N_a[vi] = e * fmax(0.1, ice->Hi[vi]);
@@ -1076,7 +1079,7 @@ int32_t orc_solve_ssa(const ufe_mesh_desc *m, const orc_csr *ops, const ufe_solv
  * calc_basal_velocities (:600-627) and calc_3D_velocities (:629-676). */
 int32_t orc_solve_diva(const ufe_mesh_desc *m, const orc_csr *ops, const ufe_solver_params *p,
                        const ufe_ice_state *ice, const ufe_bc_prescribed *bc,
-                       ufe_diva_state *ds, ufe_solve_stats *st) {
+                       ufe_diva_state *ds, ufe_solve_stats *st, const double *eta_first) {
   const int nV = m->nV, nTri = m->nTri, nz = m->nz;
   const double *zeta = m->zeta;
   ufe_solve_stats dummy;
@@ -1148,8 +1151,11 @@ int32_t orc_solve_diva(const ufe_mesh_desc *m, const orc_csr *ops, const ufe_sol
     for (int vi = 0; vi < nV; ++vi)
       for (int k = 0; k < nz; ++k) {
         int64_t ix = (int64_t)k * nV + vi;
-        double e = glen_3d(eps0_applied, ux[vi], uy[vi], du_dz_a[ix], vx[vi], vy[vi], dv_dz_a[ix],
-                           ice->A_flow[ix], n_glen);
+        /* eta_first: a depth-uniform predicted viscosity in the first iteration only (see SSA) */
+        double e = (eta_first && it == 1)
+                       ? eta_first[vi]
+                       : glen_3d(eps0_applied, ux[vi], uy[vi], du_dz_a[ix], vx[vi], vy[vi], dv_dz_a[ix],
+                                 ice->A_flow[ix], n_glen);
         eta_3D_a[ix] = fmin(fmax(e, p->visc_eff_min), eta_max);
       }
     orc_spmv(&ops[UFE_OP_MAP_A_B], eta_3D_a, ds->eta_3D_b, nz);
@@ -1246,6 +1252,7 @@ int32_t orc_solve_diva(const ufe_mesh_desc *m, const orc_csr *ops, const ufe_sol
 struct orc_ops {
   ufe_mesh_desc mesh;
   orc_csr ops[UFE_OP_COUNT];
+  double *eta_first;   /* nV: first-iteration viscosity of the next solve (consumed by it), or NULL */
 };
 
 orc_ops *orc_ops_create(const ufe_mesh_desc *mesh, int32_t *status) {
@@ -1263,7 +1270,27 @@ const orc_csr *orc_ops_op(const orc_ops *h, int32_t op) { return &h->ops[op]; }
 void orc_ops_destroy(orc_ops *h) {
   if (!h) return;
   for (int op = 0; op < UFE_OP_COUNT; ++op) orc_csr_free(&h->ops[op]);
+  free(h->eta_first);
   free(h);
+}
+
+/* The learned start's predicted viscosity (per vertex) for the first Picard iteration of the next
+ * solve on this handle; NULL clears it.  The next solve consumes it. */
+int32_t orc_ops_set_first_viscosity(orc_ops *h, const double *eta_a) {
+  if (!h) return UFE_ERR_INVALID;
+  free(h->eta_first);
+  h->eta_first = NULL;
+  if (eta_a) {
+    h->eta_first = (double *)malloc(sizeof(double) * (size_t)h->mesh.nV);
+    memcpy(h->eta_first, eta_a, sizeof(double) * (size_t)h->mesh.nV);
+  }
+  return UFE_OK;
+}
+
+static double *take_first_viscosity(orc_ops *h) {
+  double *e = h->eta_first;
+  h->eta_first = NULL;
+  return e;
 }
 
 int32_t orc_ops_info(orc_ops *h, int32_t op, int32_t *m, int32_t *n, int64_t *nnz) {
@@ -1289,12 +1316,18 @@ int32_t orc_ops_apply(orc_ops *h, int32_t op, const double *x, double *y, int32_
 
 int32_t orc_ops_solve_ssa(orc_ops *h, const ufe_solver_params *p, const ufe_ice_state *ice,
                           const ufe_bc_prescribed *bc, double *u_b, double *v_b, ufe_solve_stats *st) {
-  return orc_solve_ssa(&h->mesh, h->ops, p, ice, bc, u_b, v_b, st);
+  double *ef = take_first_viscosity(h);
+  int32_t rc = orc_solve_ssa(&h->mesh, h->ops, p, ice, bc, u_b, v_b, st, ef);
+  free(ef);
+  return rc;
 }
 
 int32_t orc_ops_solve_diva(orc_ops *h, const ufe_solver_params *p, const ufe_ice_state *ice,
                            const ufe_bc_prescribed *bc, ufe_diva_state *ds, ufe_solve_stats *st) {
-  return orc_solve_diva(&h->mesh, h->ops, p, ice, bc, ds, st);
+  double *ef = take_first_viscosity(h);
+  int32_t rc = orc_solve_diva(&h->mesh, h->ops, p, ice, bc, ds, st, ef);
+  free(ef);
+  return rc;
 }
 
 int32_t orc_ops_assemble(orc_ops *h, const ufe_solver_params *p,

@@ -53,11 +53,13 @@ int32_t orc_bicgstab(const orc_csr *A, const double *b, double *x, double rtol, 
 
 int32_t orc_solve_ssa(const ufe_mesh_desc *mesh, const orc_csr *ops, const ufe_solver_params *p,
                       const ufe_ice_state *ice, const ufe_bc_prescribed *bc,
-                      double *u_b, double *v_b, ufe_solve_stats *st);
+                      double *u_b, double *v_b, ufe_solve_stats *st,
+                      const double *eta_first /* nV or NULL: first-iteration viscosity */);
 
 int32_t orc_solve_diva(const ufe_mesh_desc *mesh, const orc_csr *ops, const ufe_solver_params *p,
                        const ufe_ice_state *ice, const ufe_bc_prescribed *bc,
-                       ufe_diva_state *ds, ufe_solve_stats *st);
+                       ufe_diva_state *ds, ufe_solve_stats *st,
+                       const double *eta_first /* nV or NULL: first-iteration viscosity */);
 
 /* Convenience for ctypes callers: build operators into an opaque handle. */
 typedef struct orc_ops orc_ops;
@@ -70,6 +72,7 @@ int32_t  orc_ops_solve_ssa(orc_ops *h, const ufe_solver_params *p, const ufe_ice
                            const ufe_bc_prescribed *bc, double *u_b, double *v_b, ufe_solve_stats *st);
 int32_t  orc_ops_solve_diva(orc_ops *h, const ufe_solver_params *p, const ufe_ice_state *ice,
                             const ufe_bc_prescribed *bc, ufe_diva_state *ds, ufe_solve_stats *st);
+int32_t  orc_ops_set_first_viscosity(orc_ops *h, const double *eta_a);
 int32_t  orc_ops_assemble(orc_ops *h, const ufe_solver_params *p,
                           const double *N_b, const double *dN_dx_b, const double *dN_dy_b,
                           const double *beta_b, const double *tau_dx_b, const double *tau_dy_b,

@@ -39,7 +39,7 @@ def _net_case(G, n=300, seed=0, scale=1.0):
     nbr = G.random_graph(n, seed)
     x = rng.normal(size=(n, G.FIN)) * scale
     p = rng.normal(size=G.NPARAMS) * 0.15
-    tgt = rng.normal(size=(n, 2))
+    tgt = rng.normal(size=(n, G.OUT))
     w = rng.uniform(0.0, 1.0, n)
     w /= w.sum()
     return nbr, x, p, tgt, w
@@ -151,3 +151,60 @@ def test_gnn_warm_start_saves_picard_iterations(pkg, gpu_lib):
         assert sum(warm) < 0.8 * sum(cold), (cold, warm)
         assert np.mean(e_warm) <= 1.5 * np.mean(e_cold), (e_cold, e_warm)
         net.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("diva", [False, True])
+def test_predicted_viscosity_start_matches_oracle(pkg, oracle_mod, gpu_lib, diva):
+    """ufe_gnn_predict_start with the viscosity: a network whose decoder is constant predicts the
+    start velocity (u0, v0) on the ice triangles and a uniform viscosity.  The GPU solve from that
+    start, whose first Picard iteration takes the predicted viscosity in place of Glen's law (every
+    layer for DIVA), matches the oracle's solve from the same velocity with the same first-iteration
+    viscosity: same Picard count, velocities within 1e-8."""
+    import gnn_oracle as G
+    if diva:
+        mesh, ice, params = pkg.geometry.small_channel(sliding="Schoof2005")
+        params.visc_it_nit = 12
+    else:
+        mesh, ice, params = pkg.geometry.small_dome(seed=1)
+    params.stress_balance_PETSc_rtol = 1e-12
+    params.stress_balance_PETSc_abstol = 0.0
+    orc = oracle_mod.Oracle(mesh)
+    u0, v0, c = 30.0, -4.0, 0.55                     # c = (log10(eta) - 7.5) / 2
+    with pkg.VelocitySolver(mesh, operators=orc.operators()) as g:
+        net = pkg.LearnedStart(g)
+        P = G.unpack(net.get_params().astype(np.float64))
+        P["Wd"][:] = 0.0
+        P["bd"][:] = [u0 / 1e3, v0 / 1e3, c]
+        net.set_params(G.pack(P).astype(np.float32))
+        g.ice_upload(ice)
+        net.predict(g, viscosity=True)
+        st = g.solve_resident(params, diva=diva, cold_start=False)
+        ug = np.r_[g.velocity_download()]
+        # a velocity-only prediction leaves Glen's law in the first iteration
+        g.ice_upload(ice)
+        net.predict(g, viscosity=False)
+        st_v = g.solve_resident(params, diva=diva, cold_start=False)
+        uv_only = np.r_[g.velocity_download()]
+        net.close()
+    on_ice = orc.apply("MAP_A_B", ice["Hi"]) > 0
+    f32 = lambda a: float(np.float32(a))
+    u_start = np.where(on_ice, f32(u0 / 1e3) * 1e3, 0.0)
+    v_start = np.where(on_ice, f32(v0 / 1e3) * 1e3, 0.0)
+    eta = np.full(mesh.nV, 10.0 ** (2.0 * f32(c) + 7.5))
+    if diva:
+        b = pkg.new_diva_state(mesh.nTri, mesh.nz)
+        b["u_vav_b"][:], b["v_vav_b"][:] = u_start, v_start
+        orc.set_first_viscosity(eta)
+        nvo, _, sto = orc.solve_DIVA(ice, b, params)
+        uo = np.r_[b["u_vav_b"], b["v_vav_b"]]
+    else:
+        b = pkg.new_ssa_state(mesh.nTri)
+        b["u_b"][:], b["v_b"][:] = u_start, v_start
+        orc.set_first_viscosity(eta)
+        nvo, _, sto = orc.solve_SSA(ice, b, params)
+        uo = np.r_[b["u_b"], b["v_b"]]
+    assert st["status"] == sto["status"] and st["n_visc_its"] == nvo, (st, nvo, sto)
+    assert _rel(ug, uo) < 1e-8, _rel(ug, uo)
+    # the predicted viscosity changed the iteration: the velocity-only start follows another path
+    assert st_v["n_visc_its"] != st["n_visc_its"] or _rel(uv_only, ug) > 1e-12

@@ -165,6 +165,23 @@ def test_oracle_diva_converges_on_channel(pkg, oracle_mod):
     assert rel_l2(uav[grounded], d["u_vav_b"][grounded]) < 0.2
 
 
+def test_oracle_first_iteration_viscosity(pkg, oracle_mod):
+    """The learned start's first-iteration viscosity in the oracle: it changes the Picard path,
+    the solve still converges to its tolerance near the plain solve, and the next solve consumes it
+    (no reference counterpart; the GPU path is compared with this in tests/test_gnn.py)."""
+    mesh, ice, params = pkg.geometry.small_dome()
+    orc = oracle_mod.Oracle(mesh)
+    a, b, c = (pkg.new_ssa_state(mesh.nTri) for _ in range(3))
+    nva, _, sta = orc.solve_SSA(ice, a, params)
+    orc.set_first_viscosity(np.full(mesh.nV, 3e8))
+    nvb, _, stb = orc.solve_SSA(ice, b, params)
+    nvc, _, stc = orc.solve_SSA(ice, c, params)          # consumed: the plain solve again
+    assert sta["status"] == stb["status"] == stc["status"] == 0
+    assert (nvb != nva) or not np.array_equal(a["u_b"], b["u_b"])
+    assert nvc == nva and np.array_equal(a["u_b"], c["u_b"]) and np.array_equal(a["v_b"], c["v_b"])
+    assert rel_l2(np.r_[b["u_b"], b["v_b"]], np.r_[a["u_b"], a["v_b"]]) < 0.05
+
+
 def test_picard_maxit_warning(pkg, oracle_mod):
     mesh, ice, params = pkg.geometry.small_dome()
     params.visc_it_nit = 2

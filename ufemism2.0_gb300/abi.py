@@ -354,6 +354,7 @@ EXPORTS = {
     "ufe_gnn_train": (C.c_int32, [C.c_void_p, C.c_int32, C.c_float, C.c_uint64, fptr, dptr]),
     "ufe_gnn_evaluate": (C.c_int32, [C.c_void_p, dptr]),
     "ufe_gnn_predict_velocity": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, dptr]),
+    "ufe_gnn_predict_start": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_int32, dptr]),
 }
 
 _LIB = None

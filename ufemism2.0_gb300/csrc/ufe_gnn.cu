@@ -79,7 +79,7 @@ __global__ void __launch_bounds__(128) k_gemm_tile_test(int M, int K, const __nv
 // The network.  Nodes are triangles; each has up to three neighbours (TriC).  Width C = 64.
 //   h0      = relu(We x + be)                                  (x: FIN = 16 features, zero-padded)
 //   layer l: a = mean_{j in N(i)} h_j;  t = relu(W1 [h, a] + b1);  h <- h + W2 t + b2   (4 layers)
-//   y       = Wd h + bd                                        (2 outputs: u, v scaled)
+//   y       = Wd h + bd        (kGnnOut = 3 outputs: u, v scaled, and the log-viscosity)
 // BF16 operands, FP32 accumulation (TMEM) and FP32 activations in global memory.
 constexpr int kC = 64;
 constexpr int kFin = 16;
@@ -91,9 +91,9 @@ constexpr int kOffWe = 0;                                   // [64 x 16]
 constexpr int kOffBe = kOffWe + kC * kFin;                  // [64]
 constexpr int kOffL0 = kOffBe + kC;
 constexpr int kLayerSize = kC * 2 * kC + kC + kC * kC + kC; // W1 [64x128], b1, W2 [64x64], b2
-constexpr int kOffWd = kOffL0 + kLayers * kLayerSize;       // [2 x 64]
-constexpr int kOffBd = kOffWd + 2 * kC;                     // [2]
-constexpr int kParams = kOffBd + 2;
+constexpr int kOffWd = kOffL0 + kLayers * kLayerSize;       // [kGnnOut x 64]
+constexpr int kOffBd = kOffWd + kGnnOut * kC;               // [kGnnOut]
+constexpr int kParams = kOffBd + kGnnOut;
 __host__ __device__ constexpr int off_W1(int l) { return kOffL0 + l * kLayerSize; }
 __host__ __device__ constexpr int off_b1(int l) { return off_W1(l) + kC * 2 * kC; }
 __host__ __device__ constexpr int off_W2(int l) { return off_b1(l) + kC; }
@@ -328,25 +328,32 @@ __global__ void k_gnn_decoder(Graph g, const float *__restrict__ prm, const floa
   double l = 0.0;
   if (i < g.n) {
     const float *hi = h + i * kC;
-    float y0 = prm[kOffBd], y1 = prm[kOffBd + 1];
-    float s0 = 0.f, s1 = 0.f;
-    for (int k = 0; k < kC; ++k) {
-      s0 += prm[kOffWd + k] * hi[k];
-      s1 += prm[kOffWd + kC + k] * hi[k];
+    float yo[kGnnOut];
+#pragma unroll
+    for (int c = 0; c < kGnnOut; ++c) {
+      float sc = 0.f;
+      for (int k = 0; k < kC; ++k) sc += prm[kOffWd + c * kC + k] * hi[k];
+      yo[c] = prm[kOffBd + c] + sc;
+      y[kGnnOut * i + c] = yo[c];
     }
-    y0 += s0;
-    y1 += s1;
-    y[2 * i] = y0;
-    y[2 * i + 1] = y1;
     if (target) {
-      const float e0 = y0 - target[2 * i], e1 = y1 - target[2 * i + 1];
       const float wi = w[i];
-      l = (double)wi * ((double)e0 * e0 + (double)e1 * e1);
-      const float d0 = 2.f * wi * e0, d1 = 2.f * wi * e1;
+      float d[kGnnOut];
+#pragma unroll
+      for (int c = 0; c < kGnnOut; ++c) {
+        const float e = yo[c] - target[kGnnOut * i + c];
+        l += (double)wi * ((double)e * e);
+        d[c] = 2.f * wi * e;
+      }
       float *dhi = dh + i * kC;
-      for (int k = 0; k < kC; ++k) dhi[k] = prm[kOffWd + k] * d0 + prm[kOffWd + kC + k] * d1;
-      y[2 * i] = d0;       // dy replaces y when training
-      y[2 * i + 1] = d1;
+      for (int k = 0; k < kC; ++k) {
+        float a = 0.f;
+#pragma unroll
+        for (int c = 0; c < kGnnOut; ++c) a += prm[kOffWd + c * kC + k] * d[c];
+        dhi[k] = a;
+      }
+#pragma unroll
+      for (int c = 0; c < kGnnOut; ++c) y[kGnnOut * i + c] = d[c];   // dy replaces y when training
     }
   }
   if (loss_part) {
@@ -566,25 +573,30 @@ __global__ void k_gnn_wgrad_reduce(int mode, int layer, int nparts, const float 
 
 // decoder gradient partials: per block, dWd[c][k] = sum_i dy_i[c] h_i[k] and dbd[c] over a fixed
 // node range; one warp per node row (lane k reads h[k], h[k+32]), warps combined in order.
-constexpr int kDecParts = 2 * kC + 2;
+constexpr int kDecParts = kGnnOut * kC + kGnnOut;
+static_assert(kDecParts <= 256, "the decoder partials are summed by one 256-thread block");
 __global__ void k_gnn_decoder_grad(Graph g, const float *__restrict__ dy, const float *__restrict__ h,
                                    float *__restrict__ part) {
   __shared__ float red[8][kDecParts];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  float a00 = 0.f, a01 = 0.f, a10 = 0.f, a11 = 0.f, b0 = 0.f, b1 = 0.f;
+  float a0[kGnnOut], a1[kGnnOut], b[kGnnOut];
+#pragma unroll
+  for (int c = 0; c < kGnnOut; ++c) a0[c] = a1[c] = b[c] = 0.f;
   for (int64_t i = (int64_t)blockIdx.x * nw + warp; i < g.n; i += (int64_t)gridDim.x * nw) {
-    const float d0 = dy[2 * i], d1 = dy[2 * i + 1];
     const float h0 = h[i * kC + lane], h1 = h[i * kC + lane + 32];
-    a00 += d0 * h0; a01 += d0 * h1; a10 += d1 * h0; a11 += d1 * h1;
-    b0 += d0; b1 += d1;
+#pragma unroll
+    for (int c = 0; c < kGnnOut; ++c) {
+      const float d = dy[kGnnOut * i + c];
+      a0[c] += d * h0;
+      a1[c] += d * h1;
+      b[c] += d;
+    }
   }
-  red[warp][lane] = a00;
-  red[warp][lane + 32] = a01;
-  red[warp][kC + lane] = a10;
-  red[warp][kC + lane + 32] = a11;
-  if (lane == 0) {
-    red[warp][2 * kC] = b0;
-    red[warp][2 * kC + 1] = b1;
+#pragma unroll
+  for (int c = 0; c < kGnnOut; ++c) {
+    red[warp][c * kC + lane] = a0[c];
+    red[warp][c * kC + lane + 32] = a1[c];
+    if (lane == 0) red[warp][kGnnOut * kC + c] = b[c];
   }
   __syncthreads();
   if ((int)threadIdx.x < kDecParts) {
@@ -599,7 +611,7 @@ __global__ void k_gnn_decoder_reduce(int nparts, const float *__restrict__ part,
   if (t >= kDecParts) return;
   float s = 0.f;
   for (int p = 0; p < nparts; ++p) s += part[(int64_t)p * kDecParts + t];
-  grad[t < 2 * kC ? kOffWd + t : kOffBd + (t - 2 * kC)] = s;
+  grad[t < kGnnOut * kC ? kOffWd + t : kOffBd + (t - kGnnOut * kC)] = s;
 }
 
 // Adam (FP32) on the flat parameter vector
@@ -746,7 +758,7 @@ void gnn_ensure(ufe_gnn *g, int64_t n) {
   g->dhB = (float *)dev_alloc(rows * 4);
   g->dacc = (float *)dev_alloc(rows * 4);
   g->dA = (float *)dev_alloc(rows * 4);
-  g->ybuf = (float *)dev_alloc((size_t)n * 2 * 4);
+  g->ybuf = (float *)dev_alloc((size_t)n * kGnnOut * 4);
   const int64_t nb = (n + 255) / 256;
   g->loss_part = (double *)dev_alloc(sizeof(double) * nb);
   if (g->loss_cap < nb) {
@@ -763,7 +775,7 @@ void gnn_ensure_scratch(ufe_gnn *g, int64_t n) {
   for (void *p : ptrs) dev_free(p);
   g->gnbr = (int32_t *)dev_alloc(sizeof(int32_t) * 3 * n);
   g->gx = (float *)dev_alloc(sizeof(float) * kFin * n);
-  g->gy = (float *)dev_alloc(sizeof(float) * 2 * n);
+  g->gy = (float *)dev_alloc(sizeof(float) * kGnnOut * n);
   g->gw = (float *)dev_alloc(sizeof(float) * n);
   g->gmask = (float *)dev_alloc(sizeof(float) * n);
   g->gcap = n;
@@ -820,7 +832,7 @@ void gnn_backward(ufe_gnn *g, cudaStream_t s, const Graph &gr, const float *x) {
   const unsigned tiles = (unsigned)((gr.n + 127) / 128);
   k_gnn_decoder_grad<<<kDecBlocks, 256, 0, s>>>(gr, g->ybuf, g->h[kLayers], g->dpart);
   UFE_CUDA(cudaGetLastError());
-  k_gnn_decoder_reduce<<<1, 160, 0, s>>>(kDecBlocks, g->dpart, g->grad);
+  k_gnn_decoder_reduce<<<1, 256, 0, s>>>(kDecBlocks, g->dpart, g->grad);   // kDecParts <= 256
   UFE_CUDA(cudaGetLastError());
   float *cur = g->dhA, *nxt = g->dhB;
   for (int l = kLayers - 1; l >= 0; --l) {
@@ -881,7 +893,7 @@ std::vector<float> init_params(uint64_t seed) {
     fill(off_W1(l), kC, 2 * kC, std::sqrt(2.0));
     fill(off_W2(l), kC, kC, 0.5);   // small residual branches at the start
   }
-  fill(kOffWd, 2, kC, 1.0);
+  fill(kOffWd, kGnnOut, kC, 1.0);
   return p;
 }
 
@@ -989,7 +1001,7 @@ extern "C" int32_t ufe_gnn_forward(ufe_gnn *g, int64_t n, const int32_t *nbr, co
     cudaStream_t s = g->ctx->stream;
     const Graph gr = upload_graph(g, s, n, nbr, x);
     gnn_forward(g, s, gr, g->gx, nullptr, nullptr);
-    UFE_CUDA(cudaMemcpyAsync(y, g->ybuf, sizeof(float) * 2 * n, cudaMemcpyDeviceToHost, s));
+    UFE_CUDA(cudaMemcpyAsync(y, g->ybuf, sizeof(float) * kGnnOut * n, cudaMemcpyDeviceToHost, s));
     gnn_check(g, s);
     return UFE_OK;
   });
@@ -1003,7 +1015,7 @@ extern "C" int32_t ufe_gnn_loss_grad(ufe_gnn *g, int64_t n, const int32_t *nbr, 
     UFE_CUDA(cudaSetDevice(g->ctx->device));
     cudaStream_t s = g->ctx->stream;
     const Graph gr = upload_graph(g, s, n, nbr, x);
-    UFE_CUDA(cudaMemcpyAsync(g->gy, target, sizeof(float) * 2 * n, cudaMemcpyHostToDevice, s));
+    UFE_CUDA(cudaMemcpyAsync(g->gy, target, sizeof(float) * kGnnOut * n, cudaMemcpyHostToDevice, s));
     UFE_CUDA(cudaMemcpyAsync(g->gw, w, sizeof(float) * n, cudaMemcpyHostToDevice, s));
     gnn_forward(g, s, gr, g->gx, g->gy, g->gw);
     gnn_backward(g, s, gr, g->gx);
@@ -1029,7 +1041,7 @@ extern "C" int32_t ufe_gnn_dataset_add(ufe_gnn *g, ufe_ctx *mesh_ctx, const floa
     m.n = n;
     m.nbr = (int32_t *)dev_alloc(sizeof(int32_t) * 3 * n);
     m.x = (float *)dev_alloc(sizeof(float) * kFin * n);
-    m.y = (float *)dev_alloc(sizeof(float) * 2 * n);
+    m.y = (float *)dev_alloc(sizeof(float) * kGnnOut * n);
     m.w = (float *)dev_alloc(sizeof(float) * n);
     try {
       gnn_mesh_graph(mesh_ctx, s, m.nbr);
@@ -1045,6 +1057,7 @@ extern "C" int32_t ufe_gnn_dataset_add(ufe_gnn *g, ufe_ctx *mesh_ctx, const floa
         gnn_mesh_features(mesh_ctx, s, 0, m.x, nullptr);
       }
       gnn_mesh_velocity(mesh_ctx, s, m.y, false, nullptr);
+      gnn_mesh_viscosity(mesh_ctx, s, m.y, false, nullptr);
       // loss weights: triangles with ice, equal weights summing to one
       std::vector<float> hx((size_t)kFin * n);
       UFE_CUDA(cudaMemcpyAsync(hx.data(), m.x, sizeof(float) * kFin * n, cudaMemcpyDeviceToHost, s));
@@ -1165,15 +1178,17 @@ extern "C" int32_t ufe_gnn_evaluate(ufe_gnn *g, double *mean_loss) {
 // Warm start: predict the velocity of the mesh context's resident ice state and store it as the
 // resident velocity, so that ufe_solve_ssa_resident / ufe_solve_diva_resident with cold_start = 0
 // start the Picard loop from it; `smooth_passes` averaging passes over each triangle and its
-// neighbours take the prediction's small-scale noise out first.
-// Kernels one ufe_gnn_predict_velocity launches: graph, features, encoder, the layers, decoder,
-// velocity store, and two per smoothing pass.
+// neighbours take the prediction's small-scale noise out first.  With `with_viscosity` the
+// predicted vertically averaged viscosity is stored on the vertices as well and the next solve's
+// first Picard iteration uses it in place of Glen's law (SSA: the viscosity; DIVA: every layer).
+// Kernels one prediction launches: graph, features, encoder, the layers, decoder, velocity store,
+// two per smoothing pass, and the viscosity store.
 extern "C" int32_t ufe_gnn_predict_kernels(int32_t smooth_passes) {
   return 1 + 1 + (2 + kLayers) + 1 + 2 * (smooth_passes > 0 ? smooth_passes : 0);
 }
 
-extern "C" int32_t ufe_gnn_predict_velocity(ufe_gnn *g, ufe_ctx *mesh_ctx, int32_t use_prev_velocity,
-                                            int32_t smooth_passes, double *device_ms) {
+extern "C" int32_t ufe_gnn_predict_start(ufe_gnn *g, ufe_ctx *mesh_ctx, int32_t use_prev_velocity,
+                                         int32_t smooth_passes, int32_t with_viscosity, double *device_ms) {
   if (!g || !mesh_ctx) return UFE_ERR_INVALID;
   return guarded(g->ctx, [&]() -> int32_t {
     UFE_REQUIRE(mesh_ctx->device == g->ctx->device, UFE_ERR_INVALID, "gnn and mesh contexts on different devices");
@@ -1189,6 +1204,7 @@ extern "C" int32_t ufe_gnn_predict_velocity(ufe_gnn *g, ufe_ctx *mesh_ctx, int32
     gnn_forward(g, s, Graph{n, g->gnbr}, g->gx, nullptr, nullptr);
     gnn_mesh_velocity(mesh_ctx, s, g->ybuf, true, g->gmask);
     if (smooth_passes > 0) gnn_mesh_smooth(mesh_ctx, s, smooth_passes, g->gmask);
+    if (with_viscosity) gnn_mesh_viscosity(mesh_ctx, s, g->ybuf, true, g->gmask);
     UFE_CUDA(cudaEventRecord(mesh_ctx->ev1, s));
     gnn_check(g, s);
     if (device_ms) {
@@ -1198,4 +1214,9 @@ extern "C" int32_t ufe_gnn_predict_velocity(ufe_gnn *g, ufe_ctx *mesh_ctx, int32
     }
     return UFE_OK;
   });
+}
+
+extern "C" int32_t ufe_gnn_predict_velocity(ufe_gnn *g, ufe_ctx *mesh_ctx, int32_t use_prev_velocity,
+                                            int32_t smooth_passes, double *device_ms) {
+  return ufe_gnn_predict_start(g, mesh_ctx, use_prev_velocity, smooth_passes, 0, device_ms);
 }

@@ -71,6 +71,8 @@ struct PicardScalars {
   int32_t prev_total_its;
   int32_t phase;       // inexact Picard (krylov_forcing > 0): 0 while forced, 1 once exact solves verify
   int32_t nconv0;      // consecutive forced iterations whose change norm met the tolerance
+  int32_t use_pred;    // the first iteration takes the learned start's predicted viscosity
+  int32_t pad_;
   double hist[kHistMax * kHistCols];
 };
 
@@ -155,6 +157,13 @@ void gnn_mesh_features(ufe_ctx *ctx, cudaStream_t s, int use_prev, float *x, flo
 void gnn_mesh_graph(ufe_ctx *ctx, cudaStream_t s, int32_t *nbr);
 void gnn_mesh_velocity(ufe_ctx *ctx, cudaStream_t s, float *y, bool to_state, const float *mask);
 void gnn_mesh_smooth(ufe_ctx *ctx, cudaStream_t s, int passes, const float *mask);
+void gnn_mesh_viscosity(ufe_ctx *ctx, cudaStream_t s, float *y, bool to_state, const float *mask);
+
+// The network's outputs per triangle: u / 1e3, v / 1e3 (m/yr) and the vertically averaged
+// effective viscosity as (log10(eta) - kGnnLogEtaOff) / kGnnLogEtaScale (eta in Pa yr).
+constexpr int kGnnOut = 3;
+constexpr double kGnnLogEtaOff = 7.5;
+constexpr double kGnnLogEtaScale = 2.0;
 
 // ufe_layout.cu: internal (Z-order) numbering and the mappings at the ABI boundary
 void layout_upload_mesh(ufe_ctx *ctx, const ufe_mesh_desc *m);

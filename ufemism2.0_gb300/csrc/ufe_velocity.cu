@@ -90,23 +90,44 @@ PhysParams make_phys(const ufe_solver_params &p, int has_bc) {
   return q;
 }
 
+// e^((1-n)/(2n)), the strain-rate power of Glen's law.  For the usual n = 3 the exponent is -1/3 and
+// the reciprocal cube root replaces the general power (several times fewer FP64 instructions, which
+// bound the viscosity passes on this GPU); n = 1 gives 1.  Both agree with pow to within an ulp or so.
+__device__ __forceinline__ double glen_epow(double e, double n) {
+  if (n == 3.0) return rcbrt(e);
+  if (n == 1.0) return 1.0;
+  return pow(e, (1.0 - n) / (2.0 * n));
+}
+
 // calc_effective_viscosity_Glen_2D / _3D_uv_only (constitutive_equation.f90:25-80)
 // Glen's flow law, 3-D (constitutive_equation.f90:25-80), with A^(-1/n) evaluated beforehand:
 // 0.5 A^(-1/n) (eps^2 + eps0^2)^((1-n)/(2n))
 __device__ __forceinline__ double glen_apow(double eps0, double ux, double uy, double vx, double vy,
                                             double uz, double vz, double A_pow, double n) {
   double e = ux * ux + vy * vy + ux * vy + 0.25 * ((uy + vx) * (uy + vx)) + 0.25 * (uz * uz + vz * vz) + eps0;
-  return 0.5 * A_pow * pow(e, (1.0 - n) / (2.0 * n));
+  return 0.5 * A_pow * glen_epow(e, n);
 }
 __device__ __forceinline__ double glen2d(double eps0, double ux, double uy, double vx, double vy,
                                          double A, double n) {
   double e = ux * ux + vy * vy + ux * vy + 0.25 * ((uy + vx) * (uy + vx)) + eps0;
-  return 0.5 * pow(A, -1.0 / n) * pow(e, (1.0 - n) / (2.0 * n));
+  return 0.5 * (n == 3.0 ? rcbrt(A) : pow(A, -1.0 / n)) * glen_epow(e, n);
 }
 
 struct SlidingIn {
   const double *beta_sq, *alpha_sq, *effp, *tys;
 };
+
+// x^(1/m) and x^m of the sliding exponent; the usual m = 3 (and m = 1) without the general power
+__device__ __forceinline__ double pow_inv_m(double x, double m) {
+  if (m == 3.0) return cbrt(x);
+  if (m == 1.0) return x;
+  return pow(x, 1.0 / m);
+}
+__device__ __forceinline__ double pow_m(double x, double m) {
+  if (m == 3.0) return x * x * x;
+  if (m == 1.0) return x;
+  return pow(x, m);
+}
 
 // velocity-dependent part of the sliding laws (sliding_laws.f90:25-351) and the beta_max cap (:76)
 __device__ double sliding_beta(const PhysParams &q, const SlidingIn &s, int vi, double u, double v) {
@@ -114,18 +135,18 @@ __device__ double sliding_beta(const PhysParams &q, const SlidingIn &s, int vi, 
   double m = q.m_weertman, beta = 0.0;
   switch (q.sliding_law) {
     case UFE_SLIDING_NO_SLIDING: beta = 0.0; break;
-    case UFE_SLIDING_WEERTMAN: beta = s.beta_sq[vi] * pow(uabs, 1.0 / m - 1.0); break;
+    case UFE_SLIDING_WEERTMAN: beta = s.beta_sq[vi] * (pow_inv_m(uabs, m) / uabs); break;
     case UFE_SLIDING_COULOMB: beta = s.tys[vi] / uabs; break;
     case UFE_SLIDING_BUDD:
       beta = s.tys[vi] * pow(uabs, q.budd_q - 1.0) / pow(q.budd_u0, q.budd_q);
       break;
     case UFE_SLIDING_TSAI2015:
-      beta = fmin(s.alpha_sq[vi] * s.effp[vi], s.beta_sq[vi] * pow(uabs, 1.0 / m)) * pow(uabs, -1.0);
+      beta = fmin(s.alpha_sq[vi] * s.effp[vi], s.beta_sq[vi] * pow_inv_m(uabs, m)) / uabs;
       break;
     case UFE_SLIDING_SCHOOF2005: {
       double b = s.beta_sq[vi], aN = s.alpha_sq[vi] * s.effp[vi];
-      beta = ((b * pow(uabs, 1.0 / m) * s.alpha_sq[vi] * s.effp[vi]) / pow(pow(b, m) * uabs + pow(aN, m), 1.0 / m)) *
-             pow(uabs, -1.0);
+      beta = ((b * pow_inv_m(uabs, m) * s.alpha_sq[vi] * s.effp[vi]) / pow_inv_m(pow_m(b, m) * uabs + pow_m(aN, m), m)) /
+             uabs;
       break;
     }
     case UFE_SLIDING_ZOET_IVERSON:   // :399-400
@@ -149,7 +170,7 @@ struct OpRow {  // a CSR family with shared pattern
 __global__ void k_prologue(int nV, int nTri, int nz, OpRow ab, const double *Hi, const double *Hs,
                            const double *A_flow, const double *zeta, double2 *tau_d, double *Avav,
                            double *A_pow, PicardScalars *ps, KrylovScalars *ks, double relax0, double eps0,
-                           double n_glen) {
+                           double n_glen, int32_t *pred_flag) {
   int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < nTri; t += stride) {
     double Hib = 0.0, dx = 0.0, dy = 0.0;
@@ -186,6 +207,8 @@ __global__ void k_prologue(int nV, int nTri, int nz, OpRow ab, const double *Hi,
     p.prev_total_its = 0;
     p.phase = 0;
     p.nconv0 = 0;
+    p.use_pred = *pred_flag;   // consumed: a later solve starts from its own viscosity again
+    *pred_flag = 0;
     p.active = 1;
     KrylovScalars k;
     memset(&k, 0, sizeof(k));
@@ -259,9 +282,13 @@ __global__ void k_diva_shear_b(int nTri, int nz, const double2 *tau_b, const dou
 // calc_horizontal_strain_rates (SSA_DIVA_utilities.f90:59-82), calc_effective_viscosity
 // (SSA_main.f90:339-392) up to N_a, and the vertex part of calc_basal_friction_coefficient
 // (sliding_laws.f90:25-81): all from one pass over the b->a operator row.
+// eta_pred: the learned start's predicted viscosity, which replaces Glen's law in the first
+// iteration of a solve that the prediction armed (no reference counterpart).
 __global__ void k_vertex_ssa(int nV, OpRow ba, const double2 *uv, const double *Avav, const double *Hi,
-                             SlidingIn sl, PhysParams q, const PicardScalars *ps, double *N_a, double *beta_a) {
+                             SlidingIn sl, PhysParams q, const PicardScalars *ps, const double *eta_pred,
+                             double *N_a, double *beta_a) {
   const double eps0 = ps->eps0, eta_max = ps->eta_max;
+  const bool pred = ps->use_pred != 0 && ps->it == 0;
   int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t vi = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; vi < nV; vi += stride) {
     double ux = 0, uy = 0, vx = 0, vy = 0, ua = 0, va = 0;
@@ -275,7 +302,7 @@ __global__ void k_vertex_ssa(int nV, OpRow ba, const double2 *uv, const double *
       ua = ua + m * w.x;
       va = va + m * w.y;
     }
-    double eta = glen2d(eps0, ux, uy, vx, vy, Avav[vi], q.n_glen);
+    double eta = pred ? eta_pred[vi] : glen2d(eps0, ux, uy, vx, vy, Avav[vi], q.n_glen);
     eta = fmin(fmax(eta, q.visc_eff_min), eta_max);
     N_a[vi] = eta * fmax(0.1, Hi[vi]);
     beta_a[vi] = sliding_beta(q, sl, (int)vi, ua, va);
@@ -286,83 +313,76 @@ __global__ void k_vertex_ssa(int nV, OpRow ba, const double2 *uv, const double *
 // calc_horizontal_strain_rates, calc_vertical_shear_strain_rates (DIVA_main.f90:375-410),
 // calc_effective_viscosity (:412-479), the surface value of calc_F_integrals' F2 (:481-520) and
 // the vertex part of calc_effective_basal_friction_coefficient (:522-574).
-// One group of G lanes per vertex, one lane per layer (layers beyond G strided): the 3-D
-// viscosity of each layer -- a pow per layer, FP64 and latency-bound -- runs in parallel across the
-// group instead of in one thread's loop.  Every lane forms the vertex's horizontal strain rates (the
-// same loads, broadcast within the warp); lane 0 then sums the vertical average and the F2 integral
-// over the layers in the reference's order and evaluates the sliding law, so every value is the
-// one the one-thread-per-vertex form gives.  The loop runs over whole warps so that __syncwarp()
-// sees all 32 lanes.
-template <int G>
-__global__ void __launch_bounds__(256) k_vertex_diva(int nV, int nTri, int nz, OpRow ba, const double2 *uv,
-                                                     const double2 *uv_base, const double2 *duz_b,
-                                                     const double *A_pow, const double *Hi, const double *zeta_g,
-                                                     SlidingIn sl, PhysParams q, const PicardScalars *ps,
-                                                     double *eta_3D_a, double *N_a, double *F2a1, double *beta_a,
-                                                     double *beta_eff_a) {
-  constexpr int kGroups = 256 / G;
-  __shared__ double zeta[kMaxNz];
-  __shared__ double eta_s[kGroups][kMaxNz];
-  __shared__ double f2_s[kGroups][kMaxNz];
+// One thread per vertex, the layers in a loop.  The FP64 pipe issues a warp instruction at the
+// same cost whatever its active mask, so this pass -- bound by that pipe (the layers' powers, the
+// divisions of F2 and the sliding law) -- keeps every lane busy on its own vertex; per-layer loads
+// and stores of the [layer][vertex] fields stay coalesced across the warp.  du/dz and dv/dz on the
+// triangles come in precomputed (duz_b, formed once per triangle).  The vertical average is summed
+// on the fly in the reference's order (zeta increasing); the F2 integral runs from the base up, so
+// its per-layer terms wait in shared memory, layer-major with one column per thread.
+// In the first iteration of a solve the learned start armed, every layer takes the predicted
+// vertically averaged viscosity eta_pred instead (a depth-uniform first viscosity).
+// Dynamic shared memory: (kMaxNz + nz * blockDim.x) doubles.
+__global__ void __launch_bounds__(128, 4) k_vertex_diva(int nV, int nTri, int nz, OpRow ba, const double2 *uv,
+                                                        const double2 *uv_base, const double2 *duz_b,
+                                                        const double *A_pow, const double *Hi, const double *zeta_g,
+                                                        SlidingIn sl, PhysParams q, const PicardScalars *ps,
+                                                        const double *eta_pred, double *eta_3D_a, double *N_a,
+                                                        double *F2a1, double *beta_a, double *beta_eff_a) {
+  extern __shared__ double vsm[];
+  double *zeta = vsm, *f2 = vsm + kMaxNz + threadIdx.x;
   for (int k = threadIdx.x; k < nz; k += blockDim.x) zeta[k] = zeta_g[k];
   __syncthreads();
   const double eps0 = ps->eps0, eta_max = ps->eta_max;
+  const bool pred = ps->use_pred != 0 && ps->it == 0;
   const float h_floor_sp = 0.1f;  // max(0.1, Hi) with a default-real literal (DIVA_main.f90:468)
-  const int lane = threadIdx.x % G, grp = threadIdx.x / G;
-  const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / 32;
-  const int64_t warps = (int64_t)gridDim.x * blockDim.x / 32;
-  for (int64_t v0 = warp * (32 / G); v0 < nV; v0 += warps * (32 / G)) {
-    const int64_t vi = v0 + (threadIdx.x % 32) / G;
-    const bool live = vi < nV;
-    if (live) {
-      const int k1 = ba.ptr[vi], k2 = ba.ptr[vi + 1];
-      double ux = 0, uy = 0, vx = 0, vy = 0;
-      for (int k = k1; k < k2; ++k) {
-        const double2 w = uv[ba.ind[k]];
-        const double dx = ba.v1[k], dy = ba.v2[k];
-        ux = ux + dx * w.x;
-        uy = uy + dy * w.x;
-        vx = vx + dx * w.y;
-        vy = vy + dy * w.y;
-      }
-      for (int l = lane; l < nz; l += G) {
+  const int bd = blockDim.x;
+  const int64_t stride = (int64_t)gridDim.x * bd;
+  for (int64_t vi = (int64_t)blockIdx.x * bd + threadIdx.x; vi < nV; vi += stride) {
+    const int k1 = ba.ptr[vi], k2 = ba.ptr[vi + 1];
+    double ux = 0, uy = 0, vx = 0, vy = 0, ua = 0, va = 0;
+    for (int k = k1; k < k2; ++k) {
+      const int t = ba.ind[k];
+      const double2 w = uv[t], wb = uv_base[t];
+      const double m = ba.v0[k], dx = ba.v1[k], dy = ba.v2[k];
+      ux = ux + dx * w.x;
+      uy = uy + dy * w.x;
+      vx = vx + dx * w.y;
+      vy = vy + dy * w.y;
+      ua = ua + m * wb.x;
+      va = va + m * wb.y;
+    }
+    double vav = 0.0, e_prev = 0.0;
+    const double e_pred = pred ? eta_pred[vi] : 0.0;
+    for (int l = 0; l < nz; ++l) {
+      const int64_t ix = (int64_t)l * nV + vi;
+      double e = e_pred;
+      if (!pred) {
         double duz = 0.0, dvz = 0.0;
+        const double2 *dl = duz_b + (int64_t)l * nTri;
         for (int k = k1; k < k2; ++k) {
-          const double2 d = duz_b[(int64_t)l * nTri + ba.ind[k]];
+          const double2 d = dl[ba.ind[k]];
           const double m = ba.v0[k];
           duz = duz + m * d.x;
           dvz = dvz + m * d.y;
         }
-        const int64_t ix = (int64_t)l * nV + vi;
-        double e = glen_apow(eps0, ux, uy, vx, vy, duz, dvz, A_pow[ix], q.n_glen);
-        e = fmin(fmax(e, q.visc_eff_min), eta_max);
-        eta_s[grp][l] = e;
-        f2_s[grp][l] = zeta[l] * zeta[l] / e;
-        eta_3D_a[ix] = e;
+        e = glen_apow(eps0, ux, uy, vx, vy, duz, dvz, A_pow[ix], q.n_glen);
       }
+      e = fmin(fmax(e, q.visc_eff_min), eta_max);
+      eta_3D_a[ix] = e;
+      f2[l * bd] = zeta[l] * zeta[l] / e;
+      if (l > 0) vav = vav + 0.5 * (e + e_prev) * (zeta[l] - zeta[l - 1]);
+      e_prev = e;
     }
-    __syncwarp();
-    if (live && lane == 0) {
-      double vav = 0.0;
-      for (int l = 1; l < nz; ++l) vav = vav + 0.5 * (eta_s[grp][l] + eta_s[grp][l - 1]) * (zeta[l] - zeta[l - 1]);
-      N_a[vi] = vav * fmax((double)h_floor_sp, Hi[vi]);
-      // F2 at the surface: integrate zeta^2/eta from the base (zeta = 1) up to zeta(1) = 0
-      double intg = 0.0;
-      for (int l = nz - 1; l >= 1; --l) intg = intg - 0.5 * (f2_s[grp][l] + f2_s[grp][l - 1]) * (zeta[l] - zeta[l - 1]);
-      const double F2 = -fmax(0.1, Hi[vi]) * intg;
-      F2a1[vi] = F2;
-      double ua = 0, va = 0;
-      for (int k = ba.ptr[vi]; k < ba.ptr[vi + 1]; ++k) {
-        const double2 wb = uv_base[ba.ind[k]];
-        const double m = ba.v0[k];
-        ua = ua + m * wb.x;
-        va = va + m * wb.y;
-      }
-      const double b = sliding_beta(q, sl, (int)vi, ua, va);
-      beta_a[vi] = b;
-      beta_eff_a[vi] = (q.sliding_law == UFE_SLIDING_NO_SLIDING) ? 1.0 / F2 : b / (1.0 + b * F2);
-    }
-    __syncwarp();
+    N_a[vi] = vav * fmax((double)h_floor_sp, Hi[vi]);
+    // F2 at the surface: integrate zeta^2/eta from the base (zeta = 1) up to zeta(1) = 0
+    double intg = 0.0;
+    for (int l = nz - 1; l >= 1; --l) intg = intg - 0.5 * (f2[l * bd] + f2[(l - 1) * bd]) * (zeta[l] - zeta[l - 1]);
+    const double F2 = -fmax(0.1, Hi[vi]) * intg;
+    F2a1[vi] = F2;
+    const double b = sliding_beta(q, sl, (int)vi, ua, va);
+    beta_a[vi] = b;
+    beta_eff_a[vi] = (q.sliding_law == UFE_SLIDING_NO_SLIDING) ? 1.0 / F2 : b / (1.0 + b * F2);
   }
 }
 
@@ -1172,6 +1192,8 @@ Work *ensure_work(ufe_ctx *ctx) {
   w->beta_eff_a = alloc_n<double>(nV);
   w->F2a1 = alloc_n<double>(nV);
   w->eta_3D_a = alloc_n<double>((size_t)nV * nz);
+  w->eta_pred_a = alloc_n<double>(nV);
+  w->pred_flag = alloc_n<int32_t>(1);
   build_sell(ctx, w);
   w->ppart = alloc_n<double>((size_t)3 * kPersistMaxBlocks * kPersistSlots);
   w->gsync = alloc_n<GridSync>(1);
@@ -1192,6 +1214,7 @@ Work *ensure_work(ufe_ctx *ctx) {
   UFE_CUDA(cudaMemsetAsync(w->eta_3D_b, 0, sizeof(double) * (size_t)nTri * nz, s));
   UFE_CUDA(cudaMemsetAsync(w->ks, 0, sizeof(KrylovScalars) * 3, s));
   UFE_CUDA(cudaMemsetAsync(w->err, 0, sizeof(int), s));
+  UFE_CUDA(cudaMemsetAsync(w->pred_flag, 0, sizeof(int32_t), s));
   UFE_CUDA(cudaStreamSynchronize(s));
   return w;
 }
@@ -1214,7 +1237,7 @@ void free_work(ufe_ctx *ctx) {
                   w->sell_blk32, w->halo_off, w->halo_idx, w->halo_lcol, w->pX, w->pR, w->pRP, w->pS, w->pT,
                   w->pdinv, w->pP[0], w->pP[1], w->pV[0], w->pV[1], w->sell_blkp, w->pair_bad,
                   w->Ti, w->mask_fl, w->fgr_v, w->Hib, w->SL, w->A_rheo, w->tys_ideal, w->cp_ptr, w->cp_idx,
-                  w->cp_w, w->duz_b};
+                  w->cp_w, w->duz_b, w->eta_pred_a, w->pred_flag};
   for (void *p : ptrs) dev_free(p);
   if (w->ks_host) cudaFreeHost(w->ks_host);
   if (w->ps_host) cudaFreeHost(w->ps_host);
@@ -1378,7 +1401,6 @@ struct Solver {
 
   int eblocks(int64_t n) const { return pick_blocks(n, kThreads, grid); }
   // blocks of 256 threads for one G-lane group per vertex
-  int vertex_blocks(int G) const { return pick_blocks((int64_t)w->nV * G, 256, 1 << 20); }
 
   SlidingIn sliding() const {
     const double *tys = p.choice_sliding_law == UFE_SLIDING_IDEALISED_SSA_ICESTREAM ? w->tys_ideal : w->tys;
@@ -1767,7 +1789,7 @@ struct Solver {
     k_prologue<<<eblocks(std::max(w->nV, w->nTri)), kThreads, 0, s>>>(
         w->nV, w->nTri, w->nz, ab, w->Hi, w->Hs, A_src(), ctx->zeta, w->tau_d, diva ? nullptr : w->Avav,
         diva ? w->A_pow : nullptr, w->ps, w->ks, p.visc_it_relax, p.Glens_flow_law_epsilon_sq_0,
-        p.Glens_flow_law_exponent);
+        p.Glens_flow_law_exponent, w->pred_flag);
     if (diva)
       k_diva_shear_b<<<eblocks(w->nTri), kThreads, 0, s>>>(w->nTri, w->nz, w->tau_b, w->eta_3D_b, ctx->zeta,
                                                            p.visc_eff_min, w->duz_b);
@@ -1777,17 +1799,14 @@ struct Solver {
 
   void enqueue_picard_pre(bool diva, CondArg inner) {
     if (diva) {
-      if (w->nz <= 16)
-        k_vertex_diva<16><<<vertex_blocks(16), 256, 0, s>>>(
-            w->nV, w->nTri, w->nz, ba, w->uv, w->uv_base, w->duz_b, w->A_pow, w->Hi, ctx->zeta,
-            sliding(), q, w->ps, w->eta_3D_a, w->N_a, w->F2a1, w->beta_a, w->beta_eff_a);
-      else
-        k_vertex_diva<32><<<vertex_blocks(32), 256, 0, s>>>(
-            w->nV, w->nTri, w->nz, ba, w->uv, w->uv_base, w->duz_b, w->A_pow, w->Hi, ctx->zeta,
-            sliding(), q, w->ps, w->eta_3D_a, w->N_a, w->F2a1, w->beta_a, w->beta_eff_a);
+      const int tpb = w->nz <= 40 ? 128 : 64;
+      const size_t smem = (size_t)(kMaxNz + w->nz * tpb) * sizeof(double);
+      k_vertex_diva<<<pick_blocks(w->nV, tpb, 1 << 20), tpb, smem, s>>>(
+          w->nV, w->nTri, w->nz, ba, w->uv, w->uv_base, w->duz_b, w->A_pow, w->Hi, ctx->zeta,
+          sliding(), q, w->ps, w->eta_pred_a, w->eta_3D_a, w->N_a, w->F2a1, w->beta_a, w->beta_eff_a);
     } else {
       k_vertex_ssa<<<eblocks(w->nV), kThreads, 0, s>>>(w->nV, ba, w->uv, w->Avav, w->Hi, sliding(), q, w->ps,
-                                                       w->N_a, w->beta_a);
+                                                       w->eta_pred_a, w->N_a, w->beta_a);
     }
     UFE_CUDA(cudaGetLastError());
     enqueue_assemble(diva ? kFromDIVA : kFromSSA, p.krylov_initial_guess == UFE_X0_CURRENT, inner);
@@ -2234,6 +2253,12 @@ static void check_sliding_inputs(const ufe_solver_params *p, const ufe_ice_state
   }
 }
 
+// A start velocity set from outside the learned start (zero, the caller's, a previous solve's)
+// carries no predicted viscosity.
+static void disarm_prediction(Work *w, cudaStream_t s) {
+  UFE_CUDA(cudaMemsetAsync(w->pred_flag, 0, sizeof(int32_t), s));
+}
+
 // Queue a resident solve; false when there is nothing to solve (no grounded ice), in which
 // case the zero velocity is already set and the stats are zero.
 static bool resident_launch(ufe_ctx *ctx, const ufe_solver_params *p, int32_t cold_start, bool diva) {
@@ -2243,6 +2268,7 @@ static bool resident_launch(ufe_ctx *ctx, const ufe_solver_params *p, int32_t co
   cudaStream_t s = ctx->stream;
   const int nTri = ctx->nTri;
   if (cold_start) {
+    disarm_prediction(w, s);
     UFE_CUDA(cudaMemsetAsync(w->uv, 0, sizeof(double2) * nTri, s));
     if (diva) {
       UFE_CUDA(cudaMemsetAsync(w->uv_base, 0, sizeof(double2) * nTri, s));
@@ -2268,6 +2294,7 @@ static int32_t resident_solve(ufe_ctx *ctx, const ufe_solver_params *p, int32_t 
   cudaStream_t s = ctx->stream;
   const int nTri = ctx->nTri;
   if (cold_start) {
+    disarm_prediction(w, s);
     UFE_CUDA(cudaMemsetAsync(w->uv, 0, sizeof(double2) * nTri, s));
     if (diva) {
       UFE_CUDA(cudaMemsetAsync(w->uv_base, 0, sizeof(double2) * nTri, s));
@@ -2341,13 +2368,49 @@ __global__ void k_gnn_graph(int nTri, const int32_t *TriC, int32_t *nbr) {
 __global__ void k_gnn_velocity(int nTri, double2 *uv, float *y, int to_state, const float *mask) {
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= nTri) return;
+  float *yt = y + t * kGnnOut;
   if (to_state) {
     const bool ice = !mask || mask[t] > 0.f;
-    uv[t] = ice ? make_double2((double)y[2 * t] * 1e3, (double)y[2 * t + 1] * 1e3) : make_double2(0.0, 0.0);
+    uv[t] = ice ? make_double2((double)yt[0] * 1e3, (double)yt[1] * 1e3) : make_double2(0.0, 0.0);
   } else {
-    y[2 * t] = (float)(uv[t].x / 1e3);
-    y[2 * t + 1] = (float)(uv[t].y / 1e3);
+    yt[0] = (float)(uv[t].x / 1e3);
+    yt[1] = (float)(uv[t].y / 1e3);
   }
+}
+
+// Training target of the viscosity output: the solve's vertically averaged effective viscosity
+// (N_a / max(0.1, Hi) on the vertices, from the last Picard iteration) mapped to the triangles,
+// as (log10(eta) - kGnnLogEtaOff) / kGnnLogEtaScale.
+__global__ void k_gnn_visc_target(int nTri, OpRow ab, const double *N_a, const double *Hi, float *y) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nTri) return;
+  double e = 0.0;
+  for (int k = ab.ptr[t]; k < ab.ptr[t + 1]; ++k) {
+    const int v = ab.ind[k];
+    e += ab.v0[k] * (N_a[v] / fmax(0.1, Hi[v]));
+  }
+  y[t * kGnnOut + 2] = (float)((log10(fmax(e, 1e-30)) - kGnnLogEtaOff) / kGnnLogEtaScale);
+}
+
+// The predicted viscosity on the vertices: the b->a map of the log-viscosity output over the
+// vertex's triangles with ice (all of them where none has ice), then arms the next solve.
+__global__ void k_gnn_visc_pred(int nV, OpRow ba, const float *y, const float *mask, double *eta_a,
+                                int32_t *pred_flag) {
+  const int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (v == 0) *pred_flag = 1;
+  if (v >= nV) return;
+  double sw = 0.0, s = 0.0, sa = 0.0;
+  for (int k = ba.ptr[v]; k < ba.ptr[v + 1]; ++k) {
+    const int t = ba.ind[k];
+    const double lv = (double)y[(int64_t)t * kGnnOut + 2];
+    sa += ba.v0[k] * lv;
+    if (!mask || mask[t] > 0.f) {
+      sw += ba.v0[k];
+      s += ba.v0[k] * lv;
+    }
+  }
+  const double l = sw > 0.0 ? s / sw : sa;
+  eta_a[v] = exp10(kGnnLogEtaScale * l + kGnnLogEtaOff);
 }
 
 // one averaging pass over each triangle and its TriC neighbours (ice triangles only)
@@ -2400,12 +2463,30 @@ void gnn_mesh_velocity(ufe_ctx *ctx, cudaStream_t s, float *y, bool to_state, co
   k_gnn_velocity<<<(ctx->nTri + 255) / 256, 256, 0, s>>>(ctx->nTri, w->uv, y, to_state ? 1 : 0, mask);
   UFE_CUDA(cudaGetLastError());
   if (to_state) {
+    disarm_prediction(w, s);   // a velocity-only prediction; gnn_mesh_viscosity arms the viscosity
     // a predicted start carries no vertical-shear state: DIVA begins its first iteration as from
     // a cold start, but with this velocity
     UFE_CUDA(cudaMemsetAsync(w->uv_base, 0, sizeof(double2) * ctx->nTri, s));
     UFE_CUDA(cudaMemsetAsync(w->tau_b, 0, sizeof(double2) * ctx->nTri, s));
     UFE_CUDA(cudaMemsetAsync(w->eta_3D_b, 0, sizeof(double) * (size_t)ctx->nTri * ctx->nz, s));
   }
+}
+
+// to_state: store the predicted viscosity (output 2 of y) on the vertices and arm the next solve's
+// first iteration with it; otherwise write the solved viscosity into output 2 of y as the target.
+void gnn_mesh_viscosity(ufe_ctx *ctx, cudaStream_t s, float *y, bool to_state, const float *mask) {
+  Work *w = ctx->work;
+  UFE_REQUIRE(w, UFE_ERR_INVALID, "learned start: upload the ice state first");
+  if (to_state) {
+    const DevCSR &mba = ctx->ops[UFE_OP_MAP_B_A];
+    OpRow ba{mba.ptr, mba.ind, mba.val, nullptr, nullptr};
+    k_gnn_visc_pred<<<(ctx->nV + 255) / 256, 256, 0, s>>>(ctx->nV, ba, y, mask, w->eta_pred_a, w->pred_flag);
+  } else {
+    const DevCSR &mab = ctx->ops[UFE_OP_MAP_A_B];
+    OpRow ab{mab.ptr, mab.ind, mab.val, nullptr, nullptr};
+    k_gnn_visc_target<<<(ctx->nTri + 255) / 256, 256, 0, s>>>(ctx->nTri, ab, w->N_a, w->Hi, y);
+  }
+  UFE_CUDA(cudaGetLastError());
 }
 
 extern "C" int32_t ufe_solve_ssa_resident(ufe_ctx *ctx, const ufe_solver_params *p, int32_t cold_start,
@@ -2551,6 +2632,7 @@ extern "C" int32_t ufe_solve_ssa(ufe_ctx *ctx, const ufe_solver_params *p, const
     check_sliding_inputs(p, ice);
     Work *w = ensure_work(ctx);
     upload_pair(ctx, w->uv, u_b, v_b);
+    disarm_prediction(w, ctx->stream);
     ufe_solve_stats st;
     int32_t r = resident_solve(ctx, p, 0, false, &st);
     download_pair(ctx, w->uv, u_b, v_b);
@@ -2580,6 +2662,7 @@ extern "C" int32_t ufe_solve_diva(ufe_ctx *ctx, const ufe_solver_params *p, cons
     upload_pair(ctx, w->uv_base, ds->u_base_b, ds->v_base_b);
     upload_pair(ctx, w->tau_b, ds->tau_bx_b, ds->tau_by_b);
     to_internal(ctx, w->eta_3D_b, ds->eta_3D_b, true, (int)nz);
+    disarm_prediction(w, s);
     ufe_solve_stats st;
     int32_t r = resident_solve(ctx, p, 0, true, &st);
     download_pair(ctx, w->uv, ds->u_vav_b, ds->v_vav_b);

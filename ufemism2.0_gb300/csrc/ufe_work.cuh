@@ -132,6 +132,10 @@ struct Work {
   double *N_a = nullptr, *beta_a = nullptr, *beta_eff_a = nullptr, *F2a1 = nullptr;
   double *eta_3D_a = nullptr;   // nz x nV
   double *F1_3D_a = nullptr;    // nz x nV (end of solve)
+  // the learned start's predicted vertically averaged viscosity per vertex, and the device flag
+  // that arms it for the first Picard iteration of the next solve (the solve's prologue clears it)
+  double *eta_pred_a = nullptr;
+  int32_t *pred_flag = nullptr;
   // linearised-solve inputs given on triangles (ufe_solve_linearised / ufe_assemble_linearised)
   double *N_b_in = nullptr, *dNx_b_in = nullptr, *dNy_b_in = nullptr, *beta_b_in = nullptr;
   // scalars

@@ -1,5 +1,6 @@
-"""Learned Picard start: a mesh-graph network that predicts the velocity an SSA/DIVA solve starts
-from, trained on solutions the plain GPU solver generates (include/ufe_gpu.h, ufe_gnn_*).
+"""Learned Picard start: a mesh-graph network that predicts the velocity and the effective viscosity
+an SSA/DIVA solve starts from, trained on solutions the plain GPU solver generates
+(include/ufe_gpu.h, ufe_gnn_*).
 
 Every solve still iterates to its own Picard tolerance; the network only replaces the zero (cold)
 or previous-step start, so a poor prediction costs iterations, never accuracy.
@@ -12,7 +13,7 @@ or previous-step start, so a poor prediction costs iterations, never accuracy.
         net.dataset_add(solver, x)          # features + the converged velocity as the target
     net.train(epochs=60, lr=1e-3)
     solver.ice_upload(new_ice)
-    net.predict(solver)                     # resident velocity <- prediction
+    net.predict(solver, viscosity=True)     # resident velocity (and first viscosity) <- prediction
     solver.solve_resident(params, diva=False, cold_start=False)
 """
 from __future__ import annotations
@@ -25,6 +26,7 @@ from . import abi
 from .solver import UfeError
 
 FEATURES = 16
+OUTPUTS = 3        # u / 1e3, v / 1e3 (m/yr), (log10(eta_vav) - 7.5) / 2 (Pa yr)
 
 
 def _f(a):
@@ -87,7 +89,7 @@ class LearnedStart:
     def forward(self, nbr, x):
         nbr = np.ascontiguousarray(nbr, dtype=np.int32)
         x = _f(x)
-        y = np.zeros((x.shape[0], 2), np.float32)
+        y = np.zeros((x.shape[0], OUTPUTS), np.float32)
         self._check(self.lib.ufe_gnn_forward(self.h, x.shape[0], abi.as_i(nbr), _fp(x), _fp(y)))
         return y
 
@@ -125,9 +127,10 @@ class LearnedStart:
         self._check(self.lib.ufe_gnn_evaluate(self.h, C.byref(l)))
         return l.value
 
-    def predict(self, solver, use_prev_velocity: bool = False, smooth_passes: int = 0):
-        """Store the predicted velocity as the solver's resident velocity; returns device ms."""
+    def predict(self, solver, use_prev_velocity: bool = False, smooth_passes: int = 0, viscosity: bool = False):
+        """Store the predicted velocity as the solver's resident velocity and, with `viscosity`, the
+        predicted viscosity for the next solve's first Picard iteration; returns device ms."""
         ms = C.c_double()
-        self._check(self.lib.ufe_gnn_predict_velocity(self.h, solver.ctx, 1 if use_prev_velocity else 0,
-                                                      smooth_passes, C.byref(ms)))
+        self._check(self.lib.ufe_gnn_predict_start(self.h, solver.ctx, 1 if use_prev_velocity else 0,
+                                                   smooth_passes, 1 if viscosity else 0, C.byref(ms)))
         return ms.value
