@@ -641,6 +641,112 @@ def run_thermo(args):
         torch.distributed.destroy_process_group()
 
 
+THICKNESS_METRIC = "semi-implicit ice-thickness steps/s (calc_dHi_dt), 1xGB300"
+THICKNESS_UNIT = "steps/s"
+
+
+def thickness_bytes(nV, nTri, nnz, nconn, its):
+    """Algorithmic bytes of one semi-implicit calc_dHi_dt step: each array a pass must read or
+    write, once.  Matrix build: connections (C, triangle pair, Cw: 20 B), vertex geometry and
+    fraction_margin (V, A, fm, ptr: 36 B), the velocities (16 B per triangle), M_divQ written (8 B
+    per entry).  Explicit pass: M_divQ and columns read (12 B per entry), 14 vertex arrays.  System
+    rows: M_divQ read and A written (20 B per entry), 9 vertex arrays.  Krylov: per iteration two
+    SpMVs (12 B per entry + row pointers + source + result) and 15 vector streams.  Finish: 8
+    vertex arrays."""
+    build = nconn * 20 + nV * 36 + nTri * 16 + nnz * 8
+    explicit = nnz * 12 + nV * 14 * 8
+    system = nnz * 20 + nV * 9 * 8
+    krylov = its * (2 * (nnz * 12 + nV * 4 + 2 * nV * 8) + 15 * nV * 8)
+    return build + explicit + system + krylov + nV * 8 * 8
+
+
+def run_thickness(args):
+    """The semi-implicit ice-thickness step (calc_dHi_dt) on a large mesh: device time per step by
+    CUDA events inside the call, end to end through ufe_calc_dHi_dt with pinned host buffers, and
+    the oracle's step on the host cores."""
+    import torch
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    pkg = __graft_entry__.load_package()
+    pkg.build()
+    t0 = time.perf_counter()
+    mesh, fields, p = pkg.geometry.thickness_case(res=args.thick_res, seed=0)
+    A, Cw = pkg.mesh.voronoi_geometry(mesh)
+    build_s = time.perf_counter() - t0
+    dt = 1.0
+    keep, fh = [], {}
+    for k, v in fields.items():
+        fh[k], t = pinned_like(torch, np.ascontiguousarray(v))
+        keep.append(t)
+    with pkg.VelocitySolver(mesh, device=local) as s:
+        s.voronoi_upload(A, Cw)
+        for _ in range(args.warmup):
+            s.calc_dHi_dt(p, fh, dt)
+        torch.cuda.synchronize()
+        dev_ms, its = [], []
+        with ClockSampler(local) as clocks:
+            t0 = time.perf_counter()
+            for _ in range(args.steps):
+                g = s.calc_dHi_dt(p, fh, dt)
+                dev_ms.append(g["stats"]["device_ms"])
+                its.append(g["stats"]["n_Axb_its"])
+            torch.cuda.synchronize()
+            wall = time.perf_counter() - t0
+        nnz = int(mesh.nV + np.asarray(mesh.nC).sum())
+        nconn = nnz - mesh.nV
+    value = args.steps / (sum(dev_ms) / 1000.0)
+    e2e_value = args.steps / wall
+    mean_its = float(np.mean(its))
+    nbytes = thickness_bytes(mesh.nV, mesh.nTri, nnz, nconn, mean_its)
+    peaks, peak_kind = measured_peaks()
+    achieved = nbytes / (np.mean(dev_ms) * 1e-3) / 1e9
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        oracle = _oracle()
+        orc = oracle.Oracle(mesh)
+        q = {k: (v.copy() if isinstance(v, np.ndarray) else v) for k, v in fields.items()}
+        for k in ("Hi_tplusdt", "divQ", "AMB"):
+            q[k] = np.zeros(mesh.nV)
+        n_cpu, tc = 0, time.perf_counter()
+        while n_cpu < 3 and (n_cpu == 0 or time.perf_counter() - tc < args.cpu_seconds):
+            q["dHi_dt"] = fields["dHi_dt"].copy()
+            orc.calc_dHi_dt(A, Cw, p, q, dt)
+            n_cpu += 1
+        sec = (time.perf_counter() - tc) / n_cpu
+        cpu = {"value": round(1.0 / sec, 4), "unit": THICKNESS_UNIT, "cores": os.cpu_count(), "kind": "port",
+               "sample": f"{n_cpu} full steps of the same workload ({sec * 1000:.0f} ms each; the BiCGStab "
+                         "loops use OpenMP, the matrix build and the border rule one core)"}
+    if rank == 0:
+        in_bytes = sum(v.nbytes for k, v in fh.items() if k in pkg.abi.THICKNESS_INPUTS or k == "dHi_dt")
+        line = {
+            "metric": THICKNESS_METRIC, "value": round(value, 2), "unit": THICKNESS_UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(float(np.mean(dev_ms)), 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic dome, relief bed, radial outflow on a generated mesh (no files)",
+            "config": {"workload": f"semi-implicit calc_dHi_dt (fs 1.5, BiCGStab/Jacobi rtol 1e-8, abstol 1e-6), "
+                                   f"dome H0 3000 m R 330 km on an 800 km square, {args.thick_res / 1e3:g} km mesh",
+                       "nV": mesh.nV, "nTri": mesh.nTri, "matrix_entries": nnz, "dt_yr": dt,
+                       "krylov_its_mean": mean_its, "host_build_s": round(build_s, 1),
+                       "l2": "every step uploads its inputs; the working set (about "
+                             f"{nbytes / max(mean_its, 1) / 1e6:.0f} MB) is under L2"},
+            "e2e": {"value": round(e2e_value, 2), "unit": THICKNESS_UNIT, "h2d_bytes_per_step": int(in_bytes),
+                    "d2h_bytes_per_step": int(4 * 8 * mesh.nV),
+                    "note": "ufe_calc_dHi_dt with pinned host arrays: upload, step, download of dHi_dt, "
+                            "Hi_tplusdt, divQ, AMB"},
+            "roofline": {"bound": "hbm", "kernel": "whole step (matrix build, explicit pass, system rows, "
+                                                   "three-kernel CSR BiCGStab)",
+                         "achieved": round(achieved, 1), "peak": peaks.get("hbm_gbs"), "unit": "GB/s",
+                         "frac": round(achieved / peaks.get("hbm_gbs"), 4), "peak_source": peak_kind,
+                         "traffic": None, "algorithmic_bytes_per_step": int(nbytes)},
+            "cpu_baseline": cpu,
+            "clocks": clocks.summary(),
+            "gpu_launches": int(args.steps * (12 + 1 + 3 * 8 * int(np.ceil(mean_its / 8)))),
+            "wall_s_timed": round(wall, 3),
+        }
+        print(json.dumps(line))
+
+
 LEARNED_WORKLOAD = ("learned Picard start, SSA ensemble: 30k-vertex mesh over 1500 km x 1500 km, bed -200 m + "
                     "GRF(400 m, 20 km), dome R = 600 km, floating below flotation, log-normal beta^2; 256 training "
                     "and 32 held-out geometries; Weertman m = 3, Picard 1e-4, BiCGStab/Jacobi 1e-8")
@@ -1418,7 +1524,10 @@ def main():
     ap.add_argument("--dome-tight", type=float, default=1e-15, help="the tight Picard tolerance of --workload dome")
     ap.add_argument("--dome-ref-tol", type=float, default=1e-16, help="Picard tolerance of the dome's reference solution")
     ap.add_argument("--dome-epochs", type=int, default=200)
-    ap.add_argument("--workload", default="diva", choices=["diva", "thermo", "learned", "ensemble", "mixed", "dome", "icestream"],
+    ap.add_argument("--thick-res", type=float, default=1.25e3,
+                    help="mesh spacing [m] of --workload thickness (1.25 km: about 410k vertices)")
+    ap.add_argument("--workload", default="diva", choices=["diva", "thermo", "learned", "ensemble", "mixed", "dome", "icestream",
+                                                         "thickness"],
                     help="diva: the headline velocity solve; thermo: the batched column thermodynamics; "
                          "learned: the learned Picard start on the SSA ensemble")
     ap.add_argument("--ens-members", type=int, default=12)
@@ -1454,6 +1563,8 @@ def main():
         run_ensemble(args)
     elif args.workload == "mixed":
         run_mixed(args)
+    elif args.workload == "thickness":
+        run_thickness(args)
     elif args.impl == "reference":
         run_reference(args)
     else:

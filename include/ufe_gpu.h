@@ -543,6 +543,74 @@ int32_t ufe_gnn_predict_velocity(ufe_gnn *g, ufe_ctx *mesh_ctx, int32_t use_prev
 int32_t ufe_gnn_predict_start(ufe_gnn *g, ufe_ctx *mesh_ctx, int32_t use_prev_velocity, int32_t smooth_passes,
                               int32_t with_viscosity, double *device_ms);
 
+/* ---- ice thickness: conservation of mass ------------------------------------------------------ */
+/* calc_dHi_dt (src/UFEMISM/ice_dynamics/conservation_of_mass/conservation_of_mass_main.f90:23-109)
+ * with the explicit scheme (conservation_of_mass_explicit.f90:22-134) and the semi-implicit one
+ * (conservation_of_mass_semiimplicit.f90:23-174): the upwind flux-divergence matrix M_divQ
+ * (conservation_of_mass_utilities.f90:22-132, edge velocities as in map_velocities_from_b_to_c_2D,
+ * map_velocities_to_c_grid.f90:17-69), the flux-limited time step (:158-204), the domain-border,
+ * prescribed-thickness and no-ice conditions, and for the semi-implicit scheme the matrix equation
+ * (1 + dt fs M_divQ) H(t+dt) = H(t) - dt (1 - fs) M_divQ H(t) + max(-H(t), dt m), solved with the
+ * same BiCGStab/Jacobi as solve_matrix_equation_CSR_PETSc.  Computed on the mesh's own (caller's)
+ * vertex numbering; every field is in the caller's order. */
+
+/* The Voronoi geometry of type_mesh the flux divergence reads (mesh_types.f90: A, Cw; built by
+ * mesh_secondary.f90): cell areas A (nV) and the lengths Cw of the shared Voronoi boundary of
+ * each connection (nV x nC_mem, column-major like C).  Once per mesh, before ufe_calc_dHi_dt. */
+int32_t ufe_mesh_voronoi_upload(ufe_ctx *ctx, const double *A, const double *Cw);
+
+enum ufe_ice_integration { UFE_DHI_NONE = 0, UFE_DHI_EXPLICIT = 1, UFE_DHI_SEMIIMPLICIT = 2 };
+enum ufe_bc_H { UFE_BC_H_ZERO = 0, UFE_BC_H_INFINITE = 1 };   /* BC_H_* 'zero', 'infinite' */
+
+typedef struct {
+  int32_t choice_ice_integration_method;                   /* ufe_ice_integration                  */
+  int32_t BC_H_west, BC_H_east, BC_H_south, BC_H_north;    /* ufe_bc_H                             */
+  int32_t dHi_PETSc_max_it;                                /* Krylov iteration limit               */
+  double dHi_semiimplicit_fs;                              /* 0 explicit .. 1 implicit, >1 over-implicit */
+  double dHi_PETSc_rtol, dHi_PETSc_abstol;
+  double dt_ice_max, dt_ice_min;                           /* [yr], calc_flux_limited_timestep     */
+  double Hi_min;                                           /* [m]                                  */
+  int32_t reserved[4];
+} ufe_thickness_params;
+
+/* The reference's configuration defaults (model_configuration.f90): semi-implicit, fs 1.5, rtol
+ * 1e-8, abstol 1e-6, dt_ice_max 10 yr, dt_ice_min 0.1 yr, Hi_min 0, BC_H 'zero' on all sides. */
+void ufe_default_thickness_params(ufe_thickness_params *p);
+
+typedef struct {
+  const double *Hi, *Hb, *SL;             /* nV: thickness, bedrock, sea level at t            */
+  const double *u_vav_b, *v_vav_b;        /* nTri: vertically averaged velocity [m/yr]          */
+  const double *SMB, *BMB, *LMB;          /* nV [m/yr]; NULL = 0                                */
+  const double *fraction_margin;          /* nV [0-1]; NULL = 1                                 */
+  const int32_t *mask_noice;              /* nV, 1 = no ice allowed; NULL = none                */
+  const double *dHi_dt_target;            /* nV [m/yr]; NULL = 0                                */
+  const int32_t *BC_prescr_mask;          /* nV, 1 = prescribed; NULL = none (then ...Hi too)   */
+  const double *BC_prescr_Hi;             /* nV                                                 */
+  double *dHi_dt;                         /* nV in: the previous rate (the semi-implicit
+                                             initial guess H + dt dH/dt; NULL in = 0); out       */
+  double *Hi_tplusdt, *divQ, *AMB;        /* nV out                                             */
+} ufe_thickness_fields;
+
+typedef struct {
+  int32_t n_Axb_its;        /* Krylov iterations of the semi-implicit solve                      */
+  int32_t krylov_status;    /* UFE_OK or UFE_WARN_KRYLOV_MAXIT                                   */
+  int32_t found_negative;   /* the reference's warning: H(t+dt) < -0.1 where H(t) > Hi_min         */
+  int32_t pad;
+  double device_ms;         /* device time of the step (CUDA events, without the copies)         */
+} ufe_thickness_stats;
+
+/* One call of calc_dHi_dt.  *dt is in/out as in the reference (the explicit scheme may shorten it). */
+int32_t ufe_calc_dHi_dt(ufe_ctx *ctx, const ufe_thickness_params *p, ufe_thickness_fields *f, double *dt,
+                        ufe_thickness_stats *stats);
+
+/* The semi-implicit system after its boundary conditions -- stiffness matrix (0-based CSR in the
+ * reference's add_entry order: the diagonal, then the neighbours in C order), load vector and
+ * initial guess -- as the semi-implicit scheme hands it to the Krylov solve (for parity checks).
+ * cap: entries val/ind can hold; *nnz receives the count. */
+int32_t ufe_thickness_assemble(ufe_ctx *ctx, const ufe_thickness_params *p, const ufe_thickness_fields *f, double dt,
+                               int32_t *ptr, int32_t *ind, double *val, double *bb, double *x0, int64_t cap,
+                               int64_t *nnz);
+
 /* ---- allocation-free solve -------------------------------------------------------------------- */
 /* The CSR matrix-equation solve of ufe_solve_csr (same BiCGStab/Jacobi, same convergence test)
  * for callers that cannot let a library allocate device memory -- e.g. a host model whose GPU

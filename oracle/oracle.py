@@ -61,6 +61,11 @@ def load():
                                            C.POINTER(abi.BCPrescribed), C.POINTER(abi.DivaState),
                                            C.POINTER(abi.SolveStats)]),
         "orc_ops_set_first_viscosity": (C.c_int32, [vp, dp]),
+        "orc_ops_calc_dHi_dt": (C.c_int32, [vp, dp, dp, C.POINTER(abi.ThicknessParams),
+                                            C.POINTER(abi.ThicknessFields), dp, C.POINTER(abi.ThicknessStats)]),
+        "orc_ops_thickness_assemble": (C.c_int32, [vp, dp, dp, C.POINTER(abi.ThicknessParams),
+                                                   C.POINTER(abi.ThicknessFields), C.c_double, ip, ip, dp, dp, dp,
+                                                   C.c_int64, C.POINTER(C.c_int64)]),
         "orc_ops_assemble": (C.c_int32, [vp, C.POINTER(abi.SolverParams), dp, dp, dp, dp, dp, dp, dp, dp,
                                          C.POINTER(abi.BCPrescribed), ip, ip, dp, dp, C.c_int64,
                                          C.POINTER(C.c_int64)]),
@@ -196,6 +201,36 @@ class Oracle:
         rc = self.lib.orc_ops_set_first_viscosity(self.h, None if arr is None else self.abi.as_d(arr))
         if rc < 0:
             raise OracleError(rc)
+
+    def calc_dHi_dt(self, A, Cw, params, fields: dict, dt: float):
+        """orc_ops_calc_dHi_dt: fills the output arrays of `fields` (dHi_dt, Hi_tplusdt, divQ, AMB;
+        dHi_dt holds the previous rate on entry); returns (dt, stats)."""
+        f, keep = self.abi.thickness_fields(fields)
+        A, Cw = np.ascontiguousarray(A, np.float64), np.asfortranarray(Cw, np.float64)
+        d = C.c_double(dt)
+        st = self.abi.ThicknessStats()
+        rc = self.lib.orc_ops_calc_dHi_dt(self.h, self.abi.as_d(A), self.abi.as_d(Cw), C.byref(params), C.byref(f),
+                                          C.byref(d), C.byref(st))
+        if rc < 0:
+            raise OracleError(rc)
+        return d.value, st.as_dict()
+
+    def thickness_assemble(self, A, Cw, params, fields: dict, dt: float):
+        """The semi-implicit system (0-based CSR, load vector, initial guess) before its solve."""
+        f, keep = self.abi.thickness_fields(fields)
+        A, Cw = np.ascontiguousarray(A, np.float64), np.asfortranarray(Cw, np.float64)
+        nV = self.mesh.nV
+        cap = int(nV + self.mesh.nC.sum())
+        ptr, ind = np.zeros(nV + 1, np.int32), np.zeros(cap, np.int32)
+        val, bb, x0 = np.zeros(cap), np.zeros(nV), np.zeros(nV)
+        nnz = C.c_int64()
+        rc = self.lib.orc_ops_thickness_assemble(self.h, self.abi.as_d(A), self.abi.as_d(Cw), C.byref(params),
+                                                 C.byref(f), dt, self.abi.as_i(ptr), self.abi.as_i(ind),
+                                                 self.abi.as_d(val), self.abi.as_d(bb), self.abi.as_d(x0), cap,
+                                                 C.byref(nnz))
+        if rc < 0:
+            raise OracleError(rc)
+        return ptr, ind[:nnz.value], val[:nnz.value], bb, x0
 
     def solve_SSA(self, ice, SSA, params, BC=None):
         st, keep = self.abi.ice_state(ice)

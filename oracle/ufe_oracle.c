@@ -1330,6 +1330,29 @@ int32_t orc_ops_solve_diva(orc_ops *h, const ufe_solver_params *p, const ufe_ice
   return rc;
 }
 
+int32_t orc_ops_calc_dHi_dt(orc_ops *h, const double *A_vor, const double *Cw, const ufe_thickness_params *p,
+                            ufe_thickness_fields *f, double *dt, ufe_thickness_stats *st) {
+  if (!h || !A_vor || !Cw || !p || !f || !dt) return UFE_ERR_INVALID;
+  return orc_calc_dHi_dt(&h->mesh, A_vor, Cw, p, f, dt, st);
+}
+
+/* the semi-implicit system, exported 0-based like ufe_thickness_assemble */
+int32_t orc_ops_thickness_assemble(orc_ops *h, const double *A_vor, const double *Cw,
+                                   const ufe_thickness_params *p, const ufe_thickness_fields *f, double dt,
+                                   int32_t *ptr, int32_t *ind, double *val, double *bb, double *x0,
+                                   int64_t cap, int64_t *nnz_out) {
+  if (!h || !A_vor || !Cw || !p || !f) return UFE_ERR_INVALID;
+  orc_csr A;
+  int32_t rc = orc_thickness_assemble(&h->mesh, A_vor, Cw, p, f, dt, &A, bb, x0);
+  if (rc != UFE_OK) return rc;
+  *nnz_out = A.nnz;
+  if (A.nnz > cap) { orc_csr_free(&A); return UFE_ERR_CAPACITY; }
+  for (int i = 0; i <= A.m; ++i) ptr[i] = A.ptr[i] - 1;
+  for (int64_t k = 0; k < A.nnz; ++k) { ind[k] = A.ind[k] - 1; val[k] = A.val[k]; }
+  orc_csr_free(&A);
+  return UFE_OK;
+}
+
 int32_t orc_ops_assemble(orc_ops *h, const ufe_solver_params *p,
                          const double *N_b, const double *dN_dx_b, const double *dN_dy_b,
                          const double *beta_b, const double *tau_dx_b, const double *tau_dy_b,

@@ -61,6 +61,17 @@ int32_t orc_solve_diva(const ufe_mesh_desc *mesh, const orc_csr *ops, const ufe_
                        ufe_diva_state *ds, ufe_solve_stats *st,
                        const double *eta_first /* nV or NULL: first-iteration viscosity */);
 
+/* calc_dHi_dt (conservation_of_mass_main.f90:23-109) and the semi-implicit system before its
+ * Krylov solve (A: 1-based CSR, freshly allocated), on the caller's vertex numbering; A_vor and Cw
+ * are type_mesh's Voronoi cell areas and connection widths (ufe_oracle_mass.c). */
+void    orc_default_thickness_params(ufe_thickness_params *p);
+int32_t orc_calc_dHi_dt(const ufe_mesh_desc *m, const double *A_vor, const double *Cw,
+                        const ufe_thickness_params *p, ufe_thickness_fields *f, double *dt,
+                        ufe_thickness_stats *st);
+int32_t orc_thickness_assemble(const ufe_mesh_desc *m, const double *A_vor, const double *Cw,
+                               const ufe_thickness_params *p, const ufe_thickness_fields *f, double dt,
+                               orc_csr *A, double *bb, double *x0);
+
 /* Convenience for ctypes callers: build operators into an opaque handle. */
 typedef struct orc_ops orc_ops;
 orc_ops *orc_ops_create(const ufe_mesh_desc *mesh, int32_t *status);
@@ -73,6 +84,12 @@ int32_t  orc_ops_solve_ssa(orc_ops *h, const ufe_solver_params *p, const ufe_ice
 int32_t  orc_ops_solve_diva(orc_ops *h, const ufe_solver_params *p, const ufe_ice_state *ice,
                             const ufe_bc_prescribed *bc, ufe_diva_state *ds, ufe_solve_stats *st);
 int32_t  orc_ops_set_first_viscosity(orc_ops *h, const double *eta_a);
+int32_t  orc_ops_calc_dHi_dt(orc_ops *h, const double *A_vor, const double *Cw, const ufe_thickness_params *p,
+                             ufe_thickness_fields *f, double *dt, ufe_thickness_stats *st);
+int32_t  orc_ops_thickness_assemble(orc_ops *h, const double *A_vor, const double *Cw,
+                                    const ufe_thickness_params *p, const ufe_thickness_fields *f, double dt,
+                                    int32_t *ptr, int32_t *ind, double *val, double *bb, double *x0,
+                                    int64_t cap, int64_t *nnz_out);
 int32_t  orc_ops_assemble(orc_ops *h, const ufe_solver_params *p,
                           const double *N_b, const double *dN_dx_b, const double *dN_dy_b,
                           const double *beta_b, const double *tau_dx_b, const double *tau_dy_b,

@@ -240,6 +240,73 @@ def heat_fields(f: dict) -> tuple[HeatFields, list]:
     return HeatFields(**vals), keep
 
 
+# -- ice thickness (conservation of mass) -------------------------------------------------------
+DHI = {"none": 0, "explicit": 1, "semi-implicit": 2}
+BC_H = {"zero": 0, "infinite": 1}
+
+
+class ThicknessParams(C.Structure):
+    _fields_ = [("choice_ice_integration_method", C.c_int32), ("BC_H_west", C.c_int32), ("BC_H_east", C.c_int32),
+                ("BC_H_south", C.c_int32), ("BC_H_north", C.c_int32), ("dHi_PETSc_max_it", C.c_int32),
+                ("dHi_semiimplicit_fs", C.c_double), ("dHi_PETSc_rtol", C.c_double), ("dHi_PETSc_abstol", C.c_double),
+                ("dt_ice_max", C.c_double), ("dt_ice_min", C.c_double), ("Hi_min", C.c_double),
+                ("reserved", C.c_int32 * 4)]
+
+
+class ThicknessFields(C.Structure):
+    _fields_ = [("Hi", dptr), ("Hb", dptr), ("SL", dptr), ("u_vav_b", dptr), ("v_vav_b", dptr),
+                ("SMB", dptr), ("BMB", dptr), ("LMB", dptr), ("fraction_margin", dptr), ("mask_noice", iptr),
+                ("dHi_dt_target", dptr), ("BC_prescr_mask", iptr), ("BC_prescr_Hi", dptr),
+                ("dHi_dt", dptr), ("Hi_tplusdt", dptr), ("divQ", dptr), ("AMB", dptr)]
+
+
+class ThicknessStats(C.Structure):
+    _fields_ = [("n_Axb_its", C.c_int32), ("krylov_status", C.c_int32), ("found_negative", C.c_int32),
+                ("pad", C.c_int32), ("device_ms", C.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_ if k != "pad"}
+
+
+def default_thickness_params(**overrides) -> ThicknessParams:
+    """The defaults of model_configuration.f90 (same values as ufe_default_thickness_params);
+    string choices ('semi-implicit', 'infinite', ...) are accepted for the enum fields."""
+    p = ThicknessParams()
+    p.choice_ice_integration_method = DHI["semi-implicit"]
+    for side in ("west", "east", "south", "north"):
+        setattr(p, f"BC_H_{side}", BC_H["zero"])
+    p.dHi_PETSc_max_it = 10000
+    p.dHi_semiimplicit_fs = 1.5
+    p.dHi_PETSc_rtol = 1e-8
+    p.dHi_PETSc_abstol = 1e-6
+    p.dt_ice_max = 10.0
+    p.dt_ice_min = 0.1
+    p.Hi_min = 0.0
+    for k, v in overrides.items():
+        if k == "choice_ice_integration_method" and isinstance(v, str):
+            v = DHI[v]
+        elif k.startswith("BC_H_") and isinstance(v, str):
+            v = BC_H[v]
+        setattr(p, k, v)
+    return p
+
+
+THICKNESS_INPUTS = ("Hi", "Hb", "SL", "u_vav_b", "v_vav_b", "SMB", "BMB", "LMB", "fraction_margin", "mask_noice",
+                    "dHi_dt_target", "BC_prescr_mask", "BC_prescr_Hi")
+THICKNESS_OUTPUTS = ("dHi_dt", "Hi_tplusdt", "divQ", "AMB")
+
+
+def thickness_fields(f: dict) -> tuple[ThicknessFields, list]:
+    """ThicknessFields over a dict of arrays (inputs as named in THICKNESS_INPUTS; the outputs in
+    THICKNESS_OUTPUTS must be present, dHi_dt holding the previous rate)."""
+    keep = [v for v in f.values() if isinstance(v, np.ndarray)]
+    vals = {}
+    for k, _ in ThicknessFields._fields_:
+        a = f.get(k)
+        vals[k] = (as_i(a) if k in ("mask_noice", "BC_prescr_mask") else as_d(a)) if a is not None else None
+    return ThicknessFields(**vals), keep
+
+
 # -- numpy <-> ctypes helpers -------------------------------------------------------------------
 def as_d(a):
     """Pointer to a contiguous float64 buffer (Fortran-ordered arrays are flattened column-major)."""
@@ -289,6 +356,13 @@ def bc_prescribed(bc: dict | None):
 # -- the library ---------------------------------------------------------------------------------
 EXPORTS = {
     "ufe_default_params": (None, [C.POINTER(SolverParams)]),
+    "ufe_default_thickness_params": (None, [C.POINTER(ThicknessParams)]),
+    "ufe_mesh_voronoi_upload": (C.c_int32, [C.c_void_p, dptr, dptr]),
+    "ufe_calc_dHi_dt": (C.c_int32, [C.c_void_p, C.POINTER(ThicknessParams), C.POINTER(ThicknessFields), dptr,
+                                    C.POINTER(ThicknessStats)]),
+    "ufe_thickness_assemble": (C.c_int32, [C.c_void_p, C.POINTER(ThicknessParams), C.POINTER(ThicknessFields),
+                                           C.c_double, iptr, iptr, dptr, dptr, dptr, C.c_int64,
+                                           C.POINTER(C.c_int64)]),
     "ufe_ctx_create": (C.c_int32, [C.c_int32, C.POINTER(C.c_void_p)]),
     "ufe_ctx_destroy": (None, [C.c_void_p]),
     "ufe_ctx_last_error": (C.c_char_p, [C.c_void_p]),

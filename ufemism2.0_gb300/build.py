@@ -18,7 +18,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libufe_gpu.so")
 SOURCES = ["ufe_ctx.cu", "ufe_layout.cu", "ufe_operators.cu", "ufe_spmv.cu", "ufe_velocity.cu", "ufe_noalloc.cu",
-           "ufe_thermo.cu", "ufe_gnn.cu"]
+           "ufe_thermo.cu", "ufe_gnn.cu", "ufe_mass.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -113,6 +113,8 @@ struct ufe_ctx {
   struct Work *work = nullptr;
   // thermodynamics workspace and resident heat-equation state (ufe_thermo.cu)
   struct ThermoWork *thermo = nullptr;
+  // ice-thickness workspace: the mesh's Voronoi geometry and the M_divQ pattern (ufe_mass.cu)
+  struct MassWork *mass = nullptr;
   // rows per warp of the block-row Krylov kernels for this mesh (0: the default; ufe_autotune)
   int32_t lanes = 0;
   // the persistent FP32 inner solve needs the whole GPU; ensembles switch it off for the member
@@ -152,6 +154,9 @@ void build_operators_gpu(ufe_ctx *ctx);
 // ufe_thermo.cu
 void free_thermo(ufe_ctx *ctx);
 
+// ufe_mass.cu
+void free_mass(ufe_ctx *ctx);
+
 // ufe_velocity.cu: the mesh side of the learned Picard start (internal order, on stream s)
 void gnn_mesh_features(ufe_ctx *ctx, cudaStream_t s, int use_prev, float *x, float *mask);
 void gnn_mesh_graph(ufe_ctx *ctx, cudaStream_t s, int32_t *nbr);
@@ -183,6 +188,15 @@ void launch_csr_spmv(cudaStream_t s, const DevCSR &A, const double *x, double *y
 
 // ufe_velocity.cu
 void free_work(ufe_ctx *ctx);
+// Work vectors of solve_csr_device for callers that solve repeatedly (nothing is allocated
+// inside the solve when a scratch with cap >= the rows is passed).
+struct CsrSolveScratch {
+  double *vec = nullptr;              // 10 x cap
+  struct KrylovScalars *ks = nullptr, *hks = nullptr;   // device, pinned host
+  int64_t cap = 0;
+};
+void csr_scratch_alloc(CsrSolveScratch &scr, int64_t m);
+void csr_scratch_free(CsrSolveScratch &scr);
 int32_t solve_csr_device(ufe_ctx *ctx, const DevCSR &A, const double *b, double *x, double rtol,
-                         double abstol, int32_t max_it, int32_t *its);
+                         double abstol, int32_t max_it, int32_t *its, CsrSolveScratch *scratch = nullptr);
 

@@ -1221,6 +1221,7 @@ Work *ensure_work(ufe_ctx *ctx) {
 
 void free_work(ufe_ctx *ctx) {
   free_thermo(ctx);   // the resident heat state depends on the mesh and its operators
+  free_mass(ctx);     // so do the Voronoi geometry and the thickness matrix pattern
   Work *w = ctx->work;
   if (!w) return;
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
@@ -2956,31 +2957,47 @@ extern "C" int32_t ufe_profile_krylov_kernels(ufe_ctx *ctx, int32_t precision, i
 
 // General CSR matrix-equation solve (solve_matrix_equation_CSR_PETSc): same BiCGStab kernels on
 // scalar rows, host-checked every few iterations.
+// inverse diagonal of a CSR matrix: the row's diagonal entries summed in storage order
+__global__ void k_csr_dinv(int m, const int32_t *ptr, const int32_t *ind, const double *val, double *dinv) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= m) return;
+  double d = 0.0;
+  for (int32_t k = ptr[i]; k < ptr[i + 1]; ++k)
+    if (ind[k] == i) d += val[k];
+  dinv[i] = d != 0.0 ? 1.0 / d : 1.0;
+}
+
+void csr_scratch_alloc(CsrSolveScratch &scr, int64_t m) {
+  scr.vec = (double *)dev_alloc(sizeof(double) * (size_t)m * 10);
+  scr.ks = (KrylovScalars *)dev_alloc(sizeof(KrylovScalars));
+  UFE_CUDA(cudaMallocHost(&scr.hks, sizeof(KrylovScalars)));
+  scr.cap = m;
+}
+
+void csr_scratch_free(CsrSolveScratch &scr) {
+  dev_free(scr.vec);
+  dev_free(scr.ks);
+  if (scr.hks) cudaFreeHost(scr.hks);
+  scr = CsrSolveScratch{};
+}
+
 int32_t solve_csr_device(ufe_ctx *ctx, const DevCSR &A, const double *b, double *x, double rtol, double abstol,
-                         int32_t max_it, int32_t *its) {
+                         int32_t max_it, int32_t *its, CsrSolveScratch *scratch) {
   cudaStream_t s = ctx->stream;
   const int m = A.m;
-  double *vec = (double *)dev_alloc(sizeof(double) * (size_t)m * 10);
-  KrylovScalars *ks = (KrylovScalars *)dev_alloc(sizeof(KrylovScalars));
-  KrylovScalars *hks = nullptr;
-  UFE_CUDA(cudaMallocHost(&hks, sizeof(KrylovScalars)));
+  CsrSolveScratch own;
+  const bool owned = !(scratch && scratch->cap >= m);
+  if (owned) csr_scratch_alloc(own, m);
+  CsrSolveScratch &scr = owned ? own : *scratch;
+  double *vec = scr.vec;
+  KrylovScalars *ks = scr.ks;
+  KrylovScalars *hks = scr.hks;
   int32_t status = UFE_OK;
   try {
     double *dinv = vec, *R = vec + m, *RP = R + m, *S = RP + m, *T = S + m, *P0 = T + m, *P1 = P0 + m,
            *V0 = P1 + m, *V1 = V0 + m;
-    // Jacobi diagonal
-    std::vector<int32_t> hp(m + 1), hi(A.nnz);
-    std::vector<double> hv(A.nnz), hd(m);
-    UFE_CUDA(cudaMemcpy(hp.data(), A.ptr, sizeof(int32_t) * (m + 1), cudaMemcpyDeviceToHost));
-    UFE_CUDA(cudaMemcpy(hi.data(), A.ind, sizeof(int32_t) * A.nnz, cudaMemcpyDeviceToHost));
-    UFE_CUDA(cudaMemcpy(hv.data(), A.val, sizeof(double) * A.nnz, cudaMemcpyDeviceToHost));
-    for (int i = 0; i < m; ++i) {
-      double d = 0.0;
-      for (int k = hp[i]; k < hp[i + 1]; ++k)
-        if (hi[k] == i) d += hv[k];
-      hd[i] = d != 0.0 ? 1.0 / d : 1.0;
-    }
-    UFE_CUDA(cudaMemcpyAsync(dinv, hd.data(), sizeof(double) * m, cudaMemcpyHostToDevice, s));
+    // Jacobi diagonal (PCJACOBI: 1 where the diagonal is zero)
+    k_csr_dinv<<<(unsigned)((m + 255) / 256), 256, 0, s>>>(m, A.ptr, A.ind, A.val, dinv);
     UFE_CUDA(cudaMemsetAsync(ks, 0, sizeof(KrylovScalars), s));
     CsrMat mat{m, A.ptr, A.ind, A.val};
     KV<double> v;
@@ -3007,13 +3024,9 @@ int32_t solve_csr_device(ufe_ctx *ctx, const DevCSR &A, const double *b, double 
     status = hks->status;
   } catch (...) {
     cudaStreamSynchronize(s);
-    dev_free(vec);
-    dev_free(ks);
-    cudaFreeHost(hks);
+    if (owned) csr_scratch_free(own);
     throw;
   }
-  dev_free(vec);
-  dev_free(ks);
-  cudaFreeHost(hks);
+  if (owned) csr_scratch_free(own);
   return status;
 }

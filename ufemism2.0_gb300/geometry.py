@@ -227,6 +227,47 @@ def transect_values(mesh, values_a, x0=0.0, dy=1e3):
     return y, out
 
 
+def thickness_case(seed=0, L=800e3, res=20e3, H0=3000.0, R=330e3, U0=400.0, nz=3):
+    """An ice-thickness (conservation of mass) workload on a generated mesh: a dome of thickness
+    H0 and radius R over a bed of relief around sea level (part of the margin floats), a radial
+    outflow velocity rising to U0 m/yr at the margin on the triangles, surface mass balance
+    falling with distance, basal melt under floating ice, a band of partly filled margin cells
+    (fraction_margin < 1), a no-ice mask near the domain border, a few prescribed-thickness
+    vertices, 'infinite' thickness borders west/south and 'zero' east/north.  Returns
+    (mesh, fields, thickness params); `res` the mesh spacing in m."""
+    mesh = generate_mesh(-L / 2, L / 2, -L / 2, L / 2, lambda x, y: np.full(np.shape(x), float(res)),
+                         seed=seed, nz=nz)
+    rng = np.random.default_rng(seed)
+    x, y = np.asarray(mesh.V[:, 0]), np.asarray(mesh.V[:, 1])
+    r = np.hypot(x, y)
+    Hi = np.ascontiguousarray(dome_thickness(x, y, H0=H0, R=R))
+    Hb = np.ascontiguousarray(-150.0 + 400.0 * np.cos(2 * np.pi * x / 300e3) * np.cos(2 * np.pi * y / 250e3)
+                              - 300.0 * (r / R) ** 2)
+    SL = np.zeros(mesh.nV)
+    gc = np.asarray(mesh.TriGC)
+    rt = np.maximum(np.hypot(gc[:, 0], gc[:, 1]), 1.0)
+    speed = U0 * np.clip(rt / R, 0.0, 1.2) ** 2 * np.exp(-np.clip(rt - R, 0.0, None) / 50e3)
+    speed = speed * (1.0 + 0.2 * rng.standard_normal(mesh.nTri))
+    u = np.ascontiguousarray(speed * gc[:, 0] / rt)
+    v = np.ascontiguousarray(speed * gc[:, 1] / rt)
+    floating = thickness_above_flotation(Hi, Hb, SL) < 0.0
+    fields = dict(
+        Hi=Hi, Hb=Hb, SL=SL, u_vav_b=u, v_vav_b=v,
+        SMB=np.ascontiguousarray(0.5 - 1.5 * (r / (L / 2)) ** 2),
+        BMB=np.ascontiguousarray(np.where(floating & (Hi > 0), -2.0, 0.0)),
+        LMB=np.zeros(mesh.nV),
+        fraction_margin=np.ascontiguousarray(np.where(np.abs(r - R) < 15e3, 0.6, 1.0)),
+        mask_noice=np.ascontiguousarray((np.maximum(np.abs(x), np.abs(y)) > 0.45 * L).astype(np.int32)),
+        dHi_dt_target=np.zeros(mesh.nV),
+        BC_prescr_mask=np.ascontiguousarray((rng.random(mesh.nV) < 0.002).astype(np.int32)),
+        BC_prescr_Hi=np.ascontiguousarray(Hi + 10.0),
+        dHi_dt=np.ascontiguousarray(0.01 * rng.standard_normal(mesh.nV)),
+    )
+    params = abi.default_thickness_params(BC_H_west="infinite", BC_H_south="infinite",
+                                          BC_H_east="zero", BC_H_north="zero")
+    return mesh, fields, params
+
+
 def small_dome(seed=0, nz=12):
     """A ~1,000-vertex dome for tests the CPU oracle finishes in seconds."""
     return dome_case(seed=seed, nz=nz, res_scale=3.0)

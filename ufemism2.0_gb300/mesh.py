@@ -316,6 +316,80 @@ def generate_points(xmin, xmax, ymin, ymax, res_fn, seed=0, jitter=0.18):
 generate_points.last_n_border = 0
 
 
+def circumcentres(mesh):
+    """Circumcentres of the triangles (nTri x 2)."""
+    V = np.asarray(mesh.V)
+    T = np.asarray(mesh.Tri) - 1
+    a, b, c = V[T[:, 0]], V[T[:, 1]], V[T[:, 2]]
+    d = 2.0 * (a[:, 0] * (b[:, 1] - c[:, 1]) + b[:, 0] * (c[:, 1] - a[:, 1]) + c[:, 0] * (a[:, 1] - b[:, 1]))
+    na, nb, nc = (a * a).sum(1), (b * b).sum(1), (c * c).sum(1)
+    ux = (na * (b[:, 1] - c[:, 1]) + nb * (c[:, 1] - a[:, 1]) + nc * (a[:, 1] - b[:, 1])) / d
+    uy = (na * (c[:, 0] - b[:, 0]) + nb * (a[:, 0] - c[:, 0]) + nc * (b[:, 0] - a[:, 0])) / d
+    return np.c_[ux, uy]
+
+
+def connection_triangles(mesh):
+    """For every connection (vi, ci): the one or two triangles of the edge from vi to C(vi, ci),
+    0-based (nV x nC_mem x 2, -1 where there is none)."""
+    T = np.asarray(mesh.Tri, dtype=np.int64) - 1
+    nV = mesh.nV
+    ends = np.r_[T[:, [0, 1]], T[:, [1, 2]], T[:, [2, 0]]]
+    tri = np.tile(np.arange(mesh.nTri), 3)
+    key = np.minimum(ends[:, 0], ends[:, 1]) * nV + np.maximum(ends[:, 0], ends[:, 1])
+    order = np.argsort(key, kind="stable")
+    key, tri = key[order], tri[order]
+    out = -np.ones((nV, mesh.nC_mem, 2), np.int64)
+    C = np.asarray(mesh.C, dtype=np.int64) - 1
+    for ci in range(mesh.nC_mem):
+        live = np.arange(nV)[ci < mesh.nC]
+        vj = C[live, ci]
+        k = np.minimum(live, vj) * nV + np.maximum(live, vj)
+        i0 = np.searchsorted(key, k)
+        out[live, ci, 0] = tri[i0]
+        two = (i0 + 1 < key.size) & (key[np.minimum(i0 + 1, key.size - 1)] == k)
+        out[live[two], ci, 1] = tri[i0[two] + 1]
+    return out
+
+
+def voronoi_geometry(mesh):
+    """The Voronoi geometry of type_mesh that the ice-thickness equation reads: cell areas A (nV)
+    and, per connection, the length Cw of the Voronoi boundary the two cells share (nV x nC_mem,
+    column-major like C).  Cells are bounded by the circumcentres of the vertex's triangles; on
+    the domain border by the border edges' midpoints and the vertex itself.  A boundary shared
+    across an interior edge runs between the circumcentres of its two triangles, across a border
+    edge from the circumcentre to the edge's midpoint.  Areas are signed polygon areas, so the
+    cells tile the domain exactly even where a circumcentre lies outside its triangle."""
+    V = np.asarray(mesh.V)
+    cc = circumcentres(mesh)
+    ct = connection_triangles(mesh)
+    nV, nC = mesh.nV, np.asarray(mesh.nC)
+    C = np.asarray(mesh.C, dtype=np.int64) - 1
+    Cw = np.zeros((nV, mesh.nC_mem))
+    for ci in range(mesh.nC_mem):
+        live = np.arange(nV)[ci < nC]
+        t1, t2 = ct[live, ci, 0], ct[live, ci, 1]
+        mid = 0.5 * (V[live] + V[C[live, ci]])
+        far = np.where((t2 >= 0)[:, None], cc[np.maximum(t2, 0)], mid)
+        Cw[live, ci] = np.hypot(*(cc[t1] - far).T)
+    # areas: the polygon of each cell, walked counter-clockwise
+    iT = np.asarray(mesh.iTri, dtype=np.int64) - 1
+    niT = np.asarray(mesh.niTri)
+    A = np.zeros(nV)
+    border = np.asarray(mesh.VBI) > 0
+    for k in range(mesh.nC_mem):
+        live = np.arange(nV)[(k < niT) & ~border]
+        a = cc[iT[live, k]]
+        b = cc[iT[live, (k + 1) % niT[live]]]
+        A[live] += 0.5 * (a[:, 0] * b[:, 1] - b[:, 0] * a[:, 1])
+    for vi in np.nonzero(border)[0]:
+        poly = [V[vi], 0.5 * (V[vi] + V[C[vi, 0]])]
+        poly += [cc[iT[vi, k]] for k in range(niT[vi])]
+        poly += [0.5 * (V[vi] + V[C[vi, nC[vi] - 1]])]
+        P = np.array(poly)
+        A[vi] = 0.5 * np.sum(P[:, 0] * np.roll(P[:, 1], -1) - np.roll(P[:, 0], -1) * P[:, 1])
+    return A, np.asfortranarray(Cw)
+
+
 def triangulate(points, xmin, xmax, ymin, ymax, nz=12, zeta=None):
     """Delaunay triangulation of the points into a :class:`Mesh`."""
     from scipy.spatial import Delaunay

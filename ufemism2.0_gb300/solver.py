@@ -12,6 +12,8 @@ reference's routine names with the reference's argument meaning:
 * ``solve_SSA_DIVA_linearised``
   (src/UFEMISM/ice_dynamics/conservation_of_momentum/SSA_DIVA/solve_linearised_SSA_DIVA.f90:23-178)
 * ``solve_SSA`` (.../SSA_DIVA/SSA_main.f90:87-242) and ``solve_DIVA`` (.../DIVA_main.f90:88-262)
+* ``calc_dHi_dt`` (src/UFEMISM/ice_dynamics/conservation_of_mass/conservation_of_mass_main.f90:23-109),
+  after ``voronoi_upload`` of the mesh's cell areas and connection widths
 
 Errors: a negative status raises :class:`UfeError` (the reference's ``crash``); positive statuses
 are warnings (the reference's ``warning``) and are returned.
@@ -284,6 +286,61 @@ class VelocitySolver:
         return u, v
 
     # -- thermodynamics on this mesh ---------------------------------------------------------
+    # -- ice thickness (conservation of mass) -------------------------------------------------
+    def voronoi_upload(self, A=None, Cw=None):
+        """The mesh's Voronoi cell areas and connection widths (type_mesh's A and Cw); computed by
+        mesh.voronoi_geometry when not given."""
+        if A is None or Cw is None:
+            from .mesh import voronoi_geometry
+            A, Cw = voronoi_geometry(self.mesh)
+        self._voronoi = (_d(A), np.asfortranarray(Cw, dtype=np.float64))
+        self._check(self.lib.ufe_mesh_voronoi_upload(self.ctx, abi.as_d(self._voronoi[0]), abi.as_d(self._voronoi[1])))
+        return self._voronoi
+
+    def calc_dHi_dt(self, params, fields: dict, dt: float):
+        """calc_dHi_dt: fields holds the inputs (Hi, Hb, SL, u_vav_b, v_vav_b and the optional SMB,
+        BMB, LMB, fraction_margin, mask_noice, dHi_dt_target, BC_prescr_mask/Hi) and, when present,
+        dHi_dt (the previous rate, the semi-implicit initial guess).  Returns a dict with dHi_dt,
+        Hi_tplusdt, divQ, AMB, dt (the time step used) and the stats."""
+        nV = self.mesh.nV
+        f = {k: fields[k] for k in abi.THICKNESS_INPUTS if fields.get(k) is not None}
+        for k in ("mask_noice", "BC_prescr_mask"):
+            if k in f:
+                f[k] = np.ascontiguousarray(f[k], dtype=np.int32)
+        for k in f:
+            if k not in ("mask_noice", "BC_prescr_mask"):
+                f[k] = _d(f[k])
+        prev = fields.get("dHi_dt")
+        out = {"dHi_dt": _d(prev).copy() if prev is not None else np.zeros(nV),
+               "Hi_tplusdt": np.zeros(nV), "divQ": np.zeros(nV), "AMB": np.zeros(nV)}
+        f.update(out)
+        tf, keep = abi.thickness_fields(f)
+        d = C.c_double(dt)
+        st = abi.ThicknessStats()
+        self._check(self.lib.ufe_calc_dHi_dt(self.ctx, C.byref(params), C.byref(tf), C.byref(d), C.byref(st)))
+        out["dt"] = d.value
+        out["stats"] = st.as_dict()
+        return out
+
+    def thickness_assemble(self, params, fields: dict, dt: float):
+        """The semi-implicit system before its solve: (ptr, ind, val) 0-based, load vector, initial guess."""
+        nV = self.mesh.nV
+        f = {k: fields[k] for k in abi.THICKNESS_INPUTS if fields.get(k) is not None}
+        for k in list(f):
+            f[k] = np.ascontiguousarray(f[k], dtype=np.int32 if k in ("mask_noice", "BC_prescr_mask") else np.float64)
+        prev = fields.get("dHi_dt")
+        f.update({"dHi_dt": _d(prev).copy() if prev is not None else np.zeros(nV), "Hi_tplusdt": np.zeros(nV),
+                  "divQ": np.zeros(nV), "AMB": np.zeros(nV)})
+        tf, keep = abi.thickness_fields(f)
+        cap = int(nV + np.asarray(self.mesh.nC).sum())
+        ptr, ind = np.zeros(nV + 1, np.int32), np.zeros(cap, np.int32)
+        val, bb, x0 = np.zeros(cap), np.zeros(nV), np.zeros(nV)
+        nnz = C.c_int64()
+        self._check(self.lib.ufe_thickness_assemble(self.ctx, C.byref(params), C.byref(tf), dt, abi.as_i(ptr),
+                                                    abi.as_i(ind), abi.as_d(val), abi.as_d(bb), abi.as_d(x0), cap,
+                                                    C.byref(nnz)))
+        return ptr, ind[:nnz.value], val[:nnz.value], bb, x0
+
     def solve_3D_heat_equation(self, fields: dict, params):
         """solve_3D_heat_equation (thermodynamics_3D_heat_equation.f90:33): the prelude and the
         column loop on the GPU; returns (Ti_next (nV, nz), n_unstable)."""
