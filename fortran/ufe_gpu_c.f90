@@ -28,6 +28,9 @@ module ufe_gpu_c
   integer(c_int32_t), parameter :: UFE_RHEOLOGY_INPUT = 0, UFE_RHEOLOGY_UNIFORM = 1, UFE_RHEOLOGY_HUYBRECHTS1992 = 2
   integer(c_int32_t), parameter :: UFE_ENH_SEPARATE = 0, UFE_ENH_INTERP = 1
   integer(c_int32_t), parameter :: UFE_COL_NONE = 0, UFE_COL_GROUNDED = 1, UFE_COL_FLOATING = 2, UFE_COL_GL_GR = 3
+  ! enum ufe_ice_integration, ufe_bc_H
+  integer(c_int32_t), parameter :: UFE_DHI_NONE = 0, UFE_DHI_EXPLICIT = 1, UFE_DHI_SEMIIMPLICIT = 2
+  integer(c_int32_t), parameter :: UFE_BC_H_ZERO = 0, UFE_BC_H_INFINITE = 1
 
   type, bind(C) :: ufe_mesh_desc
     integer(c_int32_t) :: nV, nTri, nC_mem, nz
@@ -93,7 +96,41 @@ module ufe_gpu_c
     real(c_double) :: Glens_flow_law_exponent
   end type
 
+  type, bind(C) :: ufe_thickness_params
+    integer(c_int32_t) :: choice_ice_integration_method, BC_H_west, BC_H_east, BC_H_south, BC_H_north
+    integer(c_int32_t) :: dHi_PETSc_max_it
+    real(c_double) :: dHi_semiimplicit_fs, dHi_PETSc_rtol, dHi_PETSc_abstol, dt_ice_max, dt_ice_min, Hi_min
+    integer(c_int32_t) :: reserved(4)
+  end type
+
+  type, bind(C) :: ufe_thickness_fields
+    type(c_ptr) :: Hi, Hb, SL, u_vav_b, v_vav_b, SMB, BMB, LMB, fraction_margin, mask_noice, dHi_dt_target
+    type(c_ptr) :: BC_prescr_mask, BC_prescr_Hi, dHi_dt, Hi_tplusdt, divQ, AMB
+  end type
+
+  type, bind(C) :: ufe_thickness_stats
+    integer(c_int32_t) :: n_Axb_its, krylov_status, found_negative, pad
+    real(c_double) :: device_ms
+  end type
+
   interface
+    subroutine ufe_default_thickness_params(p) bind(C, name='ufe_default_thickness_params')
+      import :: ufe_thickness_params
+      type(ufe_thickness_params), intent(out) :: p
+    end subroutine
+    integer(c_int32_t) function ufe_mesh_voronoi_upload(ctx, A, Cw) bind(C, name='ufe_mesh_voronoi_upload')
+      import :: c_int32_t, c_ptr, c_double
+      type(c_ptr), value :: ctx
+      real(c_double), intent(in) :: A(*), Cw(*)
+    end function
+    integer(c_int32_t) function ufe_calc_dHi_dt(ctx, p, f, dt, st) bind(C, name='ufe_calc_dHi_dt')
+      import :: c_int32_t, c_ptr, c_double, ufe_thickness_params, ufe_thickness_fields, ufe_thickness_stats
+      type(c_ptr), value :: ctx
+      type(ufe_thickness_params), intent(in) :: p
+      type(ufe_thickness_fields), intent(in) :: f
+      real(c_double), intent(inout) :: dt
+      type(ufe_thickness_stats), intent(out) :: st
+    end function
     subroutine ufe_default_params(p) bind(C, name='ufe_default_params')
       import :: ufe_solver_params
       type(ufe_solver_params), intent(out) :: p

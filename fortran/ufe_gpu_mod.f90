@@ -34,8 +34,10 @@ module ufe_gpu_mod
   public :: ufe_attach_mesh, ufe_detach, gpu_solve_SSA, gpu_solve_DIVA, gpu_solve_matrix_equation_CSR_PETSc
   public :: gpu_map_a_b_2D, gpu_ddx_a_b_2D, gpu_ddy_a_b_2D, gpu_map_b_a_2D, gpu_ddx_b_a_2D, gpu_ddy_b_a_2D
   public :: gpu_map_a_b_3D, gpu_map_b_a_3D, gpu_solve_3D_heat_equation, gpu_solve_tridiagonal_matrix_equation
+  public :: gpu_calc_dHi_dt
 
   type(c_ptr), save :: ctx = c_null_ptr
+  logical, save :: voronoi_uploaded = .false.    ! mesh%A, mesh%Cw sent for the attached mesh
 
 contains
 
@@ -57,6 +59,7 @@ contains
       c_loc(mesh%TriBI), c_loc(mesh%TriGC), c_loc(mesh%zeta))
     call check(ufe_mesh_upload(ctx, d), 'ufe_mesh_upload')
     call check(ufe_mesh_build_operators(ctx), 'ufe_mesh_build_operators')
+    voronoi_uploaded = .false.
   end subroutine
 
   subroutine ufe_detach()
@@ -365,5 +368,66 @@ contains
     call check(ufe_tridiagonal_solve(ctx, int(n, c_int32_t), 1_c_int32_t, a_n, b, c_n, d, x), &
       'solve_tridiagonal_matrix_equation')
   end subroutine
+
+  ! calc_dHi_dt (conservation_of_mass_main.f90:23-109) with the same arguments; the mesh's Voronoi
+  ! geometry (mesh%A, mesh%Cw) goes to the GPU on the first call after each ufe_attach_mesh
+  subroutine gpu_calc_dHi_dt(mesh, Hi, Hb, SL, u_vav_b, v_vav_b, SMB, BMB, LMB, AMB, fraction_margin, &
+      mask_noice, dt, dHi_dt, Hi_tplusdt, divQ, dHi_dt_target, BC_prescr_mask, BC_prescr_Hi)
+    type(type_mesh), target, intent(in) :: mesh
+    real(dp), dimension(mesh%vi1:mesh%vi2), target, intent(in) :: Hi, Hb, SL, SMB, BMB, LMB, fraction_margin
+    real(dp), dimension(mesh%ti1:mesh%ti2), target, intent(in) :: u_vav_b, v_vav_b
+    real(dp), dimension(mesh%vi1:mesh%vi2), target, intent(inout) :: AMB
+    logical, dimension(mesh%vi1:mesh%vi2), intent(in) :: mask_noice
+    real(dp), intent(inout) :: dt
+    real(dp), dimension(mesh%vi1:mesh%vi2), target, intent(inout) :: dHi_dt    ! in: the previous rate
+    real(dp), dimension(mesh%vi1:mesh%vi2), target, intent(out) :: Hi_tplusdt, divQ
+    real(dp), dimension(mesh%vi1:mesh%vi2), target, intent(in) :: dHi_dt_target
+    integer, dimension(mesh%vi1:mesh%vi2), target, intent(in), optional :: BC_prescr_mask
+    real(dp), dimension(mesh%vi1:mesh%vi2), target, intent(in), optional :: BC_prescr_Hi
+    type(ufe_thickness_params) :: p
+    type(ufe_thickness_fields) :: f
+    type(ufe_thickness_stats) :: st
+    integer(c_int32_t), allocatable, target :: noice(:), prescr(:)
+    if (.not. voronoi_uploaded) then
+      call check(ufe_mesh_voronoi_upload(ctx, mesh%A, mesh%Cw), 'ufe_mesh_voronoi_upload')
+      voronoi_uploaded = .true.
+    end if
+    call ufe_default_thickness_params(p)
+    select case (trim(C%choice_ice_integration_method))
+    case ('none');          p%choice_ice_integration_method = UFE_DHI_NONE
+    case ('explicit');      p%choice_ice_integration_method = UFE_DHI_EXPLICIT
+    case ('semi-implicit'); p%choice_ice_integration_method = UFE_DHI_SEMIIMPLICIT
+    case default; call crash('unknown choice_ice_integration_method "' // trim(C%choice_ice_integration_method) // '"!')
+    end select
+    p%BC_H_west = bc_H_code(C%BC_H_west); p%BC_H_east = bc_H_code(C%BC_H_east)
+    p%BC_H_south = bc_H_code(C%BC_H_south); p%BC_H_north = bc_H_code(C%BC_H_north)
+    p%dHi_semiimplicit_fs = C%dHi_semiimplicit_fs
+    p%dHi_PETSc_rtol = C%dHi_PETSc_rtol; p%dHi_PETSc_abstol = C%dHi_PETSc_abstol
+    p%dt_ice_max = C%dt_ice_max; p%dt_ice_min = C%dt_ice_min; p%Hi_min = C%Hi_min
+    noice = merge(1_c_int32_t, 0_c_int32_t, mask_noice)
+    f%Hi = c_loc(Hi); f%Hb = c_loc(Hb); f%SL = c_loc(SL); f%u_vav_b = c_loc(u_vav_b); f%v_vav_b = c_loc(v_vav_b)
+    f%SMB = c_loc(SMB); f%BMB = c_loc(BMB); f%LMB = c_loc(LMB); f%fraction_margin = c_loc(fraction_margin)
+    f%mask_noice = c_loc(noice); f%dHi_dt_target = c_loc(dHi_dt_target)
+    f%BC_prescr_mask = c_null_ptr; f%BC_prescr_Hi = c_null_ptr
+    if (present(BC_prescr_mask) .or. present(BC_prescr_Hi)) then
+      if (.not. (present(BC_prescr_mask) .and. present(BC_prescr_Hi))) call crash('need to provide prescribed both Hi and mask!')
+      prescr = int(BC_prescr_mask, c_int32_t)
+      f%BC_prescr_mask = c_loc(prescr); f%BC_prescr_Hi = c_loc(BC_prescr_Hi)
+    end if
+    f%dHi_dt = c_loc(dHi_dt); f%Hi_tplusdt = c_loc(Hi_tplusdt); f%divQ = c_loc(divQ); f%AMB = c_loc(AMB)
+    call check(ufe_calc_dHi_dt(ctx, p, f, dt, st), 'calc_dHi_dt')
+    if (st%found_negative /= 0) call warning('encountered negative values for Hi_tplusdt - time step too large?')
+  end subroutine
+
+  integer(c_int32_t) function bc_H_code(s)
+    character(len=*), intent(in) :: s
+    select case (trim(s))
+    case ('zero');     bc_H_code = UFE_BC_H_ZERO
+    case ('infinite'); bc_H_code = UFE_BC_H_INFINITE
+    case default
+      call crash('unknown BC_H "' // trim(s) // '"')
+      bc_H_code = -1
+    end select
+  end function
 
 end module ufe_gpu_mod

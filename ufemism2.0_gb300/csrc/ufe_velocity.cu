@@ -263,12 +263,14 @@ __global__ void k_icestream_yield(int nV, const double *Vy, double H, double tan
 // The triangle terms of calc_vertical_shear_strain_rates (DIVA_main.f90:375-410):
 // du/dz_b = tau_bx_b zeta / max(visc_eff_min, eta_3D_b) (and v), per triangle and layer, from the
 // previous iteration's basal stress and 3-D viscosity.  Formed once per triangle (the vertex
-// kernel's b->a sums then read them) rather than once per vertex row entry; same expression.
+// kernel's b->a sums then read them) rather than once per vertex row entry, as tau (zeta / eta):
+// one FP64 division per layer instead of two (the reference's (tau zeta) / eta rounds differently
+// by an ulp or so).
 __device__ __forceinline__ void diva_shear_b(int64_t t, int nTri, int nz, double2 tb, const double *eta_3D_b,
                                              const double *zeta, double visc_eff_min, double2 *duz_b) {
   for (int l = 0; l < nz; ++l) {
-    const double e = fmax(visc_eff_min, eta_3D_b[(int64_t)l * nTri + t]);
-    duz_b[(int64_t)l * nTri + t] = make_double2(tb.x * zeta[l] / e, tb.y * zeta[l] / e);
+    const double f = zeta[l] / fmax(visc_eff_min, eta_3D_b[(int64_t)l * nTri + t]);
+    duz_b[(int64_t)l * nTri + t] = make_double2(tb.x * f, tb.y * f);
   }
 }
 __global__ void k_diva_shear_b(int nTri, int nz, const double2 *tau_b, const double *eta_3D_b, const double *zeta,
@@ -455,7 +457,10 @@ __global__ void k_assemble(AssembleArgs a, PhysParams q, CondArg cond) {
           f2 = f2 + m * a.F2a1[v];
         }
       }
-      if (q.gl_subgrid) beta = beta * pow(a.fgr_b[t], q.fgr_exp);
+      if (q.gl_subgrid) {   // f_gr^p; the default p = 2 as a product
+        const double f = a.fgr_b[t];
+        beta = beta * (q.fgr_exp == 2.0 ? f * f : q.fgr_exp == 1.0 ? f : pow(f, q.fgr_exp));
+      }
       if (MODE == kFromDIVA) {
         a.bfc_b[t] = bfc;
         a.F2b1[t] = f2;
