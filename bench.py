@@ -728,8 +728,9 @@ def run_thickness(args):
                                    f"dome H0 3000 m R 330 km on an 800 km square, {args.thick_res / 1e3:g} km mesh",
                        "nV": mesh.nV, "nTri": mesh.nTri, "matrix_entries": nnz, "dt_yr": dt,
                        "krylov_its_mean": mean_its, "host_build_s": round(build_s, 1),
-                       "l2": "every step uploads its inputs; the working set (about "
-                             f"{nbytes / max(mean_its, 1) / 1e6:.0f} MB) is under L2"},
+                       "l2": "every step uploads its inputs; the working set (matrix entries "
+                             f"{nnz * 20 / 1e6:.0f} MB, vertex and triangle fields "
+                             f"{(mesh.nV * 30 * 8 + mesh.nTri * 16) / 1e6:.0f} MB) exceeds the 129 MB L2"},
             "e2e": {"value": round(e2e_value, 2), "unit": THICKNESS_UNIT, "h2d_bytes_per_step": int(in_bytes),
                     "d2h_bytes_per_step": int(4 * 8 * mesh.nV),
                     "note": "ufe_calc_dHi_dt with pinned host arrays: upload, step, download of dHi_dt, "
@@ -1148,8 +1149,12 @@ def run_mixed(args):
     pkg = __graft_entry__.load_package()
     mine = pkg.ensemble.shard(rank, world, sizes)
     t0 = time.perf_counter()
+    # training geometries of the learned start: seeds apart from the members', 20k-60k vertices
+    train_jobs = [(10_000 + i, int(20_000 * 3.0 ** (i / max(args.mixed_train - 1, 1))))
+                  for i in range(args.mixed_train)] if args.mixed_mode == "sequential" else []
     with mp.get_context("spawn").Pool(processes=max(1, min(len(mine), os.cpu_count() or 1))) as pool:
         built = sorted(pool.map(_mixed_member, [(k, sizes[k]) for k in mine]), key=lambda t: t[0])
+        train = pool.map(_mixed_member, train_jobs) if train_jobs else []
     gen_s = time.perf_counter() - t0
     print(f"rank {rank}: {len(built)} members built in {gen_s:.0f} s", file=sys.stderr, flush=True)
     torch.cuda.set_device(local)
@@ -1158,7 +1163,7 @@ def run_mixed(args):
     pkg.build()
     p = pkg.geometry.mixed_ensemble_params()
     if args.mixed_mode == "sequential":
-        return run_mixed_sequential(args, pkg, built, p, gen_s, rank, world, local)
+        return run_mixed_sequential(args, pkg, built, p, gen_s, rank, world, local, train)
     solvers = []
     for k, mesh, ice in built:
         sv = pkg.VelocitySolver(mesh, device=local)
@@ -1207,35 +1212,65 @@ def run_mixed(args):
     print(json.dumps(line))
 
 
-def run_mixed_sequential(args, pkg, built, p, gen_s, rank, world, local):
+def run_mixed_sequential(args, pkg, built, p, gen_s, rank, world, local, train=()):
     """Config 4 member by member: each member's solve has the whole GPU, so it runs with the
     persistent Krylov kernels (members side by side cannot: a persistent kernel needs every SM).
-    Two paths per member, each solved once (the device time of a solve excludes its graph
-    capture): plain FP64 -- the reference's algorithm -- and double-word Krylov inside the inexact
-    Picard iteration; the per-member distance between their answers is reported."""
+    Three paths per member, each solved once (the device time of a solve excludes its graph
+    capture): plain FP64 -- the reference's algorithm --, double-word Krylov inside the inexact
+    Picard iteration, and the same from the learned start with its predicted viscosity (the
+    network trained beforehand on the `train` geometries, outside the timed region); the
+    per-member distances between the answers are reported."""
     import torch
 
     p64 = _with(pkg, p, precision=pkg.abi.PREC_FP64, visc_it_nit=args.picard_nit)
     pfast = _with(pkg, p, precision=pkg.abi.PREC_FP32_PAIR, krylov_forcing=args.forcing, visc_it_nit=args.picard_nit)
+    net, host, train_info = None, None, None
+    if train:
+        host = pkg.ColumnSolver(device=local)
+        net = pkg.LearnedStart(host, seed=1)
+        gen_ms, t_tr = 0.0, time.perf_counter()
+        for k, mesh, ice in train:
+            with pkg.VelocitySolver(mesh, device=local) as sv:
+                sv.ice_upload(ice)
+                x = net.features(sv)
+                gen_ms += sv.solve_resident(p64, diva=True, cold_start=True)["device_ms"]
+                net.dataset_add(sv, x)
+        losses, train_ms = net.train(epochs=args.mixed_epochs, lr=2e-3)
+        net.dataset_clear()
+        train_info = {"geometries": len(train), "vertices": [int(m.nV) for _, m, _ in train],
+                      "solves_device_s": round(gen_ms / 1000.0, 2), "train_ms": round(train_ms, 1),
+                      "wall_s": round(time.perf_counter() - t_tr, 1),
+                      "loss_first_last": [float(losses[0]), float(losses[-1])]}
+    paths = (("fp64", p64, False), ("fp32_pair_inexact", pfast, False)) + \
+            ((("learned_visc_fp32_pair_inexact", pfast, True),) if net else ())
     rows = {}
     with ClockSampler(local) as clocks:
         for k, mesh, ice in built:
             with pkg.VelocitySolver(mesh, device=local) as sv:
                 sv.ice_upload(ice)
                 r = {"nV": mesh.nV}
-                for name, pp in (("fp64", p64), ("fp32_pair_inexact", pfast)):
+                u = {}
+                for name, pp, learned in paths:
                     try:
-                        st = sv.solve_resident(pp, diva=True, cold_start=True)
-                        r[name] = {"ms": st["device_ms"], "picard": st["n_visc_its"], "krylov": st["n_Axb_its"],
-                                   "status": st["status"], "u": np.r_[sv.velocity_download()]}
+                        pred = net.predict(sv, smooth_passes=2, viscosity=True) if learned else 0.0
+                        st = sv.solve_resident(pp, diva=True, cold_start=not learned)
+                        r[name] = {"ms": st["device_ms"] + pred, "picard": st["n_visc_its"],
+                                   "krylov": st["n_Axb_its"], "status": st["status"]}
+                        u[name] = np.r_[sv.velocity_download()]
                     except pkg.UfeError as e:
                         r[name] = {"ms": None, "status": e.code}
-                if r["fp64"].get("u") is not None and r["fp32_pair_inexact"].get("u") is not None:
-                    a, b = r["fp64"].pop("u"), r["fp32_pair_inexact"].pop("u")
-                    r["rel_l2_fast_vs_fp64"] = float("%.3g" % (np.linalg.norm(b - a) / np.linalg.norm(a)))
+                if "fp64" in u:
+                    a = u["fp64"]
+                    for name in u:
+                        if name != "fp64":
+                            key = "rel_l2_fast_vs_fp64" if name == "fp32_pair_inexact" else f"rel_l2_{name}_vs_fp64"
+                            r[key] = float("%.3g" % (np.linalg.norm(u[name] - a) / np.linalg.norm(a)))
                 rows[k] = r
-            print(f"member {k}: {mesh.nV} vertices, FP64 {r['fp64'].get('ms')} ms, fast "
-                  f"{r['fp32_pair_inexact'].get('ms')} ms", file=sys.stderr, flush=True)
+            print(f"member {k}: {mesh.nV} vertices, " + ", ".join(f"{n} {r[n].get('ms')} ms" for n, _, _ in paths),
+                  file=sys.stderr, flush=True)
+    if net:
+        net.close()
+        host.close()
     results = pkg.ensemble.gather_results(rows)
     if rank != 0:
         return
@@ -1244,6 +1279,15 @@ def run_mixed_sequential(args, pkg, built, p, gen_s, rank, world, local):
     t64 = sum(results[k]["fp64"]["ms"] or 0.0 for k in order) / 1000.0
     tf = sum(results[k]["fp32_pair_inexact"]["ms"] or 0.0 for k in order) / 1000.0
     errs = [results[k].get("rel_l2_fast_vs_fp64") for k in order if results[k].get("rel_l2_fast_vs_fp64") is not None]
+    learned = None
+    if train:
+        tl = sum(results[k]["learned_visc_fp32_pair_inexact"]["ms"] or 0.0 for k in order) / 1000.0
+        el = [results[k].get("rel_l2_learned_visc_fp32_pair_inexact_vs_fp64") for k in order
+              if results[k].get("rel_l2_learned_visc_fp32_pair_inexact_vs_fp64") is not None]
+        learned = {"value": round(world * n / tl, 4) if tl > 0 else None, "unit": UNIT, "device_s": round(tl, 2),
+                   "speedup_vs_plain_fp64": round(t64 / tl, 3) if tl > 0 else None,
+                   "rel_l2_vs_fp64": {"median": float(np.median(el)), "max": float(np.max(el))} if el else None,
+                   "training": train_info}
     line = {"metric": f"mixed-size DIVA ensemble solves/s, members one after another, {world}xGB300",
             "value": round(world * n / tf, 4), "unit": UNIT, "n_gpus": world, "steps": 1, "warmup": 0,
             "ms_per_step": round(1000.0 * tf, 1), "higher_is_better": True,
@@ -1257,6 +1301,7 @@ def run_mixed_sequential(args, pkg, built, p, gen_s, rank, world, local):
             "plain_fp64": {"value": round(world * n / t64, 4), "unit": UNIT, "device_s": round(t64, 2)},
             "speedup_vs_plain_fp64": round(t64 / tf, 3),
             "rel_l2_fast_vs_fp64": {"median": float(np.median(errs)), "max": float(np.max(errs))} if errs else None,
+            "learned_visc_fp32_pair_inexact": learned,
             "members": {str(k): results[k] for k in order},
             "host_build_s": round(gen_s, 1),
             "clocks": clocks.summary()}
@@ -1516,6 +1561,9 @@ def main():
                     help="krylov_forcing of the inexact-Picard path (the early linear solves' residual reduction)")
     ap.add_argument("--picard-nit", type=int, default=200,
                     help="visc_it_nit of every channel path (a limit only: the tolerance ends the solves)")
+    ap.add_argument("--mixed-train", type=int, default=12,
+                    help="config 4: training geometries of the learned start (20k-60k vertices; 0: no learned path)")
+    ap.add_argument("--mixed-epochs", type=int, default=60)
     ap.add_argument("--mixed-mode", choices=["sequential", "side_by_side"], default="sequential",
                     help="config 4: members one after another with the persistent kernels, or side by side")
     ap.add_argument("--ref-tols", type=float, nargs="+", default=[1e-10, 1e-9, 1e-8, 1e-7, 1e-6],

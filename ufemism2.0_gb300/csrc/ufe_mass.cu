@@ -3,9 +3,11 @@
 // explicit scheme (conservation_of_mass_explicit.f90:22-134, border rule :136-283) and the
 // semi-implicit scheme (conservation_of_mass_semiimplicit.f90:23-174, matrix conditions :176-314).
 //
-// The work runs on the caller's vertex numbering, on the mesh arrays as uploaded, so the
-// semi-implicit matrix comes out in the reference's add_entry layout without a permutation: row
-// vi holds the diagonal, then the connections C(vi, 1:nC) in order.  One thread per vertex row:
+// The work runs in the context's internal (Z-ordered) vertex numbering, on its renumbered mesh
+// arrays; every row keeps the reference's add_entry layout -- the diagonal, then the connections
+// C(vi, 1:nC) in the caller's order, which the renumbering keeps -- so the values are those of
+// the caller's numbering and an export only renames rows and columns.  Fields cross the ABI
+// through a staging buffer and one gather per array.  One thread per vertex row:
 //   k_divq_matrix   M_divQ (calc_ice_flux_divergence_matrix_upwind, conservation_of_mass_utilities.f90:22-132),
 //                   the edge velocity of map_velocities_from_b_to_c_2D (map_velocities_to_c_grid.f90:17-69)
 //                   read through the precomputed triangle pair of each connection;
@@ -20,6 +22,7 @@
 // Every expression keeps the reference's operation order, and the library is built without FMA
 // contraction, so the explicit step and the assembled system are bit-identical to the oracle's.
 // The semi-implicit matrix equation goes to the library's CSR BiCGStab/Jacobi.
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -50,11 +53,23 @@ struct MassWork {
   unsigned long long *dtlim = nullptr;          // [0], [1]: bit patterns of the limits
   int32_t *flag = nullptr;                      // negative thickness found
   CsrSolveScratch krylov;                       // the semi-implicit solve's work vectors
+  double *stage = nullptr;                      // max(nV, nTri): fields in the caller's order
+  int32_t *stagei = nullptr;                    // nV
 };
 
 namespace {
 
 __device__ __forceinline__ double opt(const double *a, int64_t i, double d) { return a ? a[i] : d; }
+
+// dst[c*n + i] = src[c*n + map[i]] (caller -> internal with perm, internal -> caller with iperm)
+template <class T>
+__global__ void k_permute(int64_t n, int ncols, const T *__restrict__ src, const int32_t *__restrict__ map,
+                          T *__restrict__ dst) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n * ncols) return;
+  const int64_t c = e / n, i = e - c * n;
+  dst[e] = src[c * n + map[i]];
+}
 
 __device__ __forceinline__ double surface_elevation(double Hi, double Hb, double SL) {
   return Hi + fmax(SL - kIceDensityM / kSeawaterDensityM * Hi, Hb);   // ice_geometry_basics.f90:28-41
@@ -320,37 +335,43 @@ void alloc_fields(MassWork *w) {
   w->valM = alloc_n<double>(w->nnz);
   w->valA = alloc_n<double>(w->nnz);
   csr_scratch_alloc(w->krylov, w->nV);
+  w->stage = alloc_n<double>(std::max(nV, nT));
+  w->stagei = alloc_n<int32_t>(nV);
 }
 
 MeshRef mesh_ref(ufe_ctx *ctx) { return MeshRef{ctx->nV, ctx->nTri, ctx->V, ctx->nC, ctx->C, ctx->VBI}; }
 
-// upload the fields the caller gave; returns the device-side view (null where not given)
+// upload the fields the caller gave, in the internal numbering; returns the device-side view
+// (null where not given)
 Inputs upload_inputs(ufe_ctx *ctx, MassWork *w, const ufe_thickness_fields *f) {
   cudaStream_t s = ctx->stream;
   const size_t nV = w->nV, nT = w->nTri;
-  auto up = [&](double *d, const double *h, size_t n) -> const double * {
+  auto up = [&](double *d, const double *h, bool tri) -> const double * {
     if (!h) return nullptr;
-    UFE_CUDA(cudaMemcpyAsync(d, h, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+    const size_t n = tri ? nT : nV;
+    UFE_CUDA(cudaMemcpyAsync(w->stage, h, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+    k_permute<double><<<blocks(n), 256, 0, s>>>((int64_t)n, 1, w->stage, tri ? ctx->perm_t : ctx->perm_v, d);
     return d;
   };
   auto upi = [&](int32_t *d, const int32_t *h) -> const int32_t * {
     if (!h) return nullptr;
-    UFE_CUDA(cudaMemcpyAsync(d, h, sizeof(int32_t) * nV, cudaMemcpyHostToDevice, s));
+    UFE_CUDA(cudaMemcpyAsync(w->stagei, h, sizeof(int32_t) * nV, cudaMemcpyHostToDevice, s));
+    k_permute<int32_t><<<blocks(nV), 256, 0, s>>>((int64_t)nV, 1, w->stagei, ctx->perm_v, d);
     return d;
   };
   Inputs in;
-  in.Hi = up(w->Hi, f->Hi, nV);
-  in.Hb = up(w->Hb, f->Hb, nV);
-  in.SL = up(w->SL, f->SL, nV);
-  up(w->u, f->u_vav_b, nT);
-  up(w->v, f->v_vav_b, nT);
-  in.SMB = up(w->SMB, f->SMB, nV);
-  in.BMB = up(w->BMB, f->BMB, nV);
-  in.LMB = up(w->LMB, f->LMB, nV);
-  in.fm = up(w->fm, f->fraction_margin, nV);
-  in.target = up(w->target, f->dHi_dt_target, nV);
-  in.prHi = up(w->prHi, f->BC_prescr_Hi, nV);
-  in.dprev = up(w->dprev, f->dHi_dt, nV);
+  in.Hi = up(w->Hi, f->Hi, false);
+  in.Hb = up(w->Hb, f->Hb, false);
+  in.SL = up(w->SL, f->SL, false);
+  up(w->u, f->u_vav_b, true);
+  up(w->v, f->v_vav_b, true);
+  in.SMB = up(w->SMB, f->SMB, false);
+  in.BMB = up(w->BMB, f->BMB, false);
+  in.LMB = up(w->LMB, f->LMB, false);
+  in.fm = up(w->fm, f->fraction_margin, false);
+  in.target = up(w->target, f->dHi_dt_target, false);
+  in.prHi = up(w->prHi, f->BC_prescr_Hi, false);
+  in.dprev = up(w->dprev, f->dHi_dt, false);
   in.noice = upi(w->noice, f->mask_noice);
   in.prmask = upi(w->prmask, f->BC_prescr_mask);
   return in;
@@ -410,6 +431,14 @@ void semi_system(ufe_ctx *ctx, MassWork *w, const ufe_thickness_params *p, const
   UFE_CUDA(cudaGetLastError());
 }
 
+// an internal vertex field into the caller's host array
+void download_vertex(ufe_ctx *ctx, MassWork *w, double *h, const double *d) {
+  cudaStream_t s = ctx->stream;
+  k_permute<double><<<blocks(w->nV), 256, 0, s>>>(w->nV, 1, d, ctx->iperm_v, w->stage);
+  UFE_CUDA(cudaMemcpyAsync(h, w->stage, sizeof(double) * w->nV, cudaMemcpyDeviceToHost, s));
+  UFE_CUDA(cudaStreamSynchronize(s));   // the staging buffer is reused by the next field
+}
+
 void prepare(ufe_ctx *ctx, MassWork *w, const ufe_thickness_params *p, const Inputs &in) {
   cudaStream_t s = ctx->stream;
   const int nV = w->nV;
@@ -429,7 +458,7 @@ void free_mass(ufe_ctx *ctx) {
   void *ptrs[] = {w->A, w->Cw, w->ct, w->ptr, w->ind, w->valM, w->valA, w->Hi, w->Hb, w->SL, w->u, w->v,
                   w->SMB, w->BMB, w->LMB, w->fm, w->target, w->prHi, w->dprev, w->noice, w->prmask, w->dHdt,
                   w->Hit, w->divQ, w->AMB, w->dex, w->Hex, w->qex, w->aex, w->Hs, w->Hs_tot, w->bb, w->nint,
-                  w->dt, w->dtlim, w->flag};
+                  w->dt, w->dtlim, w->flag, w->stage, w->stagei};
   for (void *q : ptrs) dev_free(q);
   csr_scratch_free(w->krylov);
   delete w;
@@ -468,8 +497,14 @@ extern "C" int32_t ufe_mesh_voronoi_upload(ufe_ctx *ctx, const double *A, const 
     w->A = alloc_n<double>(w->nV);
     w->Cw = alloc_n<double>(nc);
     w->ct = alloc_n<int2>(nc);
-    UFE_CUDA(cudaMemcpyAsync(w->A, A, sizeof(double) * w->nV, cudaMemcpyHostToDevice, s));
-    UFE_CUDA(cudaMemcpyAsync(w->Cw, Cw, sizeof(double) * nc, cudaMemcpyHostToDevice, s));
+    double *tmp = alloc_n<double>(nc);   // the caller's order, then gathered into the internal one
+    UFE_CUDA(cudaMemcpyAsync(tmp, A, sizeof(double) * w->nV, cudaMemcpyHostToDevice, s));
+    k_permute<double><<<blocks(w->nV), 256, 0, s>>>(w->nV, 1, tmp, ctx->perm_v, w->A);
+    UFE_CUDA(cudaMemcpyAsync(tmp, Cw, sizeof(double) * nc, cudaMemcpyHostToDevice, s));
+    UFE_CUDA(cudaStreamSynchronize(s));
+    k_permute<double><<<blocks((int64_t)nc), 256, 0, s>>>(w->nV, w->nC_mem, tmp, ctx->perm_v, w->Cw);
+    UFE_CUDA(cudaStreamSynchronize(s));
+    dev_free(tmp);
     k_conn_tris<<<blocks(w->nV), 256, 0, s>>>(w->nV, w->nTri, w->nC_mem, ctx->nC, ctx->C, ctx->niTri, ctx->iTri,
                                               ctx->Tri, w->ct);
     UFE_CUDA(cudaGetLastError());
@@ -511,12 +546,28 @@ extern "C" int32_t ufe_thickness_assemble(ufe_ctx *ctx, const ufe_thickness_para
     const Inputs in = upload_inputs(ctx, w, f);
     prepare(ctx, w, p, in);
     semi_system(ctx, w, p, in, dt, w->Hit);
-    UFE_CUDA(cudaMemcpyAsync(ptr, w->ptr, sizeof(int32_t) * (w->nV + 1), cudaMemcpyDeviceToHost, s));
-    UFE_CUDA(cudaMemcpyAsync(ind, w->ind, sizeof(int32_t) * w->nnz, cudaMemcpyDeviceToHost, s));
-    UFE_CUDA(cudaMemcpyAsync(val, w->valA, sizeof(double) * w->nnz, cudaMemcpyDeviceToHost, s));
-    UFE_CUDA(cudaMemcpyAsync(bb, w->bb, sizeof(double) * w->nV, cudaMemcpyDeviceToHost, s));
-    UFE_CUDA(cudaMemcpyAsync(x0, w->Hit, sizeof(double) * w->nV, cudaMemcpyDeviceToHost, s));
+    // rows back in the caller's numbering: caller row r is internal row iperm[r], entries in the
+    // same order, columns renamed through perm
+    const int nV = w->nV;
+    std::vector<int32_t> ip(nV + 1), ii(w->nnz);
+    std::vector<double> iv(w->nnz);
+    UFE_CUDA(cudaMemcpyAsync(ip.data(), w->ptr, sizeof(int32_t) * (nV + 1), cudaMemcpyDeviceToHost, s));
+    UFE_CUDA(cudaMemcpyAsync(ii.data(), w->ind, sizeof(int32_t) * w->nnz, cudaMemcpyDeviceToHost, s));
+    UFE_CUDA(cudaMemcpyAsync(iv.data(), w->valA, sizeof(double) * w->nnz, cudaMemcpyDeviceToHost, s));
     UFE_CUDA(cudaStreamSynchronize(s));
+    const std::vector<int32_t> &pv = ctx->perm_v_h, &iq = ctx->iperm_v_h;
+    int64_t k = 0;
+    for (int32_t r = 0; r < nV; ++r) {
+      ptr[r] = (int32_t)k;
+      const int32_t i = iq[r];
+      for (int32_t e = ip[i]; e < ip[i + 1]; ++e, ++k) {
+        ind[k] = pv[ii[e]];
+        val[k] = iv[e];
+      }
+    }
+    ptr[nV] = (int32_t)k;
+    download_vertex(ctx, w, bb, w->bb);
+    download_vertex(ctx, w, x0, w->Hit);
     return UFE_OK;
   });
 }
@@ -564,10 +615,10 @@ extern "C" int32_t ufe_calc_dHi_dt(ufe_ctx *ctx, const ufe_thickness_params *p, 
       UFE_CUDA(cudaGetLastError());
     }
     UFE_CUDA(cudaEventRecord(ctx->ev1, s));
-    UFE_CUDA(cudaMemcpyAsync(f->dHi_dt, w->dHdt, sizeof(double) * nV, cudaMemcpyDeviceToHost, s));
-    UFE_CUDA(cudaMemcpyAsync(f->Hi_tplusdt, w->Hit, sizeof(double) * nV, cudaMemcpyDeviceToHost, s));
-    UFE_CUDA(cudaMemcpyAsync(f->divQ, w->divQ, sizeof(double) * nV, cudaMemcpyDeviceToHost, s));
-    UFE_CUDA(cudaMemcpyAsync(f->AMB, w->AMB, sizeof(double) * nV, cudaMemcpyDeviceToHost, s));
+    download_vertex(ctx, w, f->dHi_dt, w->dHdt);
+    download_vertex(ctx, w, f->Hi_tplusdt, w->Hit);
+    download_vertex(ctx, w, f->divQ, w->divQ);
+    download_vertex(ctx, w, f->AMB, w->AMB);
     UFE_CUDA(cudaMemcpyAsync(dt, w->dt, sizeof(double), cudaMemcpyDeviceToHost, s));
     UFE_CUDA(cudaMemcpyAsync(&st.found_negative, w->flag, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
     UFE_CUDA(cudaStreamSynchronize(s));
