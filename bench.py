@@ -695,6 +695,15 @@ def run_thickness(args):
             wall = time.perf_counter() - t0
         nnz = int(mesh.nV + np.asarray(mesh.nC).sum())
         nconn = nnz - mesh.nV
+        # the reference's Halfar_dome integrated test for this step: 500 years with Halfar's
+        # velocity prescribed, RMSE of H against Halfar's solution per resolution
+        halfar_rows = []
+        for res in (40e3, 20e3, 10e3):
+            hm, hf, hp = pkg.geometry.halfar_case(res=res)
+            with pkg.VelocitySolver(hm, device=local) as hs:
+                hs.voronoi_upload()
+                _, rmse, nst = pkg.geometry.halfar_run(hs.calc_dHi_dt, hm, hf, hp)
+            halfar_rows.append({"resolution_km": res / 1e3, "nV": hm.nV, "steps": nst, "rmse_m": round(rmse, 2)})
     value = args.steps / (sum(dev_ms) / 1000.0)
     e2e_value = args.steps / wall
     mean_its = float(np.mean(its))
@@ -740,6 +749,11 @@ def run_thickness(args):
                          "achieved": round(achieved, 1), "peak": peaks.get("hbm_gbs"), "unit": "GB/s",
                          "frac": round(achieved / peaks.get("hbm_gbs"), 4), "peak_source": peak_kind,
                          "traffic": None, "algorithmic_bytes_per_step": int(nbytes)},
+            "halfar_dome": {"rows": halfar_rows,
+                            "reference_scoreboard_rmse_m": {"10 km": 18.02},
+                            "note": "500 yr of the semi-implicit step (f_s 1.5, dt 10 yr) with Halfar's (1983) "
+                                    "shallow-ice velocity prescribed; the reference's integrated test couples its "
+                                    "SIA solve instead"},
             "cpu_baseline": cpu,
             "clocks": clocks.summary(),
             "gpu_launches": int(args.steps * (12 + 1 + 3 * 8 * int(np.ceil(mean_its / 8)))),

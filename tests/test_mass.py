@@ -169,3 +169,44 @@ def test_gpu_thickness_at_size(pkg, gpu_lib):
     unclipped = x > 0
     r = (M @ x - bb)[unclipped]
     assert np.linalg.norm(r) <= 1e-7 * np.linalg.norm(bb) + 1e-6 * np.sqrt(mesh.nV)
+
+
+# ---- Halfar dome: the reference's integrated test for the thickness step ----------------------
+def _oracle_step(oracle_mod, mesh, A, Cw):
+    orc = oracle_mod.Oracle(mesh)
+
+    def step(p, f, dt):
+        q = _fields(f, mesh)
+        q["dt"], _ = orc.calc_dHi_dt(A, Cw, p, q, dt)
+        return q
+    return step
+
+
+def test_oracle_halfar_dome_converges(pkg, oracle_mod):
+    """500 years of the semi-implicit thickness step (f_s 1.5, dt 10 yr) with Halfar's (1983)
+    shallow-ice velocity prescribed at each step, as the reference's Halfar_dome integrated test
+    runs it with its SIA solve: the RMSE of H against Halfar's solution falls with resolution (the
+    reference's scoreboard: 18.0 m at 10 km, SIA included)."""
+    rmse = []
+    for res in (40e3, 20e3):
+        mesh, f, p = pkg.geometry.halfar_case(res=res)
+        A, Cw = pkg.mesh.voronoi_geometry(mesh)
+        _, e, n = pkg.geometry.halfar_run(_oracle_step(oracle_mod, mesh, A, Cw), mesh, f, p)
+        assert n == 50
+        rmse.append(e)
+    assert rmse[1] < 0.85 * rmse[0] and rmse[1] < 30.0, rmse
+
+
+@pytest.mark.gpu
+def test_gpu_halfar_dome_matches_oracle(pkg, oracle_mod, gpu_lib):
+    mesh, f, p = pkg.geometry.halfar_case(res=20e3)
+    A, Cw = pkg.mesh.voronoi_geometry(mesh)
+    Ho, eo, _ = pkg.geometry.halfar_run(_oracle_step(oracle_mod, mesh, A, Cw), mesh, f, p)
+    with pkg.VelocitySolver(mesh) as s:
+        s.voronoi_upload(A, Cw)
+        Hg, eg, n = pkg.geometry.halfar_run(s.calc_dHi_dt, mesh, f, p)
+    assert n == 50
+    # each step's semi-implicit solve stops at rtol 1e-8 on both sides (their reductions sum in
+    # different orders), so 50 steps agree to about that, not bitwise
+    assert abs(eg - eo) < 1e-4 * eo, (eg, eo)
+    assert np.linalg.norm(Hg - Ho) < 1e-6 * np.linalg.norm(Ho)

@@ -268,6 +268,67 @@ def thickness_case(seed=0, L=800e3, res=20e3, H0=3000.0, R=330e3, U0=400.0, nz=3
     return mesh, fields, params
 
 
+def halfar(x, y, t, A=1e-16, n=3.0, H0=3000.0, R0=500e3):
+    """Halfar's (1981, 1983) similarity solution of the isothermal shallow-ice dome on a flat bed,
+    in the form of Bueler et al. (2005, J. Glaciol. 51(173), eqs. 10-11): the thickness H and the
+    vertically averaged shallow-ice velocity u = -Gamma H^(n+1) |grad H|^(n-1) grad H,
+    Gamma = 2 A (rho g)^n / (n+2), at t years after the moment the dome has height H0 and radius
+    R0 (similarity time t0 + t).  Returns (H, u, v) at the points (x, y)."""
+    rho_g = 910.0 * 9.81
+    gam = 2.0 * A * rho_g ** n / (n + 2.0)
+    t0 = 1.0 / ((5.0 * n + 3.0) * gam) * ((2.0 * n + 1.0) / (n + 1.0)) ** n * R0 ** (n + 1.0) / H0 ** (2.0 * n + 1.0)
+    T = (t0 + t) / t0
+    alpha, beta = 2.0 / (5.0 * n + 3.0), 1.0 / (5.0 * n + 3.0)
+    p3, p4 = (n + 1.0) / n, n / (2.0 * n + 1.0)
+    x, y = np.asarray(x, float), np.asarray(y, float)
+    r = np.hypot(x, y)
+    s = np.minimum(T ** (-beta) * r / R0, 1.0)
+    f = 1.0 - s ** p3
+    H = H0 * T ** (-alpha) * np.where(f > 0.0, f, 0.0) ** p4
+    # dH/dr = H0 T^-alpha p4 f^(p4 - 1) (-p3 s^(p3 - 1)) T^-beta / R0 inside the dome
+    inside = (f > 0.0) & (r > 0.0)
+    dHdr = np.zeros_like(r)
+    fi = np.where(inside, f, 1.0)
+    dHdr[inside] = (H0 * T ** (-alpha) * p4 * fi[inside] ** (p4 - 1.0) * (-p3) * s[inside] ** (p3 - 1.0)
+                    * T ** (-beta) / R0)
+    speed = -gam * H ** (n + 1.0) * np.abs(dHdr) ** (n - 1.0) * dHdr   # radial, outward
+    rr = np.where(r > 0.0, r, 1.0)
+    return H, np.where(inside, speed * x / rr, 0.0), np.where(inside, speed * y / rr, 0.0)
+
+
+def halfar_case(res=20e3, seed=0, L=1000e3, nz=3, **kw):
+    """The reference's Halfar_dome integrated test (automated_testing/integrated_tests/idealised/
+    Halfar_dome/config_Halfar_*.cfg: H0 3000 m, R0 500 km, A 1e-16, n 3, a +-1000 km domain,
+    'zero' thickness borders, semi-implicit f_s 1.5, dt_ice_max 10 yr) for the thickness step
+    alone: the mesh, the thickness fields at t = 0 with Halfar's velocity, and the parameters."""
+    mesh = generate_mesh(-L, L, -L, L, lambda x, y: np.full(np.shape(x), float(res)), seed=seed, nz=nz)
+    H, _, _ = halfar(mesh.V[:, 0], mesh.V[:, 1], 0.0, **kw)
+    gc = np.asarray(mesh.TriGC)
+    _, u, v = halfar(gc[:, 0], gc[:, 1], 0.0, **kw)
+    fields = dict(Hi=np.ascontiguousarray(H), Hb=np.zeros(mesh.nV), SL=np.full(mesh.nV, -10000.0),
+                  u_vav_b=np.ascontiguousarray(u), v_vav_b=np.ascontiguousarray(v), dHi_dt=np.zeros(mesh.nV))
+    params = abi.default_thickness_params(dt_ice_max=10.0)
+    return mesh, fields, params
+
+
+def halfar_run(step, mesh, fields, params, years=500.0, dt=10.0, **kw):
+    """Step the thickness equation over `years` with Halfar's velocity at each step's start time;
+    step(params, fields, dt) -> dict (a calc_dHi_dt).  Returns (H at the end, RMSE against Halfar's
+    H there [m], steps)."""
+    gc = np.asarray(mesh.TriGC)
+    f = dict(fields)
+    t, n = 0.0, 0
+    while t < years - 1e-9:
+        _, u, v = halfar(gc[:, 0], gc[:, 1], t, **kw)
+        f["u_vav_b"], f["v_vav_b"] = np.ascontiguousarray(u), np.ascontiguousarray(v)
+        out = step(params, f, min(dt, years - t))
+        t += out["dt"]
+        f["Hi"], f["dHi_dt"] = out["Hi_tplusdt"], out["dHi_dt"]
+        n += 1
+    Ha, _, _ = halfar(mesh.V[:, 0], mesh.V[:, 1], t, **kw)
+    return f["Hi"], float(np.sqrt(np.mean((f["Hi"] - Ha) ** 2))), n
+
+
 def small_dome(seed=0, nz=12):
     """A ~1,000-vertex dome for tests the CPU oracle finishes in seconds."""
     return dome_case(seed=seed, nz=nz, res_scale=3.0)
