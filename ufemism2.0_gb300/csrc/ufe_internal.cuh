@@ -194,6 +194,8 @@ struct CsrSolveScratch {
   double *vec = nullptr;              // 10 x cap
   struct KrylovScalars *ks = nullptr, *hks = nullptr;   // device, pinned host
   int64_t cap = 0;
+  cudaGraphExec_t graph = nullptr;    // the whole solve with a device-side loop, for `key`
+  uint64_t key = 0;
 };
 void csr_scratch_alloc(CsrSolveScratch &scr, int64_t m);
 void csr_scratch_free(CsrSolveScratch &scr);

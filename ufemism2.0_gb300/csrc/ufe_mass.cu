@@ -37,6 +37,7 @@ struct MassWork {
   int64_t nnz = 0;
   double *A = nullptr, *Cw = nullptr;          // Voronoi areas, connection widths (nV x nC_mem)
   int2 *ct = nullptr;                           // triangles of each connection's edge (nV x nC_mem)
+  double *Dc = nullptr;                         // connection lengths D (nV x nC_mem), once per mesh
   int32_t *ptr = nullptr, *ind = nullptr;       // M_divQ pattern, 0-based
   double *valM = nullptr, *valA = nullptr;
   // inputs (nV unless noted)
@@ -81,15 +82,19 @@ __device__ __forceinline__ double thickness_from_surface(double Hb, double Hs, d
   return fmin(Hi_float, (Hs - SL) / (1.0 - (kIceDensityM / kSeawaterDensityM)));
 }
 
-// the triangles of the edge from vi to each neighbour: the ones among iTri(vi, :) holding vj
-__global__ void k_conn_tris(int nV, int nTri, int nC_mem, const int32_t *nC, const int32_t *C,
-                            const int32_t *niTri, const int32_t *iTri, const int32_t *Tri, int2 *ct) {
+// the triangles of the edge from vi to each neighbour (the ones among iTri(vi, :) holding vj),
+// and the connection length D = sqrt(D_x^2 + D_y^2) (mesh_secondary.f90:333-339)
+__global__ void k_conn_tris(int nV, int nTri, int nC_mem, const double *V, const int32_t *nC, const int32_t *C,
+                            const int32_t *niTri, const int32_t *iTri, const int32_t *Tri, int2 *ct, double *Dc) {
   const int vi = blockIdx.x * blockDim.x + threadIdx.x;
   if (vi >= nV) return;
   for (int ci = 0; ci < nC_mem; ++ci) {
     int2 r = make_int2(-1, -1);
+    double D = 0.0;
     if (ci < nC[vi]) {
       const int vj = C[(int64_t)ci * nV + vi] - 1;
+      const double Dx = V[vj] - V[vi], Dy = V[nV + vj] - V[nV + vi];
+      D = sqrt(Dx * Dx + Dy * Dy);
       for (int k = 0; k < niTri[vi]; ++k) {
         const int t = iTri[(int64_t)k * nV + vi] - 1;
         for (int q = 0; q < 3; ++q)
@@ -99,6 +104,7 @@ __global__ void k_conn_tris(int nV, int nTri, int nC_mem, const int32_t *nC, con
       }
     }
     ct[(int64_t)ci * nV + vi] = r;
+    Dc[(int64_t)ci * nV + vi] = D;
   }
 }
 
@@ -108,8 +114,10 @@ struct MeshRef {
   const int32_t *nC, *C, *VBI;
 };
 
-__global__ void k_divq_matrix(MeshRef m, const double *A, const double *Cw, const int2 *ct, const double *u,
-                              const double *v, const double *fm, const int32_t *ptr, double *val) {
+// The zero half of max(0, u_perp) / min(0, u_perp) is not divided: 0 / A_i is +0, and c0 + 0 is c0,
+// so skipping it leaves every value as the reference's expression gives it.
+__global__ void k_divq_matrix(MeshRef m, const double *A, const double *Cw, const int2 *ct, const double *Dc,
+                              const double *u, const double *v, const double *fm, const int32_t *ptr, double *val) {
   const int vi = blockIdx.x * blockDim.x + threadIdx.x;
   if (vi >= m.nV) return;
   const int nV = m.nV;
@@ -132,10 +140,10 @@ __global__ void k_divq_matrix(MeshRef m, const double *A, const double *Cw, cons
     }
     const double L_c = Cw[cix];
     const double Dx = m.V[vj] - xi, Dy = m.V[nV + vj] - yi;
-    const double D = sqrt(Dx * Dx + Dy * Dy);
+    const double D = Dc[cix];
     const double u_perp = uc * Dx / D + vc * Dy / D;
-    if (out_i) c0 = c0 + L_c * fmax(0.0, u_perp) / A_i;
-    val[k0 + 1 + ci] = (opt(fm, vj, 1.0) >= 1.0) ? L_c * fmin(0.0, u_perp) / A_i : 0.0;
+    if (out_i && u_perp > 0.0) c0 = c0 + L_c * u_perp / A_i;
+    val[k0 + 1 + ci] = (u_perp < 0.0 && opt(fm, vj, 1.0) >= 1.0) ? L_c * u_perp / A_i : 0.0;
   }
   val[k0] = c0;
 }
@@ -443,7 +451,7 @@ void prepare(ufe_ctx *ctx, MassWork *w, const ufe_thickness_params *p, const Inp
   cudaStream_t s = ctx->stream;
   const int nV = w->nV;
   const MeshRef m = mesh_ref(ctx);
-  k_divq_matrix<<<blocks(nV), 256, 0, s>>>(m, w->A, w->Cw, w->ct, w->u, w->v, in.fm, w->ptr, w->valM);
+  k_divq_matrix<<<blocks(nV), 256, 0, s>>>(m, w->A, w->Cw, w->ct, w->Dc, w->u, w->v, in.fm, w->ptr, w->valM);
   k_interior_neighbours<<<blocks(nV), 256, 0, s>>>(m, in.noice, w->nint);
   UFE_CUDA(cudaGetLastError());
   (void)p;
@@ -455,7 +463,7 @@ void free_mass(ufe_ctx *ctx) {
   MassWork *w = ctx->mass;
   if (!w) return;
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
-  void *ptrs[] = {w->A, w->Cw, w->ct, w->ptr, w->ind, w->valM, w->valA, w->Hi, w->Hb, w->SL, w->u, w->v,
+  void *ptrs[] = {w->A, w->Cw, w->ct, w->Dc, w->ptr, w->ind, w->valM, w->valA, w->Hi, w->Hb, w->SL, w->u, w->v,
                   w->SMB, w->BMB, w->LMB, w->fm, w->target, w->prHi, w->dprev, w->noice, w->prmask, w->dHdt,
                   w->Hit, w->divQ, w->AMB, w->dex, w->Hex, w->qex, w->aex, w->Hs, w->Hs_tot, w->bb, w->nint,
                   w->dt, w->dtlim, w->flag, w->stage, w->stagei};
@@ -497,6 +505,7 @@ extern "C" int32_t ufe_mesh_voronoi_upload(ufe_ctx *ctx, const double *A, const 
     w->A = alloc_n<double>(w->nV);
     w->Cw = alloc_n<double>(nc);
     w->ct = alloc_n<int2>(nc);
+    w->Dc = alloc_n<double>(nc);
     double *tmp = alloc_n<double>(nc);   // the caller's order, then gathered into the internal one
     UFE_CUDA(cudaMemcpyAsync(tmp, A, sizeof(double) * w->nV, cudaMemcpyHostToDevice, s));
     k_permute<double><<<blocks(w->nV), 256, 0, s>>>(w->nV, 1, tmp, ctx->perm_v, w->A);
@@ -505,8 +514,8 @@ extern "C" int32_t ufe_mesh_voronoi_upload(ufe_ctx *ctx, const double *A, const 
     k_permute<double><<<blocks((int64_t)nc), 256, 0, s>>>(w->nV, w->nC_mem, tmp, ctx->perm_v, w->Cw);
     UFE_CUDA(cudaStreamSynchronize(s));
     dev_free(tmp);
-    k_conn_tris<<<blocks(w->nV), 256, 0, s>>>(w->nV, w->nTri, w->nC_mem, ctx->nC, ctx->C, ctx->niTri, ctx->iTri,
-                                              ctx->Tri, w->ct);
+    k_conn_tris<<<blocks(w->nV), 256, 0, s>>>(w->nV, w->nTri, w->nC_mem, ctx->V, ctx->nC, ctx->C, ctx->niTri,
+                                              ctx->iTri, ctx->Tri, w->ct, w->Dc);
     UFE_CUDA(cudaGetLastError());
     // M_divQ's pattern: row vi = [vi, C(vi, 1:nC)] (calc_ice_flux_divergence_matrix_upwind's add_entry order)
     std::vector<int32_t> nC(w->nV), C(nc);

@@ -2962,6 +2962,12 @@ extern "C" int32_t ufe_profile_krylov_kernels(ufe_ctx *ctx, int32_t precision, i
 
 // General CSR matrix-equation solve (solve_matrix_equation_CSR_PETSc): same BiCGStab kernels on
 // scalar rows, host-checked every few iterations.
+static uint64_t bits_of_double(double d) {
+  uint64_t u;
+  memcpy(&u, &d, sizeof(u));
+  return u;
+}
+
 // inverse diagonal of a CSR matrix: the row's diagonal entries summed in storage order
 __global__ void k_csr_dinv(int m, const int32_t *ptr, const int32_t *ind, const double *val, double *dinv) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -2980,6 +2986,7 @@ void csr_scratch_alloc(CsrSolveScratch &scr, int64_t m) {
 }
 
 void csr_scratch_free(CsrSolveScratch &scr) {
+  if (scr.graph) cudaGraphExecDestroy(scr.graph);
   dev_free(scr.vec);
   dev_free(scr.ks);
   if (scr.hks) cudaFreeHost(scr.hks);
@@ -3001,6 +3008,59 @@ int32_t solve_csr_device(ufe_ctx *ctx, const DevCSR &A, const double *b, double 
   try {
     double *dinv = vec, *R = vec + m, *RP = R + m, *S = RP + m, *T = S + m, *P0 = T + m, *P1 = P0 + m,
            *V0 = P1 + m, *V1 = V0 + m;
+    if (!owned) {
+      // a caller that solves repeatedly on the same buffers: the whole solve as one graph, its
+      // iteration loop a conditional while-node that k_xr keeps open (built once per buffers,
+      // sizes and tolerances; the host waits once, at the end)
+      uint64_t key = 1469598103934665603ull;
+      const uint64_t parts[] = {(uint64_t)(uintptr_t)A.ptr, (uint64_t)(uintptr_t)A.ind, (uint64_t)(uintptr_t)A.val,
+                                (uint64_t)(uintptr_t)b, (uint64_t)(uintptr_t)x, (uint64_t)m, (uint64_t)A.nnz,
+                                (uint64_t)bits_of_double(rtol), (uint64_t)bits_of_double(abstol),
+                                (uint64_t)max_it};
+      for (uint64_t q : parts) { key ^= q; key *= 1099511628211ull; }
+      if (!scr.graph || scr.key != key) {
+        if (scr.graph) { cudaGraphExecDestroy(scr.graph); scr.graph = nullptr; }
+        cudaGraph_t g;
+        UFE_CUDA(cudaGraphCreate(&g, 0));
+        try {
+          cudaGraphConditionalHandle h;
+          UFE_CUDA(cudaGraphConditionalHandleCreate(&h, g, 0, 0));
+          const CondArg cond{h, 1};
+          CsrMat mat{m, A.ptr, A.ind, A.val};
+          KV<double> v;
+          v.X = x; v.R = R; v.RP = RP; v.S = S; v.T = T; v.B = const_cast<double *>(b); v.dinv = dinv;
+          v.P[0] = P0; v.P[1] = P1; v.V[0] = V0; v.V[1] = V1;
+          const int grid = max_grid(ctx);
+          const unsigned gk = krylov_grid(mat, kThreads, grid);
+          auto deps = capture_into(s, g, {}, [&]() {
+            k_csr_dinv<<<(unsigned)((m + 255) / 256), 256, 0, s>>>(m, A.ptr, A.ind, A.val, dinv);
+            UFE_CUDA(cudaMemsetAsync(ks, 0, sizeof(KrylovScalars), s));
+            k_krylov_init<CsrMat><<<gk, kThreads, 0, s>>>(mat, v, ks, rtol, abstol, max_it, 0, ctx->red.partials,
+                                                          ctx->red.tickets, cond);
+            UFE_CUDA(cudaGetLastError());
+          });
+          cudaGraph_t body;
+          add_while(g, deps, h, &body);
+          capture_into(s, body, {}, [&]() {
+            k_p_spmv<CsrMat><<<gk, kThreads, 0, s>>>(mat, v, ks, ctx->red.partials, ctx->red.tickets);
+            k_s_spmv<CsrMat><<<gk, kThreads, 0, s>>>(mat, v, ks, ctx->red.partials, ctx->red.tickets);
+            k_xr<CsrMat><<<gk, kThreads, 0, s>>>(mat, v, ks, ctx->red.partials, ctx->red.tickets, cond);
+            UFE_CUDA(cudaGetLastError());
+          });
+          UFE_CUDA(cudaGraphInstantiate(&scr.graph, g, 0));
+        } catch (...) {
+          cudaGraphDestroy(g);
+          throw;
+        }
+        UFE_CUDA(cudaGraphDestroy(g));
+        scr.key = key;
+      }
+      UFE_CUDA(cudaGraphLaunch(scr.graph, s));
+      UFE_CUDA(cudaMemcpyAsync(hks, ks, sizeof(KrylovScalars), cudaMemcpyDeviceToHost, s));
+      UFE_CUDA(cudaStreamSynchronize(s));
+      *its = hks->it;
+      return hks->status;
+    }
     // Jacobi diagonal (PCJACOBI: 1 where the diagonal is zero)
     k_csr_dinv<<<(unsigned)((m + 255) / 256), 256, 0, s>>>(m, A.ptr, A.ind, A.val, dinv);
     UFE_CUDA(cudaMemsetAsync(ks, 0, sizeof(KrylovScalars), s));
