@@ -158,11 +158,12 @@ typedef struct {
                                              below krylov_forcing x its initial residual (the residual of
                                              the current Picard iterate), so iterations far from the fixed
                                              point are not solved to full accuracy.  When the change norm
-                                             first meets visc_it_norm_dUV_tol, phase 2 begins: solves to
-                                             the full Krylov tolerance, until the change norm meets the
-                                             tolerance again -- a small step from a loosely solved system
-                                             never ends the solve.  0 (default) = the fixed tolerance only,
-                                             as the reference's PETSc call; otherwise in (0, 1)            */
+                                             has met visc_it_norm_dUV_tol in two such iterations in a row,
+                                             the next solve runs to the full Krylov tolerance: if the change
+                                             norm then meets the tolerance the solve ends, otherwise phase 1
+                                             resumes -- a small step from a loosely solved system never
+                                             ends the solve.  0 (default) = the fixed tolerance only, as the
+                                             reference's PETSc call; otherwise in (0, 1)                   */
   /* calc_ice_rheology_Glen (constitutive_equation.f90:84-163), model_configuration.f90:594-601 */
   int32_t choice_ice_rheology_Glen;       /* enum ufe_rheology, default UFE_RHEOLOGY_INPUT                  */
   int32_t choice_enhancement_factor_transition; /* enum ufe_enhancement, default UFE_ENH_SEPARATE          */

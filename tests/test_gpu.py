@@ -360,8 +360,9 @@ def test_diva_matches_oracle_gpu_operators(pkg, oracle_mod, gpu_lib, sliding):
 @pytest.mark.parametrize("prec", [0, 2])
 def test_inexact_picard_meets_tolerance_with_exact_final_solves(pkg, gpu_lib, prec):
     """krylov_forcing > 0: forced (loose) linear solves until the change norm has met the Picard
-    tolerance twice in a row, then solves to the full Krylov tolerance until it meets it again.
-    The result lies as close to the converged fixed point as the plain iteration's at the same
+    tolerance twice in a row, then one solve to the full Krylov tolerance, which ends the solve if
+    the change norm meets the tolerance again (and otherwise hands back to forced solves).  The
+    result lies as close to the converged fixed point as the plain iteration's at the same
     tolerance, with fewer Krylov iterations in all."""
     mesh, ice, params = pkg.geometry.small_dome(seed=1)
     base = {k: getattr(params, k) for k, _ in params._fields_ if k != "reserved"}

@@ -760,13 +760,19 @@ __device__ void picard_step(PicardScalars *psp, KrylovScalars *ks, double r1, do
   if (isnan(p.L2)) { p.status = UFE_ERR_NAN; stop = 1; }
   int converged = p.L2 < q.picard_tol;
   // inexact Picard: once the change norm has met the tolerance in two forced iterations in a row
-  // (one tiny step from a loosely solved system does not count), the forced linear solves end and
-  // the iteration goes on with solves to the full Krylov tolerance, until the change norm meets
-  // the tolerance after such a solve
-  if (!stop && q.inexact && p.phase == 0) {
-    p.nconv0 = converged ? p.nconv0 + 1 : 0;
-    if (converged && p.nconv0 >= 2) p.phase = 1;
-    converged = 0;
+  // (one tiny step from a loosely solved system does not count), the next linear solve runs to
+  // the full Krylov tolerance; the iteration stops when the change norm meets the tolerance after
+  // such a solve, and otherwise goes back to forced solves (a good start makes forced steps small
+  // long before the iterate has converged, so the check is repeated rather than made the rule)
+  if (!stop && q.inexact) {
+    if (p.phase == 0) {
+      p.nconv0 = converged ? p.nconv0 + 1 : 0;
+      if (converged && p.nconv0 >= 2) p.phase = 1;
+      converged = 0;
+    } else if (!converged) {
+      p.phase = 0;
+      p.nconv0 = 0;
+    }
   }
   if (!stop && !converged && p.it > q.visc_it_nit) {
     if (p.status == UFE_OK) p.status = UFE_WARN_PICARD_MAXIT;
