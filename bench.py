@@ -756,7 +756,10 @@ def run_thickness(args):
                                     "SIA solve instead"},
             "cpu_baseline": cpu,
             "clocks": clocks.summary(),
-            "gpu_launches": int(args.steps * (12 + 1 + 3 * 8 * int(np.ceil(mean_its / 8)))),
+            # per step: 14 input gathers, matrix + neighbour counts (2), explicit pass and system
+            # rows (10), the solve graph (Jacobi, init, 3 per Krylov iteration), 2 finishing
+            # kernels, 4 output gathers
+            "gpu_launches": int(round(args.steps * (34 + 3 * mean_its))),
             "wall_s_timed": round(wall, 3),
         }
         print(json.dumps(line))
