@@ -157,20 +157,37 @@ __device__ __forceinline__ double mass_balance(const Inputs &in, int vi) {
   return opt(in.fm, vi, 1.0) * (opt(in.SMB, vi, 0.0) + opt(in.BMB, vi, 0.0) - opt(in.target, vi, 0.0));
 }
 
-// divQ, dH/dt (= AMB before the limits) and the time-step limit of every thinning vertex
-__global__ void k_rate(int nV, const int32_t *ptr, const int32_t *ind, const double *val, Inputs in, double Hi_min,
-                       double *divQ, double *dHdt, double *AMB, unsigned long long *dtlim) {
+// divQ, dH/dt (= AMB before the limits) and the time-step limit of every thinning vertex; the
+// limits' minimum per block first (one atomic per block: contended per-vertex atomics on one
+// address serialise), on the bit patterns, which order non-negative doubles as their values
+__global__ void __launch_bounds__(256) k_rate(int nV, const int32_t *ptr, const int32_t *ind, const double *val,
+                                              Inputs in, double Hi_min, double *divQ, double *dHdt, double *AMB,
+                                              unsigned long long *dtlim) {
   const int vi = blockIdx.x * blockDim.x + threadIdx.x;
-  if (vi >= nV) return;
-  double q = 0.0;
-  for (int32_t k = ptr[vi]; k < ptr[vi + 1]; ++k) q = q + val[k] * in.Hi[ind[k]];
-  divQ[vi] = q;
-  const double r = -q + mass_balance(in, vi) + opt(in.LMB, vi, 0.0);
-  dHdt[vi] = r;
-  AMB[vi] = r;
-  if (in.Hi[vi] > Hi_min && r < 0.0) {
-    const double lim = in.Hi[vi] / fmax(r, 1e-9);   // as written: a thinning rate gives Hi / 1e-9
-    atomicMin(dtlim, (unsigned long long)__double_as_longlong(lim));
+  unsigned long long lim_bits = ~0ull;
+  if (vi < nV) {
+    double q = 0.0;
+    for (int32_t k = ptr[vi]; k < ptr[vi + 1]; ++k) q = q + val[k] * in.Hi[ind[k]];
+    divQ[vi] = q;
+    const double r = -q + mass_balance(in, vi) + opt(in.LMB, vi, 0.0);
+    dHdt[vi] = r;
+    AMB[vi] = r;
+    if (in.Hi[vi] > Hi_min && r < 0.0) {
+      const double lim = in.Hi[vi] / fmax(r, 1e-9);   // as written: a thinning rate gives Hi / 1e-9
+      lim_bits = (unsigned long long)__double_as_longlong(lim);
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long other = __shfl_xor_sync(0xffffffffu, lim_bits, o);
+    lim_bits = other < lim_bits ? other : lim_bits;
+  }
+  __shared__ unsigned long long wmin[8];
+  if ((threadIdx.x & 31) == 0) wmin[threadIdx.x >> 5] = lim_bits;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned long long b = wmin[0];
+    for (int w = 1; w < (int)(blockDim.x >> 5); ++w) b = wmin[w] < b ? wmin[w] : b;
+    if (b != ~0ull) atomicMin(dtlim, b);
   }
 }
 

@@ -3014,7 +3014,8 @@ int32_t solve_csr_device(ufe_ctx *ctx, const DevCSR &A, const double *b, double 
   try {
     double *dinv = vec, *R = vec + m, *RP = R + m, *S = RP + m, *T = S + m, *P0 = T + m, *P1 = P0 + m,
            *V0 = P1 + m, *V1 = V0 + m;
-    if (!owned) {
+    const char *ng = getenv("UFE_NO_GRAPH");
+    if (!owned && !(ng && *ng && *ng != '0')) {
       // a caller that solves repeatedly on the same buffers: the whole solve as one graph, its
       // iteration loop a conditional while-node that k_xr keeps open (built once per buffers,
       // sizes and tolerances; the host waits once, at the end)
@@ -3032,25 +3033,25 @@ int32_t solve_csr_device(ufe_ctx *ctx, const DevCSR &A, const double *b, double 
           cudaGraphConditionalHandle h;
           UFE_CUDA(cudaGraphConditionalHandleCreate(&h, g, 0, 0));
           const CondArg cond{h, 1};
-          CsrMat mat{m, A.ptr, A.ind, A.val};
+          using M4 = CsrMatL<4>;
+          M4 mat{m, A.ptr, A.ind, A.val};
           KV<double> v;
           v.X = x; v.R = R; v.RP = RP; v.S = S; v.T = T; v.B = const_cast<double *>(b); v.dinv = dinv;
           v.P[0] = P0; v.P[1] = P1; v.V[0] = V0; v.V[1] = V1;
-          const int grid = max_grid(ctx);
-          const unsigned gk = krylov_grid(mat, kThreads, grid);
+          const unsigned gk = krylov_grid(mat, kThreads, kMaxReduceBlocks);
           auto deps = capture_into(s, g, {}, [&]() {
             k_csr_dinv<<<(unsigned)((m + 255) / 256), 256, 0, s>>>(m, A.ptr, A.ind, A.val, dinv);
             UFE_CUDA(cudaMemsetAsync(ks, 0, sizeof(KrylovScalars), s));
-            k_krylov_init<CsrMat><<<gk, kThreads, 0, s>>>(mat, v, ks, rtol, abstol, max_it, 0, ctx->red.partials,
-                                                          ctx->red.tickets, cond);
+            k_krylov_init<M4><<<gk, kThreads, 0, s>>>(mat, v, ks, rtol, abstol, max_it, 0, ctx->red.partials,
+                                                      ctx->red.tickets, cond);
             UFE_CUDA(cudaGetLastError());
           });
           cudaGraph_t body;
           add_while(g, deps, h, &body);
           capture_into(s, body, {}, [&]() {
-            k_p_spmv<CsrMat><<<gk, kThreads, 0, s>>>(mat, v, ks, ctx->red.partials, ctx->red.tickets);
-            k_s_spmv<CsrMat><<<gk, kThreads, 0, s>>>(mat, v, ks, ctx->red.partials, ctx->red.tickets);
-            k_xr<CsrMat><<<gk, kThreads, 0, s>>>(mat, v, ks, ctx->red.partials, ctx->red.tickets, cond);
+            k_p_spmv<M4><<<gk, kThreads, 0, s>>>(mat, v, ks, ctx->red.partials, ctx->red.tickets);
+            k_s_spmv<M4><<<gk, kThreads, 0, s>>>(mat, v, ks, ctx->red.partials, ctx->red.tickets);
+            k_xr<M4><<<gk, kThreads, 0, s>>>(mat, v, ks, ctx->red.partials, ctx->red.tickets, cond);
             UFE_CUDA(cudaGetLastError());
           });
           UFE_CUDA(cudaGraphInstantiate(&scr.graph, g, 0));
