@@ -229,26 +229,6 @@ struct CsrMat {
   }
 };
 
-// A scalar CSR matrix read by L lanes per row (entries strided over the lanes, summed by
-// lane_reduce): the column and value loads of neighbouring lanes coalesce and L entries of a row
-// are in flight at once -- for the short rows (about 7 entries) of a vertex-graph matrix.
-template <int L>
-struct CsrMatL {
-  using Vec = double;
-  static constexpr int kLanes = L;
-  int32_t items;
-  const int32_t *__restrict__ ptr;
-  const int32_t *__restrict__ col;
-  const double *__restrict__ val;
-  template <class G>
-  __device__ __forceinline__ double row_partial(int i, int lane, G get) const {
-    double y = 0.0;
-    const int k2 = __ldg(ptr + i + 1);
-    for (int k = __ldg(ptr + i) + lane; k < k2; k += L) y = fma(__ldg(val + k), get(__ldg(col + k)), y);
-    return y;
-  }
-};
-
 template <class Vec>
 struct KV {
   Vec *X, *R, *RP, *S, *T, *B;

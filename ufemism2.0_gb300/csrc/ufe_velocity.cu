@@ -3033,25 +3033,25 @@ int32_t solve_csr_device(ufe_ctx *ctx, const DevCSR &A, const double *b, double 
           cudaGraphConditionalHandle h;
           UFE_CUDA(cudaGraphConditionalHandleCreate(&h, g, 0, 0));
           const CondArg cond{h, 1};
-          using M4 = CsrMatL<4>;
-          M4 mat{m, A.ptr, A.ind, A.val};
+          using M1 = CsrMat;
+          M1 mat{m, A.ptr, A.ind, A.val};
           KV<double> v;
           v.X = x; v.R = R; v.RP = RP; v.S = S; v.T = T; v.B = const_cast<double *>(b); v.dinv = dinv;
           v.P[0] = P0; v.P[1] = P1; v.V[0] = V0; v.V[1] = V1;
-          const unsigned gk = krylov_grid(mat, kThreads, kMaxReduceBlocks);
+          const unsigned gk = krylov_grid(mat, kThreads, max_grid(ctx));
           auto deps = capture_into(s, g, {}, [&]() {
             k_csr_dinv<<<(unsigned)((m + 255) / 256), 256, 0, s>>>(m, A.ptr, A.ind, A.val, dinv);
             UFE_CUDA(cudaMemsetAsync(ks, 0, sizeof(KrylovScalars), s));
-            k_krylov_init<M4><<<gk, kThreads, 0, s>>>(mat, v, ks, rtol, abstol, max_it, 0, ctx->red.partials,
+            k_krylov_init<M1><<<gk, kThreads, 0, s>>>(mat, v, ks, rtol, abstol, max_it, 0, ctx->red.partials,
                                                       ctx->red.tickets, cond);
             UFE_CUDA(cudaGetLastError());
           });
           cudaGraph_t body;
           add_while(g, deps, h, &body);
           capture_into(s, body, {}, [&]() {
-            k_p_spmv<M4><<<gk, kThreads, 0, s>>>(mat, v, ks, ctx->red.partials, ctx->red.tickets);
-            k_s_spmv<M4><<<gk, kThreads, 0, s>>>(mat, v, ks, ctx->red.partials, ctx->red.tickets);
-            k_xr<M4><<<gk, kThreads, 0, s>>>(mat, v, ks, ctx->red.partials, ctx->red.tickets, cond);
+            k_p_spmv<M1><<<gk, kThreads, 0, s>>>(mat, v, ks, ctx->red.partials, ctx->red.tickets);
+            k_s_spmv<M1><<<gk, kThreads, 0, s>>>(mat, v, ks, ctx->red.partials, ctx->red.tickets);
+            k_xr<M1><<<gk, kThreads, 0, s>>>(mat, v, ks, ctx->red.partials, ctx->red.tickets, cond);
             UFE_CUDA(cudaGetLastError());
           });
           UFE_CUDA(cudaGraphInstantiate(&scr.graph, g, 0));
