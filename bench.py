@@ -771,7 +771,8 @@ LEARNED_WORKLOAD = ("learned Picard start, SSA ensemble: 30k-vertex mesh over 15
 
 
 def run_learned(args):
-    """Config 3: data from plain FP64 GPU solves, GPU training, held-out solves from the learned start."""
+    """The learned start on the 30k-vertex SSA ensemble: data from plain FP64 GPU solves, GPU training,
+    held-out solves from the learned start."""
     import torch
 
     rank, world, local = dist_env()
@@ -875,7 +876,7 @@ def run_learned(args):
     print(json.dumps(line))
 
 
-DOME_WORKLOAD = ("config 0: SSA on the radially symmetric dome, 800 km square, ~8,500 vertices (10 km at the "
+DOME_WORKLOAD = ("SSA on the radially symmetric dome, 800 km square, ~8,500 vertices (10 km at the "
                  "margin, 40 km inside), Weertman m=3, BiCGStab/Jacobi 1e-8; Picard 1e-4 and a tight tolerance")
 # dome variants the learned start trains on: (H0 [m], R [m], beta^2), each on its own mesh
 DOME_VARIANTS = [(2600.0, 460e3, 7e3), (2800.0, 480e3, 1.3e4), (3200.0, 520e3, 8e3), (3400.0, 540e3, 1.2e4),
@@ -883,7 +884,7 @@ DOME_VARIANTS = [(2600.0, 460e3, 7e3), (2800.0, 480e3, 1.3e4), (3200.0, 520e3, 8
 
 
 def run_dome(args):
-    """Config 0 at full size: the GPU FP64 path against the oracle's own solve (the parity check at
+    """The ~8,500-vertex SSA dome: the GPU FP64 path against the oracle's own solve (the parity check at
     size), and the accuracy target where the reference's Picard iteration converges tightly: plain
     FP64 against learned start + double-word Krylov, both at the benchmark tolerance and at a tight
     one, with every velocity error measured against a tightly converged FP64 solution."""
@@ -1271,7 +1272,7 @@ def run_mixed(args):
 
 
 def run_mixed_sequential(args, pkg, built, p, gen_s, rank, world, local, train=()):
-    """Config 4 member by member: each member's solve has the whole GPU, so it runs with the
+    """The mixed-size DIVA ensemble member by member: each member's solve has the whole GPU, so it runs with the
     persistent Krylov kernels (members side by side cannot: a persistent kernel needs every SM).
     Three paths per member, each solved once (the device time of a solve excludes its graph
     capture): plain FP64 -- the reference's algorithm --, double-word Krylov inside the inexact
@@ -1457,7 +1458,7 @@ def accuracy_summary(plain, learned, ref_info, head_name, u_plain, err_ref):
     parts.append(f"Tighter Picard tolerances ({failed}) end in the reference's divergence stop on this channel, "
                  f"and on the way its divergence control raises eps0^2 (relaxation {ref_info['relax_applied']} "
                  f"applied to reach {T:g}), which changes the viscosity law itself; so the solutions that different "
-                 f"starts reach differ by ~1e-2 even at {T:g}.  The dome (config 0, --workload dome) converges "
+                 f"starts reach differ by ~1e-2 even at {T:g}.  The dome (--workload dome) converges "
                  f"without such steps and is where the 1e-6 target is measured.")
     out["statement"] = " ".join(parts)
     return out
@@ -1620,10 +1621,10 @@ def main():
     ap.add_argument("--picard-nit", type=int, default=200,
                     help="visc_it_nit of every channel path (a limit only: the tolerance ends the solves)")
     ap.add_argument("--mixed-train", type=int, default=12,
-                    help="config 4: training geometries of the learned start (20k-60k vertices; 0: no learned path)")
+                    help="mixed-size ensemble: training geometries of the learned start (20k-60k vertices; 0: no learned path)")
     ap.add_argument("--mixed-epochs", type=int, default=60)
     ap.add_argument("--mixed-mode", choices=["sequential", "side_by_side"], default="sequential",
-                    help="config 4: members one after another with the persistent kernels, or side by side")
+                    help="mixed-size ensemble: members one after another with the persistent kernels, or side by side")
     ap.add_argument("--ref-tols", type=float, nargs="+", default=[1e-10, 1e-9, 1e-8, 1e-7, 1e-6],
                     help="Picard tolerances tried, tightest first, for the FP64 reference solution")
     ap.add_argument("--ref-sample-picard", type=int, default=4,

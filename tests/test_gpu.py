@@ -303,13 +303,13 @@ def test_no_grounded_ice_zero_velocity(pkg, dome, gpu_golden_ops):
 # ---- the benchmark configurations at full size ------------------------------------------------
 @pytest.fixture(scope="module")
 def dome_full(pkg, oracle_mod):
-    """Config 0: the ~8,000-vertex dome, with the oracle's operators and the GPU's."""
+    """The ~8,500-vertex SSA dome, with the oracle's operators and the GPU's."""
     mesh, ice, params = pkg.geometry.dome_case(seed=0)
     return mesh, ice, params, oracle_mod.Oracle(mesh)
 
 
 def test_dome_stiffness_structure_bitexact_gpu_operators(pkg, dome_full, gpu_lib):
-    """The stiffness matrix of config 0 assembled from GPU-built operators: integer CSR structure
+    """The stiffness matrix of the 8,500-vertex SSA dome assembled from GPU-built operators: integer CSR structure
     identical to the oracle's, values within the operators' 1e-11 agreement."""
     mesh, ice, params, orc = dome_full
     rng = np.random.default_rng(11)
@@ -325,7 +325,7 @@ def test_dome_stiffness_structure_bitexact_gpu_operators(pkg, dome_full, gpu_lib
 
 
 def test_dome_ssa_matches_oracle_gpu_operators(pkg, dome_full, gpu_lib):
-    """Config 0 solved on the GPU with its own operators against the oracle: the same Picard
+    """The ~8,500-vertex SSA dome solved on the GPU with its own operators against the oracle: the same Picard
     iteration count and velocities within 1e-8 (Krylov to 1e-12)."""
     mesh, ice, params, orc = dome_full
     p = pkg.abi.default_params(**{k: getattr(params, k) for k, _ in params._fields_ if k != "reserved"})

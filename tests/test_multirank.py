@@ -15,7 +15,7 @@ def _free_port():
 
 def test_partition_balances_and_covers(pkg):
     rng = np.random.default_rng(3)
-    costs = np.exp(rng.uniform(np.log(2e4), np.log(4e5), 64))   # config-4-like member sizes
+    costs = np.exp(rng.uniform(np.log(2e4), np.log(4e5), 64))   # member sizes log-uniform in [20k, 400k]
     for world in (1, 2, 3, 4, 8):
         parts = pkg.ensemble.partition_members(costs, world)
         flat = sorted(i for p in parts for i in p)

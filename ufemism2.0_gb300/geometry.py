@@ -67,7 +67,7 @@ def thickness_above_flotation(Hi, Hb, SL):
     return Hi - np.maximum(0.0, SL - Hb) * (SEAWATER_DENSITY / ICE_DENSITY)
 
 
-# -- config 0: SSA dome ------------------------------------------------------------------------
+# -- SSA dome (~8,500 vertices) -----------------------------------------------------------------
 def dome_thickness(x, y, H0=3000.0, R=500e3):
     r = np.hypot(x, y)
     s = np.clip(1.0 - (r / R) ** (4.0 / 3.0), 0.0, None)
@@ -82,7 +82,7 @@ def dome_resolution(band=140e3, ramp=200e3, fine=10e3, coarse=40e3, R=500e3):
 
 
 def dome_case(seed=0, nz=12, L=800e3, res_scale=1.0, A=1e-16, beta_sq=1e4, H0=3000.0, R=500e3):
-    """Config 0 (or a coarser copy with res_scale > 1 for quick tests; H0, R and beta_sq vary it
+    """The SSA dome, ~8,500 vertices (or a coarser copy with res_scale > 1 for quick tests; H0, R and beta_sq vary it
     for the learned start's training set)."""
     res = dome_resolution(band=140e3 * min(res_scale, 1.0) if res_scale < 1 else 140e3,
                           fine=10e3 * res_scale, coarse=40e3 * res_scale, R=R)
@@ -104,7 +104,7 @@ def dome_case(seed=0, nz=12, L=800e3, res_scale=1.0, A=1e-16, beta_sq=1e4, H0=30
     return mesh, ice, params
 
 
-# -- config 1: DIVA channel --------------------------------------------------------------------
+# -- DIVA channel (~58k vertices) ---------------------------------------------------------------
 def mismip_bed(x, y):
     """calc_idealised_geometry_MISMIPplus bed (idealised_geometries.f90:357-401)."""
     B0, B2, B4, B6 = -150.0, -728.8, 343.91, -50.57
@@ -123,7 +123,7 @@ def channel_resolution(H=250.0, fine=0.9e3, coarse=1.35e3, taf_band=120.0):
 
 
 def channel_case(seed=0, nz=12, H=250.0, A=2e-17, res_scale=1.0, sliding="Schoof2005"):
-    """Config 1 (or a coarser copy with res_scale > 1)."""
+    """The DIVA channel, ~58k vertices (or a coarser copy with res_scale > 1)."""
     res = channel_resolution(H=H, fine=0.9e3 * res_scale, coarse=1.35e3 * res_scale)
     mesh = generate_mesh(0.0, 640e3, -40e3, 40e3, res, seed=seed, nz=nz)
     x, y = mesh.V[:, 0], mesh.V[:, 1]
@@ -501,7 +501,7 @@ def random_columns(nV, nz, seed=0, stiff_frac=0.0, stiffness=300.0):
     return zeta, {k: (np.asfortranarray(v) if isinstance(v, np.ndarray) else v) for k, v in cols.items()}
 
 
-# ---- learned-start ensemble (config 3) --------------------------------------------------------
+# ---- learned-start SSA ensemble (30k-vertex mesh) ---------------------------------------------
 def grounded_fraction_b_vertex(mesh, taf, nsub=6):
     """grounded_fraction_b with the thickness above flotation given at vertices (linear within
     each triangle)."""
@@ -560,7 +560,7 @@ def ensemble_mesh(nV=30_000, L=1500e3, seed=0, nz=12, R=600e3):
 def ensemble_member(mesh, member, A=1e-16, H0=3000.0, R=600e3, bed_sigma=400.0, bed_corr=20e3,
                     beta_mu=np.log(1e4), beta_sigma=0.5, beta_corr=50e3):
     """Geometry `member` of the learned-start ensemble on `mesh`: bed -200 m plus a Gaussian random
-    field (sigma 400 m, correlation 20 km, seeded by the member), the dome thickness of config 0
+    field (sigma 400 m, correlation 20 km, seeded by the member), the dome thickness of the SSA dome case
     with R = 600 km, floating where the ice is thinner than flotation (sea level 0), and a
     log-normal friction coefficient beta^2 (log-mean ln 1e4, log-sd 0.5, correlation 50 km).
     Returns (ice, params) for an SSA solve (Weertman m = 3, n = 3, A = 1e-16, Picard 1e-4,
