@@ -757,9 +757,9 @@ def run_thickness(args):
             "cpu_baseline": cpu,
             "clocks": clocks.summary(),
             # per step: 14 input gathers, matrix + neighbour counts (2), explicit pass and system
-            # rows (10), the solve graph (Jacobi, init, 3 per Krylov iteration), 2 finishing
+            # rows (10), the solve graph (Jacobi, init, 5 per Krylov iteration), 2 finishing
             # kernels, 4 output gathers
-            "gpu_launches": int(round(args.steps * (34 + 3 * mean_its))),
+            "gpu_launches": int(round(args.steps * (34 + 5 * mean_its))),
             "wall_s_timed": round(wall, 3),
         }
         print(json.dumps(line))

@@ -332,9 +332,13 @@ __global__ void k_krylov_init(M mat, KV<typename M::Vec> v, KrylovScalars *ks, d
   }
 }
 
+// pre = 1: p (and, in k_s_spmv, s) were formed row by row beforehand (k_p_update, k_s_update) and
+// the SpMV gathers them; pre = 0 forms them on the fly for every gathered column.  Both give the
+// same values -- the same expression on the same inputs -- but the on-the-fly form repeats the
+// update's FP64 work once per stored entry, which bounds a scalar CSR solve by the FP64 pipe.
 template <class M>
 __global__ void k_p_spmv(M mat, KV<typename M::Vec> v, KrylovScalars *ks, double *partials,
-                         unsigned int *tickets) {
+                         unsigned int *tickets, int pre = 0) {
   using Vec = typename M::Vec;
   using R = typename ScalarOf<Vec>::T;
   const KrylovScalars s = *ks;
@@ -344,15 +348,17 @@ __global__ void k_p_spmv(M mat, KV<typename M::Vec> v, KrylovScalars *ks, double
   const Vec *__restrict__ Po = v.P[cur];
   const Vec *__restrict__ Vo = v.V[cur];
   const Vec *__restrict__ Rr = v.R;
+  const Vec *__restrict__ Pn = v.P[nxt];
   double acc[1] = {0.0};
   KRYLOV_ROWS(M, i, lane) {
     const int i = (int)i_64;
     const bool live = i < mat.items;
-    Vec part = live ? mat.row_partial(i, lane, [&](int j) { return v_pupd(Rr[j], bw, Vo[j], beta, Po[j]); })
-                    : v_zero<Vec>();
+    Vec part = !live ? v_zero<Vec>()
+               : pre ? mat.row_partial(i, lane, [&](int j) { return Pn[j]; })
+                     : mat.row_partial(i, lane, [&](int j) { return v_pupd(Rr[j], bw, Vo[j], beta, Po[j]); });
     Vec y = lane_reduce<M::kLanes>(part);
     if (live && lane == 0) {
-      v.P[nxt][i] = v_pupd(Rr[i], bw, Vo[i], beta, Po[i]);
+      if (!pre) v.P[nxt][i] = v_pupd(Rr[i], bw, Vo[i], beta, Po[i]);
       Vec vn = v_mul(v.dinv[i], y);
       v.V[nxt][i] = vn;
       acc[0] += v_dot(vn, v.RP[i]);
@@ -370,7 +376,7 @@ __global__ void k_p_spmv(M mat, KV<typename M::Vec> v, KrylovScalars *ks, double
 
 template <class M>
 __global__ void k_s_spmv(M mat, KV<typename M::Vec> v, KrylovScalars *ks, double *partials,
-                         unsigned int *tickets) {
+                         unsigned int *tickets, int pre = 0) {
   using Vec = typename M::Vec;
   using R = typename ScalarOf<Vec>::T;
   const KrylovScalars s = *ks;
@@ -379,17 +385,19 @@ __global__ void k_s_spmv(M mat, KV<typename M::Vec> v, KrylovScalars *ks, double
   const R alpha = (R)s.alpha;
   const Vec *__restrict__ Vn = v.V[nxt];
   const Vec *__restrict__ Rr = v.R;
+  const Vec *__restrict__ Sg = v.S;
   double acc[3] = {0.0, 0.0, 0.0};
   KRYLOV_ROWS(M, i, lane) {
     const int i = (int)i_64;
     const bool live = i < mat.items;
-    Vec part = live ? mat.row_partial(i, lane, [&](int j) { return v_sub_scaled(Rr[j], alpha, Vn[j]); })
-                    : v_zero<Vec>();
+    Vec part = !live ? v_zero<Vec>()
+               : pre ? mat.row_partial(i, lane, [&](int j) { return Sg[j]; })
+                     : mat.row_partial(i, lane, [&](int j) { return v_sub_scaled(Rr[j], alpha, Vn[j]); });
     Vec y = lane_reduce<M::kLanes>(part);
     if (live && lane == 0) {
-      Vec si = v_sub_scaled(Rr[i], alpha, Vn[i]);
+      Vec si = pre ? Sg[i] : v_sub_scaled(Rr[i], alpha, Vn[i]);
       Vec ti = v_mul(v.dinv[i], y);
-      v.S[i] = si;
+      if (!pre) v.S[i] = si;
       v.T[i] = ti;
       acc[0] += v_dot(si, ti);
       acc[1] += v_dot(ti, ti);
@@ -410,6 +418,31 @@ __global__ void k_s_spmv(M mat, KV<typename M::Vec> v, KrylovScalars *ks, double
     }
     *ks = t;
   }
+}
+
+// Row-wise p <- r - beta omega v + beta p and s <- r - alpha v for the pre form above.
+template <class Vec>
+__global__ void k_p_update(int64_t n, KV<Vec> v, const KrylovScalars *ks) {
+  using R = typename ScalarOf<Vec>::T;
+  const KrylovScalars s = *ks;
+  if (!s.active) return;
+  const int cur = s.it & 1, nxt = cur ^ 1;
+  const R beta = (R)s.beta, bw = (R)(s.beta * s.omegaold);
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
+    v.P[nxt][i] = v_pupd(v.R[i], bw, v.V[cur][i], beta, v.P[cur][i]);
+}
+
+template <class Vec>
+__global__ void k_s_update(int64_t n, KV<Vec> v, const KrylovScalars *ks) {
+  using R = typename ScalarOf<Vec>::T;
+  const KrylovScalars s = *ks;
+  if (!s.active) return;
+  const int nxt = (s.it & 1) ^ 1;
+  const R alpha = (R)s.alpha;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
+    v.S[i] = v_sub_scaled(v.R[i], alpha, v.V[nxt][i]);
 }
 
 template <class M>

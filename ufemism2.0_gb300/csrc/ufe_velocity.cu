@@ -3048,9 +3048,12 @@ int32_t solve_csr_device(ufe_ctx *ctx, const DevCSR &A, const double *b, double 
           });
           cudaGraph_t body;
           add_while(g, deps, h, &body);
-          capture_into(s, body, {}, [&]() {
-            k_p_spmv<M1><<<gk, kThreads, 0, s>>>(mat, v, ks, ctx->red.partials, ctx->red.tickets);
-            k_s_spmv<M1><<<gk, kThreads, 0, s>>>(mat, v, ks, ctx->red.partials, ctx->red.tickets);
+          const unsigned gu = (unsigned)pick_blocks(m, kThreads, kMaxReduceBlocks);
+          capture_into(s, body, {}, [&]() {   // p and s row by row, then the SpMVs gather them
+            k_p_update<double><<<gu, kThreads, 0, s>>>(m, v, ks);
+            k_p_spmv<M1><<<gk, kThreads, 0, s>>>(mat, v, ks, ctx->red.partials, ctx->red.tickets, 1);
+            k_s_update<double><<<gu, kThreads, 0, s>>>(m, v, ks);
+            k_s_spmv<M1><<<gk, kThreads, 0, s>>>(mat, v, ks, ctx->red.partials, ctx->red.tickets, 1);
             k_xr<M1><<<gk, kThreads, 0, s>>>(mat, v, ks, ctx->red.partials, ctx->red.tickets, cond);
             UFE_CUDA(cudaGetLastError());
           });
@@ -3081,10 +3084,13 @@ int32_t solve_csr_device(ufe_ctx *ctx, const DevCSR &A, const double *b, double 
         mat, v, ks, rtol, abstol, max_it, 0, ctx->red.partials, ctx->red.tickets, none);
     UFE_CUDA(cudaGetLastError());
     for (;;) {
+      const unsigned gu = (unsigned)pick_blocks(m, kThreads, kMaxReduceBlocks);
       for (int c = 0; c < 8; ++c) {
         unsigned g = krylov_grid(mat, kThreads, grid);
-        k_p_spmv<CsrMat><<<g, kThreads, 0, s>>>(mat, v, ks, ctx->red.partials, ctx->red.tickets);
-        k_s_spmv<CsrMat><<<g, kThreads, 0, s>>>(mat, v, ks, ctx->red.partials, ctx->red.tickets);
+        k_p_update<double><<<gu, kThreads, 0, s>>>(m, v, ks);
+        k_p_spmv<CsrMat><<<g, kThreads, 0, s>>>(mat, v, ks, ctx->red.partials, ctx->red.tickets, 1);
+        k_s_update<double><<<gu, kThreads, 0, s>>>(m, v, ks);
+        k_s_spmv<CsrMat><<<g, kThreads, 0, s>>>(mat, v, ks, ctx->red.partials, ctx->red.tickets, 1);
         k_xr<CsrMat><<<g, kThreads, 0, s>>>(mat, v, ks, ctx->red.partials, ctx->red.tickets, none);
       }
       UFE_CUDA(cudaGetLastError());
