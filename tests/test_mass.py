@@ -210,3 +210,27 @@ def test_gpu_halfar_dome_matches_oracle(pkg, oracle_mod, gpu_lib):
     # different orders), so 50 steps agree to about that, not bitwise
     assert abs(eg - eo) < 1e-4 * eo, (eg, eo)
     assert np.linalg.norm(Hg - Ho) < 1e-6 * np.linalg.norm(Ho)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("method", ["explicit", "semi-implicit"])
+def test_gpu_thickness_minimal_inputs(pkg, oracle_mod, case, gpu_mass, method):
+    """Only the required fields (no mass balance, margin fraction, masks or prescribed thickness;
+    the library takes 0, 1 and none for them) and 'infinite' borders on all four sides."""
+    mesh, f, _, A, Cw = case
+    p = pkg.abi.default_thickness_params(choice_ice_integration_method=method, BC_H_west="infinite",
+                                         BC_H_east="infinite", BC_H_south="infinite", BC_H_north="infinite")
+    if method == "semi-implicit":
+        p.dHi_PETSc_rtol, p.dHi_PETSc_abstol = 1e-13, 0.0
+    g_in = {k: f[k] for k in ("Hi", "Hb", "SL", "u_vav_b", "v_vav_b", "dHi_dt")}
+    q = _fields(g_in, mesh)
+    dto, _ = oracle_mod.Oracle(mesh).calc_dHi_dt(A, Cw, p, q, 2.0)
+    g = gpu_mass.calc_dHi_dt(p, g_in, 2.0)
+    assert g["dt"] == dto
+    if method == "explicit":
+        for k in ("Hi_tplusdt", "dHi_dt", "AMB", "divQ"):
+            np.testing.assert_array_equal(g[k], q[k], err_msg=k)
+    else:
+        np.testing.assert_array_equal(g["divQ"], q["divQ"])
+        rel = np.linalg.norm(g["Hi_tplusdt"] - q["Hi_tplusdt"]) / np.linalg.norm(q["Hi_tplusdt"])
+        assert rel < 1e-10, rel
