@@ -104,13 +104,22 @@ def test_default_thermo_params_match(gpu_lib, pkg):
     assert bytes(p) == bytes(q)
 
 
+def test_default_thickness_params_match(gpu_lib, pkg):
+    p = pkg.abi.ThicknessParams()
+    gpu_lib.ufe_default_thickness_params(C.byref(p))
+    q = pkg.abi.default_thickness_params()
+    assert bytes(p) == bytes(q)
+
+
 def test_struct_layout_matches_header(pkg, tmp_path):
     """Compile a C probe against include/ufe_gpu.h and compare sizes/offsets with ctypes."""
     abi = pkg.abi
     structs = {"ufe_mesh_desc": abi.MeshDesc, "ufe_solver_params": abi.SolverParams, "ufe_ice_state": abi.IceState,
                "ufe_bc_prescribed": abi.BCPrescribed, "ufe_diva_state": abi.DivaState,
                "ufe_solve_stats": abi.SolveStats, "ufe_thermo_params": abi.ThermoParams,
-               "ufe_thermo_columns": abi.ThermoColumns, "ufe_heat_fields": abi.HeatFields}
+               "ufe_thermo_columns": abi.ThermoColumns, "ufe_heat_fields": abi.HeatFields,
+               "ufe_thickness_params": abi.ThicknessParams, "ufe_thickness_fields": abi.ThicknessFields,
+               "ufe_thickness_stats": abi.ThicknessStats}
     lines = ["#include <stdio.h>", "#include <stddef.h>", f'#include "{HEADER}"', "int main(void){"]
     for cname, cls in structs.items():
         lines.append(f'printf("{cname} %zu\\n", sizeof({cname}));')
