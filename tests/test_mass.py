@@ -234,3 +234,26 @@ def test_gpu_thickness_minimal_inputs(pkg, oracle_mod, case, gpu_mass, method):
         np.testing.assert_array_equal(g["divQ"], q["divQ"])
         rel = np.linalg.norm(g["Hi_tplusdt"] - q["Hi_tplusdt"]) / np.linalg.norm(q["Hi_tplusdt"])
         assert rel < 1e-10, rel
+
+
+def test_halfar_solution_is_consistent(pkg):
+    """geometry.halfar (the published similarity solution) checked against itself: the dome's
+    volume is constant in time, and its thickness and shallow-ice velocity satisfy the continuity
+    equation dH/dt = -div(H u) inside the margin (central differences)."""
+    G = pkg.geometry
+    x = np.linspace(-800e3, 800e3, 1601)
+    X, Y = np.meshgrid(x, x)
+    vol = [G.halfar(X, Y, t)[0].sum() * (x[1] - x[0]) ** 2 for t in (0.0, 500.0, 5000.0)]
+    assert max(abs(v - vol[0]) for v in vol) < 2e-3 * vol[0], vol
+    rng = np.random.default_rng(0)
+    r = rng.uniform(50e3, 350e3, 20)
+    th = rng.uniform(0.0, 2 * np.pi, 20)
+    px, py = r * np.cos(th), r * np.sin(th)
+    t, dt, h = 200.0, 0.05, 50.0
+    dHdt = (G.halfar(px, py, t + dt)[0] - G.halfar(px, py, t - dt)[0]) / (2 * dt)
+
+    def flux(qx, qy):
+        H, u, v = G.halfar(qx, qy, t)
+        return H * u, H * v
+    div = ((flux(px + h, py)[0] - flux(px - h, py)[0]) + (flux(px, py + h)[1] - flux(px, py - h)[1])) / (2 * h)
+    np.testing.assert_allclose(dHdt, -div, rtol=2e-3, atol=1e-6)
